@@ -1,0 +1,207 @@
+/*
+ * peridem_gb300.h -- C-ABI of the GB300 explicit-step engine for PeriDEM.
+ *
+ * PeriDEM (DavoodDamircheli/PeriDEM) runs its time loop behind two boundaries:
+ *   1. a process/file boundary: `simulate3d -c <main.conf> -i <setup.h5> -o <outdir>`
+ *      (run/simulate3d.cpp:86-105) reading the `main.conf` grammar
+ *      (src/read/read_config.h:170-435) and the setup schema of
+ *      src/read/load_hdf5.h:41-181, writing plotinfo.h5 / tc_%05u.h5 / wall_%05u.h5
+ *      (src/particle/timeloop.h:321-350, 801-953);
+ *   2. an in-process C++ boundary:
+ *      run_timeloop<dim>(vector<ParticleN<dim>>&, Timeloop, Contact, RectWall<dim>, ConfigVal)
+ *      (src/particle/timeloop.h:231-965), which mutates the particles in place.
+ * This header replaces both with plain C entry points: no C++ exceptions and no torch
+ * types cross it; every function returns an int status (PD_OK == 0, negative on error).
+ *
+ * Ownership: device memory belongs to the handle; caller buffers are copied and never
+ * retained. A handle is not thread-safe. Work is enqueued on the handle's CUDA stream.
+ */
+#ifndef PERIDEM_GB300_H
+#define PERIDEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------------- */
+#define PD_OK 0
+#define PD_EINVAL (-1)    /* bad argument / inconsistent setup arrays               */
+#define PD_ECUDA (-2)     /* a CUDA runtime call failed (no GPU, launch error, ...)  */
+#define PD_ENOMEM (-3)    /* device or host allocation failed                       */
+#define PD_EIO (-4)       /* file missing, unreadable or not in the expected schema */
+#define PD_ETIMEOUT (-5)  /* pd_sync: the bounded wait ran out                      */
+#define PD_EDEVICE (-6)   /* the device raised its error word (NaN, list overflow)  */
+#define PD_ECONFIG (-7)   /* config file could not be opened                        */
+#define PD_ESTATE (-8)    /* call not valid in the handle's current state           */
+
+/* ---- precision forms ------------------------------------------------------------ */
+#define PD_FP64 0         /* plain FP64, same operation order as the reference        */
+#define PD_FP32C 1        /* FP32 bond forces, cancellation-free stretch, Kahan sums  */
+
+/* ---- device error word bits (pd_device_errors) ----------------------------------- */
+#define PD_DERR_NONFINITE 1u      /* a NaN/Inf force density was produced             */
+#define PD_DERR_CAND_OVERFLOW 2u  /* per-node contact candidate list overflowed       */
+#define PD_DERR_CONTACT_OVERFLOW 4u /* more in-range contacts than the per-node cap   */
+
+/*
+ * pd_config: the run parameters of `main.conf`. Field names, meanings, defaults and
+ * sentinels (-1 = "not set" for the contact overrides and new_snot, -999 = "not set"
+ * for wall positions) follow ConfigVal (src/read/read_config.h:14-167). Booleans are
+ * int32 (0/1).
+ */
+typedef struct pd_config {
+  uint32_t timesteps;                 /* default 8000 */
+  uint32_t modulo;                    /* default 100  */
+  double dt;                          /* default 0.02/1e5 */
+  int32_t is_parallel;
+  int32_t do_resume, wall_resume;
+  uint32_t resume_ind;                /* default 50 */
+  int32_t save_file;                  /* default 1 */
+  int32_t enable_fracture;            /* default 0 */
+  int32_t nl_bdry_only;               /* default 0 */
+  int32_t allow_damping, allow_friction; /* default 1, 1 */
+  double normal_stiffness, damping_ratio, friction_coefficient; /* -1: use setup file */
+  double new_snot;                    /* -1: keep per-particle snot */
+  int32_t self_contact;               /* default 1 */
+  double self_contact_rad;            /* -1 (parsed, unused on the path) */
+  int32_t enable_cohesion;            /* parsed, unused on the path */
+  double cohesion_scaling;
+  int32_t enable_torque;
+  int32_t set_torque_timestep, set_fracture_timestep, set_self_contact_timestep;
+  int32_t set_zero_wall_speed_timestep, set_damping_timestep;
+  int32_t set_movable_index, set_movable_timestep;
+  int32_t set_stoppable_index, set_stoppable_timestep;
+  int32_t reset_partzero_y;
+  uint32_t reset_partzero_y_timestep;
+  double wheel_rad;
+  int32_t particle_w_fixed_velocity, set_fix_velocity_timestep;
+  int32_t fix_velocity_angular;
+  double prescribed_angular_vel;
+  int32_t fix_velocity_mean_x;
+  double prescribed_velocity_mean_x;
+  double wall_left, wall_right, wall_top, wall_bottom;            /* 2D names, -999 */
+  double wall_x_min, wall_y_min, wall_z_min, wall_x_max, wall_y_max, wall_z_max;
+  double speed_wall_left, speed_wall_right, speed_wall_top, speed_wall_bottom;
+  double speed_wall_x_min, speed_wall_y_min, speed_wall_z_min;
+  double speed_wall_x_max, speed_wall_y_max, speed_wall_z_max;
+  int32_t brazil;
+  int32_t brazil_reset_wall_bottom_freq, brazil_nonzero_wall_bottom_speed_freq;
+  double brazil_reset_wall_bottom_y;
+  int32_t forcefield_type;
+  double forcefield_scaling;
+  int32_t gradient_extforce;
+  uint32_t extforce_maxstep;
+  int32_t compute_wall_reaction;
+  char setup_filename[1024];          /* default "data/hdf5/all.h5"  (-i) */
+  char output_dir[1024];              /* default "output/hdf5/"      (-o) */
+  uint32_t n_unknown_keys;            /* keys the parser reported as "Wrong config name" */
+} pd_config;
+
+/*
+ * pd_setup_arrays: the setup schema (exp_dict.py:2119-2185, read by
+ * src/read/load_hdf5.h:41-181) as caller-owned host arrays. Particles are concatenated
+ * in file order (P_00000, P_00001, ...): particle p owns nodes
+ * [node_offset[p], node_offset[p+1]) of every per-node array. Connectivity rows use
+ * particle-local node indices (i < j, sorted, as written by exp_dict.py:567).
+ */
+typedef struct pd_setup_arrays {
+  uint32_t n_particles;
+  const uint64_t *node_offset;      /* n_particles+1 */
+  const double *pos;                /* N*3 */
+  const double *vol;                /* N   */
+  const double *disp, *vel, *acc;   /* N*3 initial data */
+  const double *extforce;           /* N*3 */
+  const uint64_t *conn_offset;      /* n_particles+1, rows of Connectivity */
+  const uint32_t *conn;             /* M*2 local pairs */
+  const uint64_t *bdry_offset;      /* n_particles+1 (may be NULL: no bdry lists) */
+  const uint32_t *bdry;             /* local node ids */
+  const uint64_t *clamped_offset;   /* n_particles+1 (may be NULL) */
+  const uint32_t *clamped;          /* local node ids */
+  const double *delta, *rho, *cnot, *snot, *torque_val; /* per particle */
+  const int32_t *movable, *breakable, *stoppable;        /* per particle */
+  const uint32_t *torque_axis;                           /* per particle */
+  double contact_radius, normal_stiffness, damping_ratio, friction_coefficient;
+  int32_t allow_wall;
+  int32_t n_geom_wall;              /* 6 in 3D; 1 means "no wall geometry" */
+  double geom_wall_info[6];         /* x_min y_min z_min x_max y_max z_max */
+} pd_setup_arrays;
+
+typedef struct pd_sim pd_sim;
+
+/* Per-step counters read back by pd_get_stats. */
+typedef struct pd_stats {
+  uint64_t step;                 /* the step counter t of the last completed step     */
+  uint64_t live_bonds;           /* live directed bonds at the start of the last step */
+  uint64_t pairwise_computations;/* particle pairs evaluated, summed since last read  */
+  uint64_t contacts;             /* node-node contact pairs applied in the last step  */
+  uint64_t rebuilds;             /* contact broad-phase rebuilds so far               */
+  uint32_t device_errors;        /* PD_DERR_* bits                                    */
+} pd_stats;
+
+/* ---- configuration (replaces ConfigVal + read_file, read_config.h:102-435) -------- */
+int pd_config_default(pd_config *cfg);
+/* Parses `key = value` lines (whitespace removed, '#' comments). Unknown keys print
+ * "[Error]: Wrong config name: <key> !!" to stderr and are counted, like read_config.h:425. */
+int pd_config_read(const char *path, pd_config *cfg);
+
+/* ---- simulation handles ----------------------------------------------------------- */
+/* Copies the arrays to the device, applies the config the way simulate3d.cpp:125-139
+ * and the apply_config methods (timeloop.h:184-225, contact.h:151-179, 325-372) do,
+ * builds the bond lists (load_hdf5.h:27-37 + particle2.h:241-257) and initial AABBs
+ * (timeloop.h:389-393). `precision` is PD_FP64 or PD_FP32C. */
+int pd_create_from_arrays(const pd_setup_arrays *setup, const pd_config *cfg,
+                          int precision, pd_sim **out);
+/* Reads main.conf + setup.h5 and prepares outdir, like simulate3d -c -i -o. */
+int pd_open(const char *conf, const char *setup_h5, const char *outdir, int precision,
+            pd_sim **out);
+/* Runs the whole configured time loop with saves (run_timeloop, timeloop.h:395-965). */
+int pd_run(pd_sim *sim);
+/* Enqueues `nsteps` explicit steps (timeloop.h:395-797) on the handle's stream. */
+int pd_step(pd_sim *sim, uint32_t nsteps);
+/* Bounded wait for the handle's stream; PD_ETIMEOUT when timeout_ms passes first,
+ * PD_EDEVICE when the device error word is set. timeout_ms < 0 waits without limit. */
+int pd_sync(pd_sim *sim, int timeout_ms);
+/* Uses an external CUDA stream (cudaStream_t passed as void*; NULL = handle's own). */
+int pd_set_stream(pd_sim *sim, void *cuda_stream);
+
+/* ---- state access (all arrays N*3 in particle file order; any pointer may be NULL) -- */
+int pd_num_nodes(const pd_sim *sim, uint64_t *n_nodes, uint32_t *n_particles);
+int pd_get_state(pd_sim *sim, double *curpos, double *vel, double *acc, double *force);
+int pd_get_disp(pd_sim *sim, double *disp);
+/* Overwrites the kinematic state (resume from a frame, timeloop.h:262-312). */
+int pd_set_state(pd_sim *sim, const double *disp, const double *vel, const double *acc);
+/* Connectivity (local i<q pairs of live bonds) of one particle, as NbdArr2conn
+ * (timeloop.h:20-44). With pairs == NULL only *n is returned. */
+int pd_get_connectivity(pd_sim *sim, uint32_t particle, uint32_t *pairs, uint64_t cap,
+                        uint64_t *n);
+/* Wall geometry lrtb() (6) and reaction (6*3, x_min..z_max order of get_reaction). */
+int pd_get_wall(pd_sim *sim, double *wall_info, double *reaction);
+/* Particle AABBs as used by the next step (get_minmax, contact.h:1187-1225): P*6. */
+int pd_get_aabb(pd_sim *sim, double *lrtb);
+int pd_get_stats(pd_sim *sim, pd_stats *stats);
+/* Writes tc_%05u.h5 and wall_%05u.h5 for `counter` into the output dir. */
+int pd_write_frame(pd_sim *sim, uint32_t counter);
+/* Text of the last error on this handle (never NULL). */
+const char *pd_last_error(const pd_sim *sim);
+/* Text of the last error of a call that could not return a handle. */
+const char *pd_global_error(void);
+int pd_close(pd_sim *sim);
+
+/* Tuning knobs: contact skin as a fraction of the contact radius (<= 0 keeps it), per-node
+ * candidate capacity (0 keeps it, at most 64), threads per block (<= 0 keeps it), per-step
+ * statistics on/off (< 0 keeps it; on adds the pair-count kernel), CUDA-graph replay on/off. */
+int pd_set_tuning(pd_sim *sim, double skin_frac, uint32_t cand_cap, int threads_per_block,
+                  int stats, int use_graphs);
+/* Clears the device error word after the caller has handled it. */
+int pd_clear_device_errors(pd_sim *sim);
+
+/* Algorithmic byte count of one step (4.125 B per live directed bond + 224 B per node). */
+double pd_step_bytes(const pd_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PERIDEM_GB300_H */

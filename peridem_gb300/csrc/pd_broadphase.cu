@@ -1,0 +1,222 @@
+// pd_broadphase.cu -- contact broad phase: hashed cell list built by counting sort, and
+// per-node candidate lists (global indices, ascending) of the nodes of the same simulation
+// within contact radius + skin. The reference tests every node pair of every particle
+// pair whose AABBs intersect (timeloop.h:637-651, contact.h:754-769); the exact distance
+// test of the reference is still made for every candidate in every step (pd_kernels.cu),
+// so the lists only need to be a superset of the pairs within the contact radius.
+//
+// The lists are rebuilt only when the accumulated bound on node movement since the last
+// build could exceed half the skin: every kernel here first reads the rebuild flag set by
+// k_bp_decide and returns at once when no rebuild is due, so the whole sequence can sit
+// in a CUDA graph that replays every step.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pd_engine.h"
+#include "pd_math.cuh"
+
+namespace pdg {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanBlock = kScanThreads * kScanPer;
+constexpr int kMaxCand = 64;
+
+__device__ __forceinline__ uint32_t cell_hash(long long cx, long long cy, long long cz, uint32_t sim,
+                                              uint32_t mask) {
+  unsigned long long h = (unsigned long long)cx * 0x9E3779B97F4A7C15ull;
+  h ^= (unsigned long long)cy * 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
+  h ^= (unsigned long long)cz * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
+  h ^= (unsigned long long)sim * 0x27D4EB2F165667C5ull;
+  h ^= h >> 31;
+  h *= 0x7FB5D329728EA185ull;
+  h ^= h >> 27;
+  return (uint32_t)h & mask;
+}
+
+__device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double cell, long long &cx,
+                                          long long &cy, long long &cz, double &x, double &y, double &z) {
+  x = v.pos[n] + v.disp[n];
+  y = v.pos[n + v.Ncap] + v.disp[n + v.Ncap];
+  z = v.pos[n + 2 * v.Ncap] + v.disp[n + 2 * v.Ncap];
+  cx = (long long)floor(x / cell);
+  cy = (long long)floor(y / cell);
+  cz = (long long)floor(z / cell);
+}
+
+// Decide whether this step rebuilds; also zero the wall reactions of every simulation
+// (Wall.setzero_reaction at the top of each step, timeloop.h:397).
+__global__ void k_bp_decide(DevView v, double half_skin) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    DevCounters &c = *v.cnt;
+    double stepmax = __longlong_as_double((long long)c.stepmax_bits);
+    c.rebuild = (c.moved + stepmax > half_skin) ? 1u : 0u;
+  }
+  for (uint32_t s = t; s < v.S; s += gridDim.x * blockDim.x)
+    for (int k = 0; k < 18; ++k) v.ss[s].react[k] = 0.0;
+}
+
+__global__ void k_bp_clear(DevView v, uint32_t *count, uint64_t T) {
+  if (!v.cnt->rebuild) return;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += (uint64_t)gridDim.x * blockDim.x)
+    count[i] = 0;
+}
+
+__global__ void k_bp_count(DevView v, uint32_t *count, uint32_t *key, uint32_t *slot, uint32_t mask) {
+  if (!v.cnt->rebuild) return;
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t sim = v.parts[v.pid[n]].sim;
+  long long cx, cy, cz;
+  double x, y, z;
+  node_cell(v, n, v.sp[sim].cell, cx, cy, cz, x, y, z);
+  uint32_t kk = cell_hash(cx, cy, cz, sim, mask);
+  key[n] = kk;
+  slot[n] = atomicAdd(&count[kk], 1u);
+}
+
+// exclusive scan, phase 1: per-block scan, block totals
+__global__ void k_scan_blocks(const DevView v, const uint32_t *in, uint32_t *out, uint32_t *sums, uint64_t T) {
+  if (!v.cnt->rebuild) return;
+  __shared__ uint32_t sh[kScanThreads];
+  const uint64_t base = (uint64_t)blockIdx.x * kScanBlock + (uint64_t)threadIdx.x * kScanPer;
+  uint32_t vals[kScanPer];
+  uint32_t tot = 0;
+  for (int i = 0; i < kScanPer; ++i) {
+    uint64_t idx = base + i;
+    vals[i] = idx < T ? in[idx] : 0u;
+    tot += vals[i];
+  }
+  sh[threadIdx.x] = tot;
+  __syncthreads();
+  for (int o = 1; o < kScanThreads; o <<= 1) {
+    uint32_t add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0u;
+    __syncthreads();
+    sh[threadIdx.x] += add;
+    __syncthreads();
+  }
+  uint32_t run = sh[threadIdx.x] - tot;  // exclusive prefix of this thread
+  for (int i = 0; i < kScanPer; ++i) {
+    uint64_t idx = base + i;
+    if (idx < T) out[idx] = run;
+    run += vals[i];
+  }
+  if (threadIdx.x == kScanThreads - 1) sums[blockIdx.x] = sh[threadIdx.x];
+}
+
+// phase 2: one block scans the block totals in place (exclusive)
+__global__ void k_scan_top(const DevView v, uint32_t *sums, uint32_t nb) {
+  if (!v.cnt->rebuild) return;
+  __shared__ uint32_t sh[kScanThreads];
+  const uint32_t per = (nb + kScanThreads - 1) / kScanThreads;
+  const uint32_t b0 = threadIdx.x * per;
+  uint32_t tot = 0;
+  for (uint32_t i = 0; i < per; ++i)
+    if (b0 + i < nb) tot += sums[b0 + i];
+  sh[threadIdx.x] = tot;
+  __syncthreads();
+  for (int o = 1; o < kScanThreads; o <<= 1) {
+    uint32_t add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0u;
+    __syncthreads();
+    sh[threadIdx.x] += add;
+    __syncthreads();
+  }
+  uint32_t run = sh[threadIdx.x] - tot;
+  for (uint32_t i = 0; i < per; ++i) {
+    if (b0 + i < nb) {
+      uint32_t x = sums[b0 + i];
+      sums[b0 + i] = run;
+      run += x;
+    }
+  }
+}
+
+// phase 3: add block offsets
+__global__ void k_scan_add(const DevView v, uint32_t *out, const uint32_t *sums, uint64_t T) {
+  if (!v.cnt->rebuild) return;
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < T) out[i] += sums[i / kScanBlock];
+}
+
+__global__ void k_bp_scatter(DevView v, const uint32_t *start, const uint32_t *key, const uint32_t *slot,
+                             uint32_t *sorted) {
+  if (!v.cnt->rebuild) return;
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  sorted[start[key[n]] + slot[n]] = (uint32_t)n;
+}
+
+__global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t *start, const uint32_t *sorted,
+                                uint32_t mask, uint32_t *cand, uint16_t *cand_n, uint32_t cap) {
+  if (!v.cnt->rebuild) return;
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t sim = v.parts[v.pid[n]].sim;
+  const DevSimParams &sp = v.sp[sim];
+  long long cx, cy, cz;
+  double x, y, z;
+  node_cell(v, n, sp.cell, cx, cy, cz, x, y, z);
+  uint32_t list[kMaxCand];
+  int cnt = 0;
+  bool overflow = false;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        uint32_t kk = cell_hash(cx + dx, cy + dy, cz + dz, sim, mask);
+        uint32_t b = start[kk], e = b + count[kk];
+        for (uint32_t it = b; it < e; ++it) {
+          uint32_t m = sorted[it];
+          if (m == n) continue;
+          if (v.parts[v.pid[m]].sim != sim) continue;
+          double mx = v.pos[m] + v.disp[m];
+          double my = v.pos[m + v.Ncap] + v.disp[m + v.Ncap];
+          double mz = v.pos[m + 2 * v.Ncap] + v.disp[m + 2 * v.Ncap];
+          double ddx = mx - x, ddy = my - y, ddz = mz - z;
+          if (ddx * ddx + ddy * ddy + ddz * ddz > sp.cand_r2) continue;
+          // insert keeping ascending order; drop duplicates (hash collisions can make two
+          // stencil cells share a bucket)
+          int pos = cnt;
+          while (pos > 0 && list[pos - 1] > m) --pos;
+          if (pos > 0 && list[pos - 1] == m) continue;
+          if (cnt >= (int)cap) {
+            overflow = true;
+            continue;
+          }
+          for (int q = cnt; q > pos; --q) list[q] = list[q - 1];
+          list[pos] = m;
+          ++cnt;
+        }
+      }
+  uint32_t *out = cand + n * cap;
+  for (int i = 0; i < cnt; ++i) out[i] = list[i];
+  cand_n[n] = (uint16_t)cnt;
+  if (overflow) atomicOr(&v.cnt->err, PD_DERR_CAND_OVERFLOW);
+}
+
+}  // namespace
+
+void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s) {
+  const uint64_t T = 1ull << bp.table_bits;
+  const uint32_t mask = (uint32_t)(T - 1);
+  const uint32_t nb = (uint32_t)((T + kScanBlock - 1) / kScanBlock);
+  const uint64_t nblk = (v.N + 255) / 256;
+  k_bp_clear<<<1024, 256, 0, s>>>(v, bp.count, T);
+  if (nblk) k_bp_count<<<(unsigned)nblk, 256, 0, s>>>(v, bp.count, bp.key, bp.slot, mask);
+  k_scan_blocks<<<nb, kScanThreads, 0, s>>>(v, bp.count, bp.start, bp.block_sums, T);
+  k_scan_top<<<1, kScanThreads, 0, s>>>(v, bp.block_sums, nb);
+  k_scan_add<<<(unsigned)((T + 255) / 256), 256, 0, s>>>(v, bp.start, bp.block_sums, T);
+  if (nblk) {
+    k_bp_scatter<<<(unsigned)nblk, 256, 0, s>>>(v, bp.start, bp.key, bp.slot, bp.sorted);
+    k_bp_candidates<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask,
+                                                                  bp.cand, bp.cand_n, bp.cand_cap);
+  }
+}
+
+void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s) {
+  k_bp_decide<<<1, 128, 0, s>>>(v, half_skin);
+}
+
+}  // namespace pdg

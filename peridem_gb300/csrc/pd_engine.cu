@@ -1,0 +1,740 @@
+// pd_engine.cu -- host side of the explicit-step engine: builds the HBM layout described in
+// pd_engine.h from one or more simulations, captures one step as a CUDA graph and replays
+// it, and reads results back in the reference's shapes.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <thread>
+
+#include "pd_engine.h"
+#include "pd_math.cuh"
+
+namespace pdg {
+
+namespace {
+inline uint64_t round_up(uint64_t x, uint64_t m) { return (x + m - 1) / m * m; }
+}  // namespace
+
+Engine::~Engine() {
+  for (int i = 0; i < 2; ++i)
+    if (graph_[i]) cudaGraphExecDestroy(graph_[i]);
+  for (void *p : allocs_) cudaFree(p);
+  if (own_stream_ && capture_stream_) cudaStreamDestroy(capture_stream_);
+}
+
+int Engine::check(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return PD_OK;
+  err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA;
+}
+
+#define PD_TRY(expr)             \
+  do {                           \
+    int _rc = (expr);            \
+    if (_rc != PD_OK) return _rc; \
+  } while (0)
+
+template <typename T>
+static int dalloc(Engine *E, std::vector<void *> &allocs, T **p, uint64_t count, std::string &err) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    err = std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " B): " + cudaGetErrorString(e);
+    (void)E;
+    return e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA;
+  }
+  allocs.push_back((void *)*p);
+  return PD_OK;
+}
+
+DevView Engine::view(int cur) const {
+  DevView v;
+  std::memset(&v, 0, sizeof(v));
+  v.N = N_;
+  v.Ncap = Ncap_;
+  v.P = P_;
+  v.S = S_;
+  v.pos = d_pos_;
+  v.disp = d_disp_;
+  v.vel_in = d_vel_[cur];
+  v.vel_out = d_vel_[cur ^ 1];
+  v.acc = d_acc_;
+  v.force = d_force_;
+  v.ext = d_ext_;
+  v.vol = d_vol_;
+  v.pid = d_pid_;
+  v.bdry = d_bdry_;
+  v.slice_ptr = d_slice_ptr_;
+  v.deg = d_deg_;
+  v.col = d_col_;
+  v.mask = d_mask_;
+  v.bxi = d_bxi_;
+  v.bxin = d_bxin_;
+  v.brxin = d_brxin_;
+  v.E = E_;
+  v.pos32 = d_pos32_;
+  v.disp32 = d_disp32_;
+  v.anchor = d_anchor_;
+  v.break_band = 1e-4;
+  v.parts = d_parts_;
+  v.lrtb = d_lrtb_;
+  v.lrtb_next = d_lrtb_next_;
+  v.sp = d_sp_;
+  v.ss = d_ss_;
+  v.cand = bp_.cand;
+  v.cand_n = bp_.cand_n;
+  v.cand_cap = bp_.cand_cap;
+  v.centroid = d_centroid_;
+  v.cnt = d_cnt_;
+  v.stats = stats_ ? 1 : 0;
+  return v;
+}
+
+// Host mirror of the sticky toggles of timeloop.h:405-464 for the first step.
+static void host_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t) {
+  if (sp.set_torque_ts != -1 && t == (uint32_t)sp.set_torque_ts) st.torque = 1;
+  if (sp.set_fracture_ts != -1 && t == (uint32_t)sp.set_fracture_ts) st.fracture = 1;
+  if (sp.set_self_contact_ts != -1 && t == (uint32_t)sp.set_self_contact_ts) st.self_contact = 1;
+  if (sp.set_damping_ts != -1 && t == (uint32_t)sp.set_damping_ts) st.damping = 1;
+  if (sp.set_zero_wall_speed_ts != -1 && t == (uint32_t)sp.set_zero_wall_speed_ts)
+    for (int c = 0; c < 6; ++c) st.spd[c] = 0;
+  if (sp.gradient_extforce) {
+    double sc = (double)t / (double)sp.extforce_maxstep;
+    if (sc > 1) sc = 1;
+    st.extf_scale = sc;
+  }
+}
+
+int Engine::init(std::vector<HostSim> &sims, int precision) {
+  sims_.swap(sims);
+  precision_ = precision;
+  S_ = (uint32_t)sims_.size();
+  P_ = 0;
+  N_ = 0;
+  for (auto &s : sims_) {
+    P_ += s.np;
+    N_ += s.node_offset[s.np];
+  }
+  if (N_ == 0 || P_ == 0) {
+    err = "empty setup";
+    return PD_EINVAL;
+  }
+  if (N_ >= 0xFFFFFFF0ull) {
+    err = "too many nodes for 32-bit node indices";
+    return PD_EINVAL;
+  }
+  Ncap_ = round_up(N_, 32);
+  nslices_ = Ncap_ / 32;
+  PD_TRY(check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate"));
+  own_stream_ = true;
+  capture_stream_ = stream_;
+  return alloc_and_upload();
+}
+
+int Engine::build_bonds() {
+  // conn2NArr (load_hdf5.h:27-37): for every Connectivity row (i, j) push j onto row i and
+  // i onto row j; rows keep that push order.
+  std::vector<uint32_t> deg(Ncap_, 0);
+  uint64_t gnode = 0;
+  for (auto &s : sims_) {
+    for (uint32_t p = 0; p < s.np; ++p) {
+      uint64_t g0 = gnode + s.node_offset[p];
+      uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
+      for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
+        uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
+        if (i >= nloc || j >= nloc) {
+          err = "Connectivity index out of range in particle " + std::to_string(p);
+          return PD_EINVAL;
+        }
+        deg[g0 + i]++;
+        deg[g0 + j]++;
+      }
+    }
+    gnode += s.node_offset[s.np];
+  }
+  uint32_t maxdeg = 0;
+  for (uint64_t n = 0; n < N_; ++n) maxdeg = std::max(maxdeg, deg[n]);
+  if (maxdeg > 65535) {
+    err = "node degree above 65535";
+    return PD_EINVAL;
+  }
+  h_deg_.assign(Ncap_, 0);
+  for (uint64_t n = 0; n < Ncap_; ++n) h_deg_[n] = (uint16_t)deg[n];
+  h_slice_ptr_.assign(nslices_ + 1, 0);
+  for (uint64_t s = 0; s < nslices_; ++s) {
+    uint32_t w = 0;
+    for (int l = 0; l < 32; ++l) w = std::max(w, deg[s * 32 + l]);
+    h_slice_ptr_[s + 1] = h_slice_ptr_[s] + 32ull * w;
+  }
+  E_ = h_slice_ptr_[nslices_];
+  std::vector<uint32_t> col(std::max<uint64_t>(E_, 1), kNoCol);
+  std::vector<uint32_t> mask(std::max<uint64_t>(E_ / 32, 1), 0u);
+  std::vector<uint32_t> fill(Ncap_, 0);
+  gnode = 0;
+  for (auto &s : sims_) {
+    for (uint32_t p = 0; p < s.np; ++p) {
+      uint64_t g0 = gnode + s.node_offset[p];
+      for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
+        uint64_t a = g0 + s.conn[2 * l], b = g0 + s.conn[2 * l + 1];
+        uint64_t ea = h_slice_ptr_[a >> 5] + 32ull * fill[a] + (a & 31);
+        col[ea] = (uint32_t)b;
+        mask[(h_slice_ptr_[a >> 5] >> 5) + fill[a]] |= 1u << (a & 31);
+        fill[a]++;
+        uint64_t eb = h_slice_ptr_[b >> 5] + 32ull * fill[b] + (b & 31);
+        col[eb] = (uint32_t)a;
+        mask[(h_slice_ptr_[b >> 5] >> 5) + fill[b]] |= 1u << (b & 31);
+        fill[b]++;
+      }
+    }
+    gnode += s.node_offset[s.np];
+  }
+  initial_bonds_ = 0;
+  for (uint64_t n = 0; n < N_; ++n) initial_bonds_ += deg[n];
+  PD_TRY(dalloc(this, allocs_, &d_slice_ptr_, nslices_ + 1, err));
+  PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));
+  PD_TRY(dalloc(this, allocs_, &d_col_, col.size(), err));
+  PD_TRY(dalloc(this, allocs_, &d_mask_, mask.size(), err));
+  PD_TRY(check(cudaMemcpy(d_slice_ptr_, h_slice_ptr_.data(), (nslices_ + 1) * 8, cudaMemcpyHostToDevice), "upload slice_ptr"));
+  PD_TRY(check(cudaMemcpy(d_deg_, h_deg_.data(), Ncap_ * 2, cudaMemcpyHostToDevice), "upload deg"));
+  PD_TRY(check(cudaMemcpy(d_col_, col.data(), col.size() * 4, cudaMemcpyHostToDevice), "upload col"));
+  PD_TRY(check(cudaMemcpy(d_mask_, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice), "upload mask"));
+  return PD_OK;
+}
+
+int Engine::alloc_and_upload() {
+  const uint64_t C = Ncap_;
+  std::vector<double> pos(3 * C, 0.0), disp(3 * C, 0.0), vel(3 * C, 0.0), acc(3 * C, 0.0), ext(3 * C, 0.0);
+  std::vector<double> vol(C, 0.0);
+  h_pid_.assign(C, 0);
+  std::vector<uint8_t> bdry(C, 0);
+  std::vector<DevPart> parts(P_);
+  std::vector<DevSimParams> sps(S_);
+  std::vector<DevSimState> sss(S_);
+  std::vector<uint32_t> clamped_ptr(P_ + 1, 0), clamped_list;
+  h_g0_.assign(P_, 0);
+  uint64_t gnode = 0;
+  uint32_t gpart = 0;
+  torque_possible_ = false;
+  double min_half_skin = 1e300;
+  for (uint32_t si = 0; si < S_; ++si) {
+    HostSim &s = sims_[si];
+    const pd_config &cf = s.cfg;
+    const uint64_t ns = s.node_offset[s.np];
+    for (uint64_t k = 0; k < ns; ++k) {
+      uint64_t g = gnode + k;
+      for (int c = 0; c < 3; ++c) {
+        pos[c * C + g] = s.pos[3 * k + c];
+        disp[c * C + g] = s.disp[3 * k + c];
+        vel[c * C + g] = s.vel[3 * k + c];
+        acc[c * C + g] = s.acc[3 * k + c];
+        ext[c * C + g] = s.ext[3 * k + c];
+      }
+      vol[g] = s.vol[k];
+    }
+    for (uint32_t p = 0; p < s.np; ++p) {
+      uint32_t gp = gpart + p;
+      DevPart &P = parts[gp];
+      P.g0 = (uint32_t)(gnode + s.node_offset[p]);
+      P.n = (uint32_t)(s.node_offset[p + 1] - s.node_offset[p]);
+      P.sim = si;
+      P.taxis = s.taxis[p];
+      P.rho = s.rho[p];
+      P.irho = 1 / s.rho[p];
+      P.cnot = s.cnot[p];
+      P.snot = (cf.new_snot != -1) ? cf.new_snot : s.snot[p];  // timeloop.h:314-318
+      P.tval = s.tval[p];
+      P.movable = s.movable[p];
+      P.breakable = s.breakable[p];
+      P.stoppable = s.stoppable[p];
+      P.break_bonds = 1;  // simulate3d.cpp:137-139
+      if (P.n == 0) {
+        err = "particle " + std::to_string(p) + " has no nodes";
+        return PD_EINVAL;
+      }
+      for (int c = 0; c < 3; ++c) P.anchor_pos[c] = pos[c * C + P.g0];
+      h_g0_[gp] = P.g0;
+      for (uint32_t k = 0; k < P.n; ++k) h_pid_[P.g0 + k] = gp;
+      if (!s.bdry_offset.empty())
+        for (uint64_t l = s.bdry_offset[p]; l < s.bdry_offset[p + 1]; ++l) bdry[P.g0 + s.bdry[l]] = 1;
+      clamped_ptr[gp + 1] = clamped_ptr[gp];
+      if (!s.clamped_offset.empty())
+        for (uint64_t l = s.clamped_offset[p]; l < s.clamped_offset[p + 1]; ++l) {
+          clamped_list.push_back(P.g0 + s.clamped[l]);
+          clamped_ptr[gp + 1]++;
+        }
+    }
+    // Contact: setup values, then Contact::apply_config overrides (contact.h:151-179)
+    DevSimParams &sp = sps[si];
+    std::memset(&sp, 0, sizeof(sp));
+    double Kn = s.Kn, zeta = s.zeta, mu = s.mu;
+    if (cf.damping_ratio != -1) zeta = cf.damping_ratio;
+    if (cf.friction_coefficient != -1) mu = cf.friction_coefficient;
+    if (cf.normal_stiffness != -1) Kn = cf.normal_stiffness;
+    sp.dt = cf.dt;
+    sp.hdt2 = (cf.dt * cf.dt) * 0.5;
+    sp.hdt = 0.5 * cf.dt;
+    sp.Rc = s.Rc;
+    sp.Kn = Kn;
+    sp.sc = Kn * s.Rc;
+    sp.zeta2 = 2 * zeta;
+    sp.mu = mu;
+    sp.pi3 = M_PI / 3;
+    sp.pi4 = M_PI / 4;
+    const double skin = bp_.skin_frac * s.Rc;
+    const double rcand = (s.Rc + skin) * (1.0 + 1e-9);
+    sp.cell = rcand * (1.0 + 1e-9);
+    sp.cand_r2 = rcand * rcand;
+    min_half_skin = std::min(min_half_skin, 0.5 * skin);
+    sp.nl_bdry_only = cf.nl_bdry_only;
+    sp.compute_wall_reaction = cf.compute_wall_reaction;
+    sp.gradient_extforce = cf.gradient_extforce;
+    sp.allow_wall = s.allow_wall ? 1 : 0;
+    sp.extforce_maxstep = cf.extforce_maxstep;
+    sp.set_torque_ts = cf.set_torque_timestep;
+    sp.set_fracture_ts = cf.set_fracture_timestep;
+    sp.set_self_contact_ts = cf.set_self_contact_timestep;
+    sp.set_damping_ts = cf.set_damping_timestep;
+    sp.set_zero_wall_speed_ts = cf.set_zero_wall_speed_timestep;
+    sp.set_movable_index = cf.set_movable_index;
+    sp.set_movable_ts = cf.set_movable_timestep;
+    sp.set_stoppable_index = cf.set_stoppable_index;
+    sp.set_stoppable_ts = cf.set_stoppable_timestep;
+    sp.p0 = gpart;
+    sp.np = s.np;
+    sp.node0 = gnode;
+    sp.nnodes = ns;
+    // Wall: load_wall<3> then RectWall::apply_config (contact.h:325-372)
+    DevSimState &st = sss[si];
+    std::memset(&st, 0, sizeof(st));
+    for (int c = 0; c < 6; ++c) st.wall[c] = (s.n_geom_wall != 1) ? s.geom[c] : 0.0;
+    if (cf.wall_top != -999) st.wall[5] = cf.wall_top;
+    if (cf.wall_right != -999) st.wall[4] = cf.wall_right;
+    if (cf.wall_x_min != -999) st.wall[0] = cf.wall_x_min;
+    if (cf.wall_y_min != -999) st.wall[1] = cf.wall_y_min;
+    if (cf.wall_z_min != -999) st.wall[2] = cf.wall_z_min;
+    if (cf.wall_x_max != -999) st.wall[3] = cf.wall_x_max;
+    if (cf.wall_y_max != -999) st.wall[4] = cf.wall_y_max;
+    if (cf.wall_z_max != -999) st.wall[5] = cf.wall_z_max;
+    st.spd[0] = cf.speed_wall_x_min;
+    st.spd[1] = cf.speed_wall_y_min;
+    st.spd[2] = cf.speed_wall_z_min;
+    st.spd[3] = cf.speed_wall_x_max;
+    st.spd[4] = cf.speed_wall_y_max;
+    st.spd[5] = cf.speed_wall_z_max;
+    st.extf_scale = 1.0;
+    st.t = 1;
+    st.fracture = cf.enable_fracture;
+    st.self_contact = cf.self_contact;
+    st.damping = cf.allow_damping;
+    st.friction = cf.allow_friction;
+    st.torque = cf.enable_torque;
+    st.active = 1;
+    host_sim_toggles(sp, st, 1);
+    for (uint32_t p = 0; p < s.np; ++p) {
+      DevPart &P = parts[gpart + p];
+      if (cf.set_movable_index != -1 && (uint32_t)cf.set_movable_index == p && (uint32_t)cf.set_movable_timestep == 1u)
+        P.movable = 1;
+      if (cf.set_stoppable_index != -1 && (uint32_t)cf.set_stoppable_index == p &&
+          (uint32_t)cf.set_stoppable_timestep == 1u)
+        P.stoppable = 1;
+    }
+    if (cf.enable_torque || cf.set_torque_timestep != -1) torque_possible_ = true;
+    gnode += ns;
+    gpart += s.np;
+  }
+  half_skin_ = min_half_skin;
+
+  PD_TRY(dalloc(this, allocs_, &d_pos_, 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_disp_, 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_vel_[0], 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_vel_[1], 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_acc_, 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_force_, 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_ext_, 3 * C, err));
+  PD_TRY(dalloc(this, allocs_, &d_vol_, C, err));
+  PD_TRY(dalloc(this, allocs_, &d_pid_, C, err));
+  PD_TRY(dalloc(this, allocs_, &d_bdry_, C, err));
+  PD_TRY(dalloc(this, allocs_, &d_parts_, P_, err));
+  PD_TRY(dalloc(this, allocs_, &d_lrtb_, 6ull * P_, err));
+  PD_TRY(dalloc(this, allocs_, &d_lrtb_next_, 6ull * P_, err));
+  PD_TRY(dalloc(this, allocs_, &d_centroid_, 3ull * P_, err));
+  PD_TRY(dalloc(this, allocs_, &d_sp_, S_, err));
+  PD_TRY(dalloc(this, allocs_, &d_ss_, S_, err));
+  PD_TRY(dalloc(this, allocs_, &d_cnt_, 1, err));
+  auto up = [&](void *d, const void *h, size_t b, const char *w) { return check(cudaMemcpy(d, h, b, cudaMemcpyHostToDevice), w); };
+  PD_TRY(up(d_pos_, pos.data(), 3 * C * 8, "upload pos"));
+  PD_TRY(up(d_disp_, disp.data(), 3 * C * 8, "upload disp"));
+  PD_TRY(up(d_vel_[0], vel.data(), 3 * C * 8, "upload vel"));
+  PD_TRY(up(d_vel_[1], vel.data(), 3 * C * 8, "upload vel"));
+  PD_TRY(up(d_acc_, acc.data(), 3 * C * 8, "upload acc"));
+  PD_TRY(check(cudaMemset(d_force_, 0, 3 * C * 8), "memset force"));
+  PD_TRY(up(d_ext_, ext.data(), 3 * C * 8, "upload extforce"));
+  PD_TRY(up(d_vol_, vol.data(), C * 8, "upload vol"));
+  PD_TRY(up(d_pid_, h_pid_.data(), C * 4, "upload pid"));
+  PD_TRY(up(d_bdry_, bdry.data(), C, "upload bdry"));
+  PD_TRY(up(d_parts_, parts.data(), P_ * sizeof(DevPart), "upload particles"));
+  PD_TRY(up(d_sp_, sps.data(), S_ * sizeof(DevSimParams), "upload sim params"));
+  PD_TRY(up(d_ss_, sss.data(), S_ * sizeof(DevSimState), "upload sim state"));
+  PD_TRY(check(cudaMemset(d_centroid_, 0, 3ull * P_ * 8), "memset centroid"));
+  DevCounters cnt;
+  std::memset(&cnt, 0, sizeof(cnt));
+  cnt.moved = 1e300;  // forces the first broad-phase build
+  PD_TRY(up(d_cnt_, &cnt, sizeof(cnt), "upload counters"));
+  n_clamped_ = clamped_list.size();
+  if (n_clamped_) {
+    std::vector<uint32_t> cl(clamped_ptr);
+    cl.insert(cl.end(), clamped_list.begin(), clamped_list.end());
+    PD_TRY(dalloc(this, allocs_, &d_clamped_, cl.size(), err));
+    PD_TRY(up(d_clamped_, cl.data(), cl.size() * 4, "upload clamped"));
+    PD_TRY(dalloc(this, allocs_, &d_clamped_disp_, 3 * n_clamped_, err));
+    h_clamped_ = clamped_list;
+  }
+
+  PD_TRY(build_bonds());
+
+  if (precision_ == PD_FP64) {
+    PD_TRY(dalloc(this, allocs_, &d_bxi_, 3 * std::max<uint64_t>(E_, 1), err));
+    PD_TRY(dalloc(this, allocs_, &d_bxin_, std::max<uint64_t>(E_, 1), err));
+    PD_TRY(dalloc(this, allocs_, &d_brxin_, std::max<uint64_t>(E_, 1), err));
+  } else {
+    std::vector<float4> p32(C);
+    for (uint64_t g = 0; g < C; ++g) {
+      if (g < N_) {
+        const DevPart &P = parts[h_pid_[g]];
+        p32[g] = make_float4((float)(pos[g] - P.anchor_pos[0]), (float)(pos[C + g] - P.anchor_pos[1]),
+                             (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)vol[g]);
+      } else {
+        p32[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    PD_TRY(dalloc(this, allocs_, &d_pos32_, C, err));
+    PD_TRY(dalloc(this, allocs_, &d_disp32_, C, err));
+    PD_TRY(dalloc(this, allocs_, &d_anchor_, 3ull * P_, err));
+    PD_TRY(up(d_pos32_, p32.data(), C * sizeof(float4), "upload pos32"));
+    PD_TRY(check(cudaMemset(d_disp32_, 0, C * sizeof(float4)), "memset disp32"));
+  }
+
+  // broad phase
+  uint32_t bits = 10;
+  while ((1ull << bits) < 2 * N_) ++bits;
+  bp_.table_bits = bits;
+  const uint64_t T = 1ull << bits;
+  if (bp_.cand_cap == 0) bp_.cand_cap = 32;
+  PD_TRY(dalloc(this, allocs_, &bp_.count, T, err));
+  PD_TRY(dalloc(this, allocs_, &bp_.start, T, err));
+  PD_TRY(dalloc(this, allocs_, &bp_.key, C, err));
+  PD_TRY(dalloc(this, allocs_, &bp_.slot, C, err));
+  PD_TRY(dalloc(this, allocs_, &bp_.sorted, C, err));
+  PD_TRY(dalloc(this, allocs_, &bp_.block_sums, (T + 4095) / 4096 + 1, err));
+  PD_TRY(alloc_candidates());
+
+  DevView v = view(0);
+  if (precision_ == PD_FP64) launch_bond_constants(v, d_bxi_, d_bxin_, d_brxin_, stream_);
+  launch_init_lrtb(v, stream_);
+  PD_TRY(check(cudaGetLastError(), "init kernels"));
+  PD_TRY(check(cudaStreamSynchronize(stream_), "init sync"));
+  return PD_OK;
+}
+
+int Engine::alloc_candidates() {
+  if (bp_.cand) {
+    cudaFree(bp_.cand);
+    cudaFree(bp_.cand_n);
+    allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)bp_.cand), allocs_.end());
+    allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)bp_.cand_n), allocs_.end());
+    bp_.cand = nullptr;
+    bp_.cand_n = nullptr;
+  }
+  PD_TRY(dalloc(this, allocs_, &bp_.cand, Ncap_ * bp_.cand_cap, err));
+  PD_TRY(dalloc(this, allocs_, &bp_.cand_n, Ncap_, err));
+  PD_TRY(check(cudaMemset(bp_.cand_n, 0, Ncap_ * 2), "memset cand_n"));
+  return PD_OK;
+}
+
+int Engine::launch_step_seq(int cur, cudaStream_t s) {
+  DevView v = view(cur);
+  launch_predict(v, tpb_, s);
+  if (torque_possible_) launch_centroids(v, s);
+  launch_bp_decide(v, half_skin_, s);
+  launch_broadphase(v, bp_, s);
+  launch_step_kernel(v, precision_, tpb_, s);
+  if (stats_) launch_pairwise_count(v, s);
+  launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, s);
+  return check(cudaGetLastError(), "step launch");
+}
+
+int Engine::capture_graphs() {
+  for (int i = 0; i < 2; ++i) {
+    if (graph_[i]) {
+      cudaGraphExecDestroy(graph_[i]);
+      graph_[i] = nullptr;
+    }
+  }
+  for (int i = 0; i < 2; ++i) {
+    cudaGraph_t g;
+    PD_TRY(check(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "begin capture"));
+    int rc = launch_step_seq(i, capture_stream_);
+    cudaError_t e = cudaStreamEndCapture(capture_stream_, &g);
+    if (rc != PD_OK) return rc;
+    PD_TRY(check(e, "end capture"));
+    e = cudaGraphInstantiate(&graph_[i], g, 0);
+    cudaGraphDestroy(g);
+    PD_TRY(check(e, "graph instantiate"));
+  }
+  graphs_ok_ = true;
+  return PD_OK;
+}
+
+int Engine::step(uint32_t nsteps) {
+  if (!graphs_ok_ && use_graphs_) PD_TRY(capture_graphs());
+  for (uint32_t i = 0; i < nsteps; ++i) {
+    if (use_graphs_) {
+      PD_TRY(check(cudaGraphLaunch(graph_[cur_], stream_), "graph launch"));
+    } else {
+      PD_TRY(launch_step_seq(cur_, stream_));
+    }
+    cur_ ^= 1;
+    ++steps_done_;
+  }
+  return PD_OK;
+}
+
+int Engine::sync(int timeout_ms) {
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(stream_);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) return check(e, "stream");
+    if (timeout_ms >= 0) {
+      auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+      if (ms > timeout_ms) {
+        err = "pd_sync: timed out after " + std::to_string(timeout_ms) + " ms";
+        return PD_ETIMEOUT;
+      }
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  DevCounters c;
+  PD_TRY(check(cudaMemcpy(&c, d_cnt_, sizeof(c), cudaMemcpyDeviceToHost), "read counters"));
+  if (c.err) {
+    err = "device error word 0x" + std::to_string(c.err);
+    if (c.err & PD_DERR_NONFINITE) err += " (non-finite force density)";
+    if (c.err & PD_DERR_CAND_OVERFLOW) err += " (contact candidate list overflow: raise cand_cap)";
+    return PD_EDEVICE;
+  }
+  return PD_OK;
+}
+
+int Engine::set_stream(cudaStream_t s) {
+  PD_TRY(sync(-1));
+  if (s == nullptr) {
+    stream_ = capture_stream_;
+  } else {
+    stream_ = s;
+  }
+  return PD_OK;
+}
+
+int Engine::get_state(double *curpos, double *vel, double *acc, double *force, double *disp) {
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t C = Ncap_;
+  std::vector<double> buf(3 * C);
+  auto scatter = [&](double *dst) {
+    // [3][Ncap] device layout -> N*3 row vectors
+    for (uint64_t n = 0; n < N_; ++n)
+      for (int c = 0; c < 3; ++c) dst[3 * n + c] = buf[c * C + n];
+  };
+  auto fetch = [&](const double *d, double *dst) -> int {
+    PD_TRY(check(cudaMemcpy(buf.data(), d, 3 * C * 8, cudaMemcpyDeviceToHost), "read state"));
+    scatter(dst);
+    return PD_OK;
+  };
+  if (curpos || disp) {
+    std::vector<double> dsp(3 * N_);
+    PD_TRY(fetch(d_disp_, dsp.data()));
+    if (disp) std::memcpy(disp, dsp.data(), 3 * N_ * 8);
+    if (curpos) {
+      if (n_clamped_ && steps_done_ > 0) {
+        // CurrPos of clamped nodes keeps the predicted displacement (zeroed afterwards)
+        std::vector<double> cd(3 * n_clamped_);
+        PD_TRY(check(cudaMemcpy(cd.data(), d_clamped_disp_, 3 * n_clamped_ * 8, cudaMemcpyDeviceToHost), "read clamped"));
+        for (uint64_t i = 0; i < n_clamped_; ++i)
+          for (int c = 0; c < 3; ++c) dsp[3 * (uint64_t)h_clamped_[i] + c] = cd[3 * i + c];
+      }
+      uint64_t off = 0;
+      for (auto &s : sims_) {
+        uint64_t ns = s.node_offset[s.np];
+        for (uint64_t k = 0; k < ns; ++k)
+          for (int c = 0; c < 3; ++c) curpos[3 * (off + k) + c] = s.pos[3 * k + c] + dsp[3 * (off + k) + c];
+        off += ns;
+      }
+    }
+  }
+  if (vel) PD_TRY(fetch(d_vel_[cur_], vel));
+  if (acc) PD_TRY(fetch(d_acc_, acc));
+  if (force) PD_TRY(fetch(d_force_, force));
+  return PD_OK;
+}
+
+int Engine::set_state(const double *disp, const double *vel, const double *acc) {
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t C = Ncap_;
+  std::vector<double> buf(3 * C, 0.0);
+  auto put = [&](double *d, const double *src) -> int {
+    for (uint64_t n = 0; n < N_; ++n)
+      for (int c = 0; c < 3; ++c) buf[c * C + n] = src[3 * n + c];
+    return check(cudaMemcpy(d, buf.data(), 3 * C * 8, cudaMemcpyHostToDevice), "write state");
+  };
+  if (disp) PD_TRY(put(d_disp_, disp));
+  if (vel) PD_TRY(put(d_vel_[cur_], vel));
+  if (acc) PD_TRY(put(d_acc_, acc));
+  // a resumed state re-derives CurrPos/AABBs (timeloop.h:389-393) and the contact lists
+  DevView v = view(cur_);
+  launch_init_lrtb(v, stream_);
+  double big = 1e300;
+  PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
+  return check(cudaStreamSynchronize(stream_), "set_state");
+}
+
+int Engine::get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, uint64_t *n) {
+  if (particle >= P_) {
+    err = "particle index out of range";
+    return PD_EINVAL;
+  }
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t g0 = h_g0_[particle];
+  uint64_t nloc = 0;
+  {
+    uint64_t off = 0;
+    uint32_t pacc = 0;
+    for (auto &s : sims_) {
+      if (particle < pacc + s.np) {
+        uint32_t p = particle - pacc;
+        nloc = s.node_offset[p + 1] - s.node_offset[p];
+        break;
+      }
+      pacc += s.np;
+      off += s.node_offset[s.np];
+    }
+  }
+  const uint64_t s0 = g0 >> 5, s1 = (g0 + nloc + 31) >> 5;
+  const uint64_t e0 = h_slice_ptr_[s0], e1 = h_slice_ptr_[std::min<uint64_t>(s1, nslices_)];
+  std::vector<uint32_t> col(e1 - e0), mask((e1 - e0) / 32);
+  if (e1 > e0) {
+    PD_TRY(check(cudaMemcpy(col.data(), d_col_ + e0, (e1 - e0) * 4, cudaMemcpyDeviceToHost), "read col"));
+    PD_TRY(check(cudaMemcpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, cudaMemcpyDeviceToHost), "read mask"));
+  }
+  uint64_t c = 0;
+  for (uint64_t i = 0; i < nloc; ++i) {
+    const uint64_t g = g0 + i;
+    const uint64_t base = h_slice_ptr_[g >> 5] - e0 + (g & 31);
+    const uint64_t mbase = (h_slice_ptr_[g >> 5] - e0) >> 5;
+    for (uint32_t j = 0; j < h_deg_[g]; ++j) {
+      if (!((mask[mbase + j] >> (g & 31)) & 1u)) continue;
+      uint64_t q = col[base + 32ull * j] - g0;
+      if (i < q) {
+        if (pairs && c < cap) {
+          pairs[2 * c] = (uint32_t)i;
+          pairs[2 * c + 1] = (uint32_t)q;
+        }
+        ++c;
+      }
+    }
+  }
+  *n = c;
+  if (pairs && c > cap) {
+    err = "connectivity buffer too small";
+    return PD_EINVAL;
+  }
+  return PD_OK;
+}
+
+int Engine::get_wall(uint32_t sim, double *wall_info, double *reaction) {
+  if (sim >= S_) return PD_EINVAL;
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  DevSimState st;
+  PD_TRY(check(cudaMemcpy(&st, d_ss_ + sim, sizeof(st), cudaMemcpyDeviceToHost), "read wall"));
+  if (wall_info) std::memcpy(wall_info, st.wall, 6 * 8);
+  if (reaction) std::memcpy(reaction, st.react, 18 * 8);
+  return PD_OK;
+}
+
+int Engine::get_aabb(double *lrtb) {
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  return check(cudaMemcpy(lrtb, d_lrtb_, 6ull * P_ * 8, cudaMemcpyDeviceToHost), "read aabb");
+}
+
+int Engine::get_stats(pd_stats *st) {
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  DevCounters c;
+  PD_TRY(check(cudaMemcpy(&c, d_cnt_, sizeof(c), cudaMemcpyDeviceToHost), "read counters"));
+  DevSimState s0;
+  PD_TRY(check(cudaMemcpy(&s0, d_ss_, sizeof(s0), cudaMemcpyDeviceToHost), "read sim"));
+  st->step = s0.t - 1;
+  st->live_bonds = stats_ ? c.live_bonds : initial_bonds_;
+  st->pairwise_computations = c.pairwise;
+  st->contacts = c.contacts;
+  st->rebuilds = c.rebuilds;
+  st->device_errors = c.err;
+  unsigned long long z = 0;
+  PD_TRY(check(cudaMemcpy(&d_cnt_->pairwise, &z, 8, cudaMemcpyHostToDevice), "reset pairwise"));
+  return PD_OK;
+}
+
+int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, int use_graphs) {
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  bool relaunch = false;
+  if (skin_frac > 0 && skin_frac != bp_.skin_frac) {
+    bp_.skin_frac = skin_frac;
+    std::vector<DevSimParams> sps(S_);
+    PD_TRY(check(cudaMemcpy(sps.data(), d_sp_, S_ * sizeof(DevSimParams), cudaMemcpyDeviceToHost), "read params"));
+    double mh = 1e300;
+    for (auto &sp : sps) {
+      const double skin = skin_frac * sp.Rc;
+      const double rcand = (sp.Rc + skin) * (1.0 + 1e-9);
+      sp.cell = rcand * (1.0 + 1e-9);
+      sp.cand_r2 = rcand * rcand;
+      mh = std::min(mh, 0.5 * skin);
+    }
+    half_skin_ = mh;
+    PD_TRY(check(cudaMemcpy(d_sp_, sps.data(), S_ * sizeof(DevSimParams), cudaMemcpyHostToDevice), "write params"));
+    double big = 1e300;
+    PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
+    relaunch = true;
+  }
+  if (cand_cap > 0 && cand_cap != bp_.cand_cap) {
+    if (cand_cap > 64) {
+      err = "cand_cap above 64";
+      return PD_EINVAL;
+    }
+    bp_.cand_cap = cand_cap;
+    PD_TRY(alloc_candidates());
+    double big = 1e300;
+    PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
+    relaunch = true;
+  }
+  if (tpb > 0 && tpb != tpb_) {
+    tpb_ = tpb;
+    relaunch = true;
+  }
+  if (stats >= 0 && (stats != 0) != stats_) {
+    stats_ = stats != 0;
+    relaunch = true;
+  }
+  if (use_graphs >= 0) use_graphs_ = use_graphs != 0;
+  if (relaunch) graphs_ok_ = false;
+  return PD_OK;
+}
+
+int Engine::clear_device_errors() {
+  uint32_t z = 0;
+  return check(cudaMemcpy(&d_cnt_->err, &z, 4, cudaMemcpyHostToDevice), "clear errors");
+}
+
+double Engine::step_bytes(uint64_t live) const {
+  return 4.125 * (double)live + 224.0 * (double)N_;
+}
+
+}  // namespace pdg

@@ -1,0 +1,250 @@
+// pd_engine.h -- device data layout and host engine of the GB300 explicit step.
+//
+// Layout in HBM (all particles of all simulations of a batch concatenated in file order;
+// node n of particle p is global node node_offset[p] + local index):
+//   * node state, FP64 structure-of-arrays: pos/disp/vel/acc/force/extforce as [3][Ncap]
+//     (x block, y block, z block), vol[N]; vel is double-buffered (the fused kernel reads
+//     partners' step-start velocity while it writes the corrected one);
+//   * bonds, SELL-32: nodes are grouped in slices of 32 consecutive nodes (one warp); a
+//     slice stores its rows column-major, entry (slice s, position j, lane l) at
+//     slice_ptr[s] + 32*j + l, so the 32 lanes of a warp read 128 contiguous bytes of
+//     column indices per position. Each row keeps the reference's neighbour order
+//     (conn2NArr push order, ascending for a sorted Connectivity). One 32-bit word per
+//     (slice, position) holds the live bits of the 32 lanes: bit l of
+//     mask[slice_ptr[s]/32 + j]. Breaking clears a bit; bonds are never re-added;
+//   * FP64 form only: per-entry constants xi = pos[q]-pos[i] (3 doubles), |xi| and the
+//     correctly rounded reciprocal of |xi| (gen_xi, particle2.h:241-257);
+//   * FP32-compensated form only: float4 (local position, volume) and float4 (local
+//     displacement) per node, local = relative to the particle's anchor node;
+//   * contact broad phase: hashed cell list (counting sort) rebuilt only when the nodes may
+//     have moved more than half the skin since the last build; per-node candidate lists
+//     (fixed capacity, ascending global index) of nodes within contact radius + skin.
+#ifndef PD_ENGINE_H
+#define PD_ENGINE_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "peridem_gb300.h"
+
+namespace pdg {
+
+constexpr int kSlice = 32;
+constexpr uint32_t kNoCol = 0xFFFFFFFFu;
+
+// Per-particle parameters (ParticleN scalars, particle2.h:51-59).
+struct DevPart {
+  uint32_t g0, n, sim, taxis;
+  double rho, irho, cnot, snot, tval;
+  int32_t movable, breakable, stoppable, break_bonds;
+  double anchor_pos[3];  // FP32 form: position of the anchor node
+};
+
+// Per-simulation constants (Contact, RectWall and Timeloop fields after apply_config).
+struct DevSimParams {
+  double dt, hdt2, hdt;       // dt, (dt*dt)*0.5, 0.5*dt
+  double Rc, Kn, sc, zeta2, mu;  // contact radius, stiffness, Kn*Rc, 2*damping, friction
+  double pi3, pi4;            // M_PI/3, M_PI/4 (segment_mass)
+  double cell;                // broad-phase cell edge (Rc + skin, slightly enlarged)
+  double cand_r2;             // squared candidate radius
+  int32_t nl_bdry_only, compute_wall_reaction, gradient_extforce, allow_wall;
+  uint32_t extforce_maxstep;
+  int32_t set_torque_ts, set_fracture_ts, set_self_contact_ts, set_damping_ts;
+  int32_t set_zero_wall_speed_ts, set_movable_index, set_movable_ts;
+  int32_t set_stoppable_index, set_stoppable_ts;
+  uint32_t p0, np;            // particle range of this simulation
+  uint64_t node0, nnodes;     // node range of this simulation
+};
+
+// Per-simulation state that changes from step to step.
+struct DevSimState {
+  double wall[6];   // x_min y_min z_min x_max y_max z_max
+  double spd[6];
+  double react[18]; // 6 faces x 3, get_reaction() order
+  double extf_scale;
+  uint32_t t;       // index of the step about to run (1-based, like timeloop.h:395)
+  int32_t fracture, self_contact, damping, friction, torque, active;
+  uint32_t pad;
+};
+
+// Global counters (one block of device memory, read back by pd_get_stats).
+struct DevCounters {
+  unsigned long long stepmax_bits;  // max |disp increment| of the current step (double bits)
+  double moved;                     // accumulated bound since the last rebuild
+  uint32_t rebuild;                 // set when this step rebuilt the broad phase
+  uint32_t err;                     // PD_DERR_* bits
+  unsigned long long contacts;
+  unsigned long long pairwise;
+  unsigned long long rebuilds;
+  unsigned long long live_bonds;
+};
+
+// Everything a kernel needs, passed by value.
+struct DevView {
+  uint64_t N;            // nodes
+  uint64_t Ncap;         // stride of the [3][Ncap] arrays
+  uint32_t P, S;         // particles, simulations
+  const double *pos;     // [3][Ncap]
+  double *disp;
+  const double *vel_in;
+  double *vel_out;
+  double *acc, *force;
+  const double *ext, *vol;
+  const uint32_t *pid;   // particle of each node
+  const uint8_t *bdry;   // 1 if node is in its particle's bdry_nodes list
+  // bonds
+  const uint64_t *slice_ptr;
+  const uint16_t *deg;
+  const uint32_t *col;
+  uint32_t *mask;
+  const double *bxi, *bxin, *brxin;  // FP64 form, [3][E], [E], [E]
+  uint64_t E;
+  // FP32-compensated form
+  float4 *pos32, *disp32;
+  const double *anchor;  // [P][3] anchor displacement for the current step
+  double break_band;     // relative band around snot where the FP64 stretch decides
+  // particles / sims
+  DevPart *parts;
+  double *lrtb, *lrtb_next;  // [P][6]; lrtb_next holds ordered-integer min/max keys
+  const DevSimParams *sp;
+  DevSimState *ss;
+  // contact
+  const uint32_t *cand;  // [N][cap]
+  const uint16_t *cand_n;
+  uint32_t cand_cap;
+  // torque centroids [P][3]
+  const double *centroid;
+  DevCounters *cnt;
+  int stats;
+};
+
+// Broad-phase scratch (hashed cell list).
+struct BroadPhase {
+  uint32_t table_bits = 0;
+  uint32_t *count = nullptr, *start = nullptr, *key = nullptr, *slot = nullptr, *sorted = nullptr;
+  uint32_t *block_sums = nullptr;
+  uint32_t *cand = nullptr;
+  uint16_t *cand_n = nullptr;
+  uint32_t cand_cap = 0;
+  double skin_frac = 0.5;
+};
+
+// Host-side description of one simulation (setup + resolved config).
+struct HostSim {
+  pd_config cfg;
+  uint32_t np = 0;
+  std::vector<uint64_t> node_offset;
+  std::vector<double> pos, vol, disp, vel, acc, ext;     // N*3 / N
+  std::vector<uint64_t> conn_offset;
+  std::vector<uint32_t> conn;
+  std::vector<uint64_t> bdry_offset, clamped_offset;
+  std::vector<uint32_t> bdry, clamped;
+  std::vector<double> delta, rho, cnot, snot, tval;
+  std::vector<int32_t> movable, breakable, stoppable;
+  std::vector<uint32_t> taxis;
+  double Rc = 0, Kn = 0, zeta = 0, mu = 0;
+  int32_t allow_wall = 0, n_geom_wall = 6;
+  double geom[6] = {0, 0, 0, 0, 0, 0};
+};
+
+class Engine {
+ public:
+  Engine() = default;
+  ~Engine();
+  int init(std::vector<HostSim> &sims, int precision);
+  int step(uint32_t nsteps);
+  int sync(int timeout_ms);
+  int set_stream(cudaStream_t s);
+  int get_state(double *curpos, double *vel, double *acc, double *force, double *disp);
+  int set_state(const double *disp, const double *vel, const double *acc);
+  int get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, uint64_t *n);
+  int get_wall(uint32_t sim, double *wall_info, double *reaction);
+  int get_aabb(double *lrtb);
+  int get_stats(pd_stats *st);
+  // skin_frac <= 0, cand_cap == 0, tpb <= 0, stats < 0, use_graphs < 0 keep the setting
+  int set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, int use_graphs);
+  int clear_device_errors();
+  double step_bytes(uint64_t live_bonds) const;
+  uint64_t initial_bonds() const { return initial_bonds_; }
+  uint64_t num_nodes() const { return N_; }
+  uint32_t num_particles() const { return P_; }
+  uint64_t steps_done() const { return steps_done_; }
+  cudaStream_t stream() const { return stream_; }
+  int precision() const { return precision_; }
+  std::string err;
+  const std::vector<HostSim> &sims() const { return sims_; }
+
+ private:
+  int alloc_and_upload();
+  int alloc_candidates();
+  int build_bonds();
+  int launch_step_seq(int cur, cudaStream_t s);
+  int capture_graphs();
+  int check(cudaError_t e, const char *what);
+  DevView view(int cur) const;
+
+  std::vector<HostSim> sims_;
+  int precision_ = PD_FP64;
+  uint64_t N_ = 0, Ncap_ = 0, E_ = 0, nslices_ = 0;
+  uint32_t P_ = 0, S_ = 0;
+  cudaStream_t stream_ = nullptr;          // stream work is enqueued on
+  cudaStream_t capture_stream_ = nullptr;  // the handle's own stream (graphs are captured here)
+  bool own_stream_ = false;
+  int tpb_ = 128;
+  int cur_ = 0;  // which vel buffer holds the current velocity
+  bool torque_possible_ = false;
+  bool stats_ = false;
+  bool use_graphs_ = true;
+  uint64_t steps_done_ = 0;
+  uint64_t initial_bonds_ = 0;
+  double half_skin_ = 0;
+
+  // host mirrors used when reading results back
+  std::vector<uint32_t> h_pid_;
+  std::vector<uint64_t> h_slice_ptr_;
+  std::vector<uint16_t> h_deg_;
+  std::vector<uint32_t> h_g0_;
+  std::vector<uint32_t> h_clamped_;
+
+  // device buffers
+  double *d_pos_ = nullptr, *d_disp_ = nullptr, *d_vel_[2] = {nullptr, nullptr}, *d_acc_ = nullptr;
+  double *d_force_ = nullptr, *d_ext_ = nullptr, *d_vol_ = nullptr;
+  uint32_t *d_pid_ = nullptr;
+  uint8_t *d_bdry_ = nullptr;
+  uint64_t *d_slice_ptr_ = nullptr;
+  uint16_t *d_deg_ = nullptr;
+  uint32_t *d_col_ = nullptr, *d_mask_ = nullptr;
+  double *d_bxi_ = nullptr, *d_bxin_ = nullptr, *d_brxin_ = nullptr;
+  float4 *d_pos32_ = nullptr, *d_disp32_ = nullptr;
+  double *d_anchor_ = nullptr;
+  DevPart *d_parts_ = nullptr;
+  double *d_lrtb_ = nullptr, *d_lrtb_next_ = nullptr, *d_centroid_ = nullptr;
+  DevSimParams *d_sp_ = nullptr;
+  DevSimState *d_ss_ = nullptr;
+  DevCounters *d_cnt_ = nullptr;
+  uint32_t *d_clamped_ = nullptr;  // [P+1] offsets followed by global node ids
+  double *d_clamped_disp_ = nullptr;
+  uint64_t n_clamped_ = 0;
+  BroadPhase bp_;
+  std::vector<void *> allocs_;
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  bool graphs_ok_ = false;
+};
+
+// kernel launchers (pd_kernels.cu / pd_broadphase.cu)
+void launch_predict(const DevView &v, int tpb, cudaStream_t s);
+void launch_step_kernel(const DevView &v, int precision, int tpb, cudaStream_t s);
+void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
+                     cudaStream_t s);
+void launch_centroids(const DevView &v, cudaStream_t s);
+void launch_bond_constants(const DevView &v, double *bxi, double *bxin, double *brxin, cudaStream_t s);
+void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s);
+void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s);
+void launch_pairwise_count(const DevView &v, cudaStream_t s);
+void launch_init_lrtb(const DevView &v, cudaStream_t s);
+
+}  // namespace pdg
+#endif

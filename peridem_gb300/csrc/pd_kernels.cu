@@ -1,0 +1,715 @@
+// pd_kernels.cu -- the per-step kernels (compiled with -fmad=false).
+//
+// One step (src/particle/timeloop.h:395-797) is:
+//   k_predict        predictor for all nodes (timeloop.h:537-540), step-max displacement
+//                    increment for the broad-phase rebuild test, FP32 local displacement
+//   [broad phase]    pd_broadphase.cu, runs only when a rebuild is due
+//   k_step<PREC>     fused per-node force and corrector: PD bond sum with breaking
+//                    (particle2.h:107-237), self-contact, walls, extforce, torque
+//                    (timeloop.h:544-634), node-node contact of particle pairs in
+//                    ascending partner order (timeloop.h:636-651, contact.h:744-942) and
+//                    the velocity-Verlet corrector (timeloop.h:661-781)
+//   k_end_particles  AABB refresh, clamped nodes, anchors, per-particle toggles
+//   k_end_sims       wall motion (timeloop.h:784-797), scheduled toggles, step counter
+// Each node's force is gathered by one thread in the reference's summation order, so the
+// FP64 form reproduces the reference bit for bit without atomics on forces.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include "pd_engine.h"
+#include "pd_math.cuh"
+
+namespace pdg {
+
+// ------------------------------------------------------------------------------------
+// small helpers
+
+__device__ __forceinline__ D3 ld3(const double *a, uint64_t n, uint64_t cap) {
+  return d3(a[n], a[n + cap], a[n + 2 * cap]);
+}
+__device__ __forceinline__ void st3(double *a, uint64_t n, uint64_t cap, D3 v) {
+  a[n] = v.x;
+  a[n + cap] = v.y;
+  a[n + 2 * cap] = v.z;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// intersects_box_fext<3> (contact.h:1143-1183): only box A is extended by c.
+__device__ __forceinline__ bool intersects_fext(const double *A, const double *B, double c) {
+  double A_min_x = A[0] - c, A_min_y = A[1] - c, A_min_z = A[2] - c;
+  double A_max_x = A[3] + c, A_max_y = A[4] + c, A_max_z = A[5] + c;
+  return (A_min_x <= B[3]) && (A_max_x >= B[0]) && (A_max_y >= B[1]) && (A_min_y <= B[4]) &&
+         (A_min_z <= B[5]) && (A_max_z >= B[2]);
+}
+
+// within_interior_fext (contact.h:1229-1243) with its 2D indexing of 3D boxes.
+__device__ __forceinline__ bool within_interior(const double *A, const double *B, double c) {
+  double A_Left = A[0] - c, A_Right = A[1] + c, A_Top = A[2] + c, A_Bottom = A[3] - c;
+  return (B[0] < A_Left) && (A_Right < B[1]) && (B[2] > A_Top) && (B[3] < A_Bottom);
+}
+
+// Normal, damping and friction force densities of one node-node contact, computed from
+// the point of view of the "C" node as update_contact_force_by_boundary does
+// (contact.h:798-934). fc is always set; fd/ff only when has_fd/has_ff.
+struct PairForce {
+  D3 fc, fd, ff;
+  bool has_fd, has_ff;
+};
+
+__device__ __forceinline__ void pair_force(D3 dir, double dn, double len_ref, double sc,
+                                           double N_vol, double rho_C, D3 velC, D3 velN,
+                                           const DevSimParams &sp, const DevSimState &st,
+                                           PairForce &o) {
+  D3 unit = dir / dn;
+  double s = (dn - len_ref) / len_ref;
+  double fmag = (sc * s) * N_vol;
+  o.fc = fmag * unit;
+  double fcn = norm3(o.fc);
+  o.has_fd = false;
+  o.has_ff = false;
+  if (st.damping) {
+    D3 rel = velC - velN;
+    double rvp = dot3(rel, unit);
+    D3 rvn = rvp * unit;
+    double dc = (sp.zeta2 * sqrt(sc * rho_C)) * sqrt(N_vol);
+    o.fd = (-dc) * rvn;
+    o.has_fd = true;
+  }
+  if (st.friction) {
+    D3 rel = velC - velN;
+    double rd = dot3(rel, unit);
+    D3 rvt = rel - rd * unit;
+    double rvtn = norm3(rvt);
+    if (rvtn > 0) {
+      D3 tu = rvt / norm3(rvt);
+      double fm = (-sp.mu) * fcn;
+      if (rvtn < ((sp.mu * fcn) * sp.dt) / rho_C) fm = ((-rvtn) / rho_C) / sp.dt;
+      o.ff = fm * tu;
+      o.has_ff = true;
+    }
+  }
+}
+
+// segment_mass<3> + wall_side_force_update<3> (contact.h:14-39, 381-502) for one face.
+__device__ __forceinline__ void wall_face(double dist, int dir, D3 vel, double vol, double rho,
+                                          D3 &f, double wspeed, int face,
+                                          const DevSimParams &sp, DevSimState &st, bool reaction) {
+  const double R = sp.Rc;
+  if (!(fabs(dist) <= R)) return;
+  double d = fabs(dist);
+  double rd = R - d;
+  double area = (sp.pi3 * (rd * rd)) * (2 * R - d);
+  double w = R * R - d * d;
+  double I = sp.pi4 * (w * w);
+  double cen = I / area;
+  double crc = R - cen;
+  double pcrc = (crc > 0 ? crc : 0);
+  double F = (sp.Kn * pcrc) * area;
+  double c_sign = (dist > 0 ? 1.0 : -1.0);
+  double r0 = 0, r1 = 0, r2 = 0;  // reaction contributions in dir, t1, t2
+  {
+    double a = c_sign * F;
+    set_comp(f, dir, comp(f, dir) + a);
+    r0 -= ((vol * c_sign) * F);
+  }
+  D3 rel = vel;
+  set_comp(rel, dir, comp(rel, dir) - wspeed);
+  const int t1 = (dir + 1) % 3, t2 = (dir + 2) % 3;
+  if (st.friction) {
+    double v1 = comp(rel, t1), v2 = comp(rel, t2);
+    double vn = sqrt(v1 * v1 + v2 * v2);
+    if (vn > 0) {
+      double u1 = v1 / vn, u2 = v2 / vn;
+      double aF = fabs(F);
+      double ff1 = ((-sp.mu) * aF) * u1;
+      double ff2 = ((-sp.mu) * aF) * u2;
+      if (vn < ((sp.mu * aF) * sp.dt) / rho) {
+        double g = ((-vn) / rho) / sp.dt;
+        ff1 = g * u1;
+        ff2 = g * u2;
+      }
+      set_comp(f, t1, comp(f, t1) + ff1);
+      set_comp(f, t2, comp(f, t2) + ff2);
+      r1 -= (vol * ff1);
+      r2 -= (vol * ff2);
+    }
+  }
+  if (st.damping) {
+    double dc = ((sp.zeta2) * sqrt(sp.Kn * rho)) * sqrt(fabs(area));
+    double df = (-dc) * comp(rel, dir);
+    set_comp(f, dir, comp(f, dir) + df);
+    r0 -= (vol * df);
+  }
+  if (reaction) {
+    atomicAdd(&st.react[3 * face + dir], r0);
+    if (r1 != 0) atomicAdd(&st.react[3 * face + t1], r1);
+    if (r2 != 0) atomicAdd(&st.react[3 * face + t2], r2);
+  }
+}
+
+// Does row n hold a live bond to global node m? (std::find over NbdArr, contact.h:783)
+__device__ __forceinline__ bool row_has_live(const DevView &v, uint64_t n, uint32_t m) {
+  const uint64_t s = n >> 5;
+  const uint32_t lane = (uint32_t)(n & 31);
+  const uint64_t base = v.slice_ptr[s] + lane;
+  const uint64_t mbase = v.slice_ptr[s] >> 5;
+  const int dg = v.deg[n];
+  for (int j = 0; j < dg; ++j) {
+    if (v.col[base + 32ull * j] == m) return (v.mask[mbase + j] >> lane) & 1u;
+  }
+  return false;
+}
+
+// ------------------------------------------------------------------------------------
+// predictor
+
+__global__ void k_predict(DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double inc = 0.0;
+  if (n < v.N) {
+    const uint32_t k = v.pid[n];
+    const DevPart &P = v.parts[k];
+    const DevSimParams &sp = v.sp[P.sim];
+    if (v.ss[P.sim].active) {
+      D3 d = ld3(v.disp, n, v.Ncap), ve = ld3(v.vel_in, n, v.Ncap), a = ld3(v.acc, n, v.Ncap);
+      // disp += dt*vel + (dt*dt*0.5)*acc  (timeloop.h:538, overloads.h:129-159)
+      D3 dv = sp.dt * ve;
+      D3 da = sp.hdt2 * a;
+      D3 in = dv + da;
+      d = d + in;
+      st3(v.disp, n, v.Ncap, d);
+      inc = norm3(in);
+      if (v.disp32) {
+        const double *an = v.anchor + 3 * (uint64_t)k;
+        v.disp32[n] = make_float4((float)(d.x - an[0]), (float)(d.y - an[1]), (float)(d.z - an[2]), 0.f);
+      }
+    }
+  }
+  inc = warp_max(inc);
+  if ((threadIdx.x & 31) == 0 && inc > 0)
+    atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(inc));
+}
+
+void launch_predict(const DevView &v, int tpb, cudaStream_t s) {
+  uint64_t blocks = (v.N + tpb - 1) / tpb;
+  if (blocks) k_predict<<<(unsigned)blocks, tpb, 0, s>>>(v);
+}
+
+// ------------------------------------------------------------------------------------
+// fused force + corrector
+
+template <int PREC>
+__global__ void __launch_bounds__(128) k_step(DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  const uint32_t k = v.pid[nn];
+  const DevPart P = v.parts[k];
+  const DevSimParams &sp = v.sp[P.sim];
+  DevSimState &st = v.ss[P.sim];
+  const bool run = valid && st.active;
+  const uint64_t C3 = v.Ncap;
+
+  D3 f = d3(0.0, 0.0, 0.0);
+  D3 di = ld3(v.disp, nn, C3);
+  const D3 pi = ld3(v.pos, nn, C3);
+  const D3 vi = ld3(v.vel_in, nn, C3);
+  const double voli = v.vol[nn];
+  const bool bdry_i = v.bdry[nn] != 0;
+  unsigned long long live = 0, ncontacts = 0;
+
+  if (run && P.movable) {
+    // ---- peridynamic bond force (particle2.h:117-157) and breaking (particle2.h:196-237)
+    const uint64_t s = nn >> 5;
+    const uint32_t lane = (uint32_t)(nn & 31);
+    const uint64_t base = v.slice_ptr[s] + lane;
+    const uint64_t mbase = v.slice_ptr[s] >> 5;
+    const int dg = v.deg[nn];
+    const bool brk = st.fracture && P.breakable && P.break_bonds;
+    if (PREC == PD_FP64) {
+      D3 acc = d3(0.0, 0.0, 0.0);
+      for (int j = 0; j < dg; ++j) {
+        const uint32_t mw = v.mask[mbase + j];
+        if (!((mw >> lane) & 1u)) continue;
+        const uint64_t e = base + 32ull * j;
+        const uint32_t q = v.col[e];
+        ++live;
+        D3 dq = ld3(v.disp, q, C3);
+        D3 eta = (dq - di) + d3(v.bxi[e], v.bxi[e + v.E], v.bxi[e + 2 * v.E]);
+        double en = norm3(eta);
+        double xn = v.bxin[e];
+        double str = div_rcp(en - xn, xn, v.brxin[e]);
+        double mag = (P.cnot * str) * v.vol[q];
+        double ren = __drcp_rn(en);
+        D3 unit = d3(div_rcp(eta.x, en, ren), div_rcp(eta.y, en, ren), div_rcp(eta.z, en, ren));
+        acc = acc + mag * unit;
+        if (brk && str > P.snot) atomicAnd(&v.mask[mbase + j], ~(1u << lane));
+      }
+      f = d3(0.0, 0.0, 0.0) + acc;
+    } else {
+      // FP32 bond forces: cancellation-free stretch s = (2 xi.eta + eta.eta) /
+      // ((|xi+eta| + |xi|) |xi|) on anchor-relative FP32 positions/displacements, and
+      // Kahan-compensated FP32 sums. The stretch-vs-snot decision falls back to the FP64
+      // formula inside a relative band around snot.
+      const float4 pi4 = v.pos32[nn];
+      const float4 ui4 = v.disp32[nn];
+      const float cn = (float)P.cnot;
+      const float snot_lo = (float)(P.snot * (1.0 - v.break_band));
+      const float snot_hi = (float)(P.snot * (1.0 + v.break_band));
+      float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+      for (int j = 0; j < dg; ++j) {
+        const uint32_t mw = v.mask[mbase + j];
+        if (!((mw >> lane) & 1u)) continue;
+        const uint64_t e = base + 32ull * j;
+        const uint32_t q = v.col[e];
+        ++live;
+        const float4 pq = v.pos32[q];
+        const float4 uq = v.disp32[q];
+        const float xx = pq.x - pi4.x, xy = pq.y - pi4.y, xz = pq.z - pi4.z;
+        const float ex = uq.x - ui4.x, ey = uq.y - ui4.y, ez = uq.z - ui4.z;
+        const float yx = xx + ex, yy = xy + ey, yz = xz + ez;
+        const float xin = sqrtf(__fmaf_rn(xx, xx, __fmaf_rn(xy, xy, xz * xz)));
+        const float yn = sqrtf(__fmaf_rn(yx, yx, __fmaf_rn(yy, yy, yz * yz)));
+        const float xe = __fmaf_rn(xx, ex, __fmaf_rn(xy, ey, xz * ez));
+        const float ee = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, ez * ez));
+        const float str = __fdividef(__fmaf_rn(2.f, xe, ee), (yn + xin) * xin);
+        const float g = __fdividef(cn * str * pq.w, yn);
+        // Kahan-compensated accumulation of g * (xi + eta)
+        float t, y;
+        y = __fmaf_rn(g, yx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
+        y = __fmaf_rn(g, yy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
+        y = __fmaf_rn(g, yz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
+        if (brk && str > snot_lo) {
+          bool cut = str > snot_hi;
+          if (!cut) {
+            // FP64 stretch of the reference formula for bonds near the threshold
+            D3 dq = ld3(v.disp, q, C3);
+            D3 xi64 = ld3(v.pos, q, C3) - pi;
+            D3 eta = (dq - di) + xi64;
+            double en = norm3(eta), xn = norm3(xi64);
+            cut = ((en - xn) / xn) > P.snot;
+          }
+          if (cut) atomicAnd(&v.mask[mbase + j], ~(1u << lane));
+        }
+      }
+      f = d3((double)sx - (double)cx, (double)sy - (double)cy, (double)sz - (double)cz);
+    }
+
+    // ---- self-contact (timeloop.h:554-557, contact.h:779-796), C side only
+    if (st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || bdry_i)) {
+      const uint32_t *cl = v.cand + nn * v.cand_cap;
+      const int nc = v.cand_n[nn];
+      for (int c = 0; c < nc; ++c) {
+        const uint32_t m = cl[c];
+        if (m < P.g0) continue;
+        if (m >= P.g0 + P.n) break;
+        if (sp.nl_bdry_only && !v.bdry[m]) continue;
+        D3 xi = ld3(v.pos, m, C3) - pi;
+        D3 dir = (ld3(v.disp, m, C3) - di) + xi;
+        double dn = norm3(dir);
+        if (!(dn <= sp.Rc)) continue;
+        double xin = norm3(xi);
+        double len_ref = sp.Rc, sc = sp.sc;
+        if (row_has_live(v, nn, m)) continue;
+        if (xin < sp.Rc) {
+          len_ref = xin;
+          sc = P.cnot;
+        }
+        if (!(dn < len_ref)) continue;
+        PairForce pf;
+        pair_force(dir, dn, len_ref, sc, v.vol[m], P.rho, vi, ld3(v.vel_in, m, C3), sp, st, pf);
+        if (P.stoppable) {
+          f = f + pf.fc;
+          if (pf.has_fd) f = f + pf.fd;
+          if (pf.has_ff) f = f + pf.ff;
+        }
+      }
+    }
+
+    // ---- walls (timeloop.h:561-569, contact.h:1094-1121)
+    if (P.stoppable && sp.allow_wall && !within_interior(v.lrtb + 6 * (uint64_t)k, st.wall, sp.Rc) &&
+        (!sp.nl_bdry_only || bdry_i)) {
+      D3 cur = pi + di;
+      const bool rx = sp.compute_wall_reaction != 0;
+      wall_face(cur.x - st.wall[0], 0, vi, voli, P.rho, f, st.spd[0], 0, sp, st, rx);
+      wall_face(cur.x - st.wall[3], 0, vi, voli, P.rho, f, st.spd[3], 3, sp, st, rx);
+      wall_face(cur.y - st.wall[1], 1, vi, voli, P.rho, f, st.spd[1], 1, sp, st, rx);
+      wall_face(cur.y - st.wall[4], 1, vi, voli, P.rho, f, st.spd[4], 4, sp, st, rx);
+      wall_face(cur.z - st.wall[2], 2, vi, voli, P.rho, f, st.spd[2], 2, sp, st, rx);
+      wall_face(cur.z - st.wall[5], 2, vi, voli, P.rho, f, st.spd[5], 5, sp, st, rx);
+    }
+
+    // ---- external force (timeloop.h:582-597)
+    D3 ex = ld3(v.ext, nn, C3);
+    if (sp.gradient_extforce) ex = st.extf_scale * ex;
+    f = f + ex;
+  }
+
+  // ---- torque about the centroid (timeloop.h:600-633), for movable and fixed particles
+  if (run && st.torque) {
+    const double *c = v.centroid + 3 * (uint64_t)k;
+    D3 r = (pi + di) - d3(c[0], c[1], c[2]);
+    double rn = norm3(r);
+    double r_inv = (rn != 0.0 ? 1 / rn : 0);
+    const int ta = (int)P.taxis;
+    set_comp(r, ta, 0.0);
+    D3 perp = d3(0.0, 0.0, 0.0);
+    set_comp(perp, (ta + 1) % 3, -comp(r, (ta + 2) % 3));
+    set_comp(perp, (ta + 2) % 3, comp(r, (ta + 1) % 3));
+    double pn = norm3(perp);
+    if (pn > 0) {
+      perp = perp / pn;
+    } else {
+      set_comp(perp, (ta + 1) % 3, 0.0);
+      set_comp(perp, (ta + 2) % 3, 0.0);
+    }
+    f = f + (r_inv * P.tval) * perp;
+  }
+
+  // ---- node-node contact of particle pairs (timeloop.h:636-651, contact.h:754-937):
+  // partners in ascending global index; a partner in a lower particle index acts as the
+  // "C" node of the pair (reaction form), a partner in a higher index as the "N" node.
+  if (run && P.stoppable && (!sp.nl_bdry_only || bdry_i)) {
+    const uint32_t *cl = v.cand + nn * v.cand_cap;
+    const int nc = v.cand_n[nn];
+    for (int c = 0; c < nc; ++c) {
+      const uint32_t m = cl[c];
+      if (m >= P.g0 && m < P.g0 + P.n) continue;
+      const uint32_t km = v.pid[m];
+      const uint32_t a = km < k ? km : k, b = km < k ? k : km;
+      if (!(v.parts[a].movable || v.parts[b].movable)) continue;
+      if (!intersects_fext(v.lrtb + 6 * (uint64_t)a, v.lrtb + 6 * (uint64_t)b, sp.Rc)) continue;
+      if (sp.nl_bdry_only && !v.bdry[m]) continue;
+      const D3 pm = ld3(v.pos, m, C3), dm = ld3(v.disp, m, C3), vm = ld3(v.vel_in, m, C3);
+      const double volm = v.vol[m];
+      if (km > k) {
+        D3 xi = pm - pi;
+        D3 dir = (dm - di) + xi;
+        double dn = norm3(dir);
+        if (!(dn <= sp.Rc) || !(dn < sp.Rc)) continue;
+        PairForce pf;
+        pair_force(dir, dn, sp.Rc, sp.sc, volm, P.rho, vi, vm, sp, st, pf);
+        f = f + pf.fc;
+        if (pf.has_fd) f = f + pf.fd;
+        if (pf.has_ff) f = f + pf.ff;
+        ++ncontacts;
+      } else {
+        D3 xi = pi - pm;
+        D3 dir = (di - dm) + xi;
+        double dn = norm3(dir);
+        if (!(dn <= sp.Rc) || !(dn < sp.Rc)) continue;
+        PairForce pf;
+        pair_force(dir, dn, sp.Rc, sp.sc, voli, v.parts[km].rho, vm, vi, sp, st, pf);
+        f = f - (pf.fc / voli) * volm;
+        if (pf.has_fd) {
+          double sn = sqrt(voli), sv = sqrt(volm);
+          f = f - (pf.fd / sn) * sv;
+        }
+        if (pf.has_ff) f = f - pf.ff;
+      }
+    }
+  }
+
+  // ---- corrector (timeloop.h:662-781)
+  if (run) {
+    st3(v.force, nn, C3, f);
+    if (!(isfinite(f.x) && isfinite(f.y) && isfinite(f.z))) atomicOr(&v.cnt->err, PD_DERR_NONFINITE);
+    D3 vo = vi;
+    if (P.movable) {
+      const D3 ao = ld3(v.acc, nn, C3);
+      const D3 an = P.irho * f;
+      D3 tmp = ao + an;
+      tmp = sp.hdt * tmp;
+      vo = vi + tmp;
+      st3(v.acc, nn, C3, an);
+    }
+    st3(v.vel_out, nn, C3, vo);
+  }
+
+  // ---- AABB of CurrPos for the next step (timeloop.h:779), warp-reduced
+  {
+    const bool contrib = run && P.movable;
+    D3 cur = pi + di;
+    double lo[3] = {contrib ? cur.x : INFINITY, contrib ? cur.y : INFINITY, contrib ? cur.z : INFINITY};
+    double hi[3] = {contrib ? cur.x : -INFINITY, contrib ? cur.y : -INFINITY, contrib ? cur.z : -INFINITY};
+    const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+    const bool uniform = __all_sync(0xffffffffu, k == k0);
+    if (uniform) {
+      for (int o = 16; o > 0; o >>= 1) {
+        for (int c = 0; c < 3; ++c) {
+          lo[c] = fmin(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+          hi[c] = fmax(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+      }
+    }
+    const bool writer = uniform ? ((threadIdx.x & 31) == 0) : contrib;
+    if (writer && lo[0] <= hi[0]) {
+      unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+      for (int c = 0; c < 3; ++c) {
+        atomicMin(&L[c], ord_key(lo[c]));
+        atomicMax(&L[3 + c], ord_key(hi[c]));
+      }
+    }
+  }
+
+  if (v.stats) {
+    for (int o = 16; o > 0; o >>= 1) {
+      live += __shfl_xor_sync(0xffffffffu, live, o);
+      ncontacts += __shfl_xor_sync(0xffffffffu, ncontacts, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (live) atomicAdd(&v.cnt->live_bonds, live);
+      if (ncontacts) atomicAdd(&v.cnt->contacts, ncontacts);
+    }
+  }
+}
+
+void launch_step_kernel(const DevView &v, int precision, int tpb, cudaStream_t s) {
+  uint64_t blocks = (v.N + 127) / 128;
+  (void)tpb;
+  if (!blocks) return;
+  if (precision == PD_FP32C)
+    k_step<PD_FP32C><<<(unsigned)blocks, 128, 0, s>>>(v);
+  else
+    k_step<PD_FP64><<<(unsigned)blocks, 128, 0, s>>>(v);
+}
+
+// ------------------------------------------------------------------------------------
+// end of step
+
+__global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const uint32_t *clamped,
+                                double *clamped_disp) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= v.P) return;
+  DevPart &P = v.parts[k];
+  const DevSimState &st = v.ss[P.sim];
+  const DevSimParams &sp = v.sp[P.sim];
+  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+  if (!st.active) return;
+  if (P.movable) {
+    for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
+  }
+  for (int c = 0; c < 3; ++c) {
+    L[c] = ord_key(INFINITY);
+    L[3 + c] = ord_key(-INFINITY);
+  }
+  // anchor of the FP32 local frame: this step's displacement of the particle's first node
+  if (v.disp32) {
+    double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
+    an[0] = v.disp[P.g0];
+    an[1] = v.disp[P.g0 + v.Ncap];
+    an[2] = v.disp[P.g0 + 2 * v.Ncap];
+  }
+  // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
+  // keeps this step's predicted displacement, saved for the readback
+  if (clamped_ptr) {
+    double jump = 0;
+    for (uint32_t c = clamped_ptr[k]; c < clamped_ptr[k + 1]; ++c) {
+      uint64_t g = clamped[c];
+      D3 d = ld3(v.disp, g, v.Ncap);
+      clamped_disp[3 * (uint64_t)c] = d.x;
+      clamped_disp[3 * (uint64_t)c + 1] = d.y;
+      clamped_disp[3 * (uint64_t)c + 2] = d.z;
+      if (P.movable) {
+        jump = fmax(jump, norm3(d));
+        st3(v.disp, g, v.Ncap, d3(0.0, 0.0, 0.0));
+        st3(v.vel_out, g, v.Ncap, d3(0.0, 0.0, 0.0));
+        st3(v.acc, g, v.Ncap, d3(0.0, 0.0, 0.0));
+      }
+    }
+    if (jump > 0) atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(jump));
+  }
+  // per-particle toggles for the next step (timeloop.h:481-498)
+  const uint32_t tn = st.t + 1;
+  const uint32_t kl = k - sp.p0;
+  if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
+    P.movable = 1;
+  if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
+      (uint32_t)sp.set_stoppable_ts == tn)
+    P.stoppable = 1;
+}
+
+// Flags a simulation uses in step t (the sticky toggles of timeloop.h:405-464).
+__device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t) {
+  if (sp.set_torque_ts != -1 && t == (uint32_t)sp.set_torque_ts) st.torque = 1;
+  if (sp.set_fracture_ts != -1 && t == (uint32_t)sp.set_fracture_ts) st.fracture = 1;
+  if (sp.set_self_contact_ts != -1 && t == (uint32_t)sp.set_self_contact_ts) st.self_contact = 1;
+  if (sp.set_damping_ts != -1 && t == (uint32_t)sp.set_damping_ts) st.damping = 1;
+  if (sp.set_zero_wall_speed_ts != -1 && t == (uint32_t)sp.set_zero_wall_speed_ts)
+    for (int c = 0; c < 6; ++c) st.spd[c] = 0;
+  if (sp.gradient_extforce) {
+    double sc = (double)t / (double)sp.extforce_maxstep;
+    if (sc > 1) sc = 1;
+    st.extf_scale = sc;
+  }
+}
+
+__global__ void k_end_sims(DevView v, double half_skin) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < v.S) {
+    const DevSimParams &sp = v.sp[s];
+    DevSimState &st = v.ss[s];
+    if (st.active) {
+      for (int c = 0; c < 6; ++c) st.wall[c] += st.spd[c] * sp.dt;  // timeloop.h:791-796
+      st.t += 1;
+      apply_sim_toggles(sp, st, st.t);
+      for (int c = 0; c < 18; ++c) st.react[c] = 0.0;  // Wall.setzero_reaction (timeloop.h:397)
+    }
+  }
+  if (s == 0) {
+    DevCounters &c = *v.cnt;
+    double stepmax = __longlong_as_double((long long)c.stepmax_bits);
+    if (c.rebuild) {
+      c.moved = 0.0;
+      c.rebuilds += 1;
+    } else {
+      c.moved += stepmax;
+    }
+    // clamped-node jumps recorded after the rebuild test count towards the next one
+    c.stepmax_bits = 0;
+    c.rebuild = 0;
+    (void)half_skin;
+  }
+}
+
+void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
+                     cudaStream_t s) {
+  const uint32_t *cptr = n_clamped ? clamped : nullptr;
+  const uint32_t *clist = n_clamped ? clamped + (v.P + 1) : nullptr;
+  k_end_particles<<<(v.P + 127) / 128, 128, 0, s>>>(v, cptr, clist, clamped_disp);
+  k_end_sims<<<(v.S + 127) / 128, 128, 0, s>>>(v, 0.0);
+}
+
+// ------------------------------------------------------------------------------------
+// auxiliary kernels
+
+// mean_CurrPos per particle (particle2.h:94-103): a sequential sum in node order.
+__global__ void k_centroids(DevView v) {
+  const uint32_t k = blockIdx.x;
+  const int c = threadIdx.x;
+  if (k >= v.P || c >= 3) return;
+  const DevPart &P = v.parts[k];
+  if (!v.ss[P.sim].torque) return;
+  double m = 0.0;
+  const double *pp = v.pos + c * v.Ncap, *dd = v.disp + c * v.Ncap;
+  for (uint32_t i = 0; i < P.n; ++i) m = m + (pp[P.g0 + i] + dd[P.g0 + i]);
+  const_cast<double *>(v.centroid)[3 * (uint64_t)k + c] = m / (double)P.n;
+}
+
+void launch_centroids(const DevView &v, cudaStream_t s) {
+  if (v.P) k_centroids<<<v.P, 32, 0, s>>>(v);
+}
+
+// gen_xi (particle2.h:241-257): xi = pos[q] - pos[i], |xi| and RN(1/|xi|) per SELL entry.
+__global__ void k_bond_constants(DevView v, double *bxi, double *bxin, double *brxin) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint64_t s = n >> 5;
+  const uint32_t lane = (uint32_t)(n & 31);
+  const uint64_t base = v.slice_ptr[s] + lane;
+  const D3 pi = ld3(v.pos, n, v.Ncap);
+  const int dg = v.deg[n];
+  for (int j = 0; j < dg; ++j) {
+    const uint64_t e = base + 32ull * j;
+    const uint32_t q = v.col[e];
+    D3 xi = ld3(v.pos, q, v.Ncap) - pi;
+    double xn = norm3(xi);
+    bxi[e] = xi.x;
+    bxi[e + v.E] = xi.y;
+    bxi[e + 2 * v.E] = xi.z;
+    bxin[e] = xn;
+    brxin[e] = __drcp_rn(xn);
+  }
+}
+
+void launch_bond_constants(const DevView &v, double *bxi, double *bxin, double *brxin, cudaStream_t s) {
+  uint64_t blocks = (v.N + 127) / 128;
+  if (blocks) k_bond_constants<<<(unsigned)blocks, 128, 0, s>>>(v, bxi, bxin, brxin);
+}
+
+// AABBs of all particles before the loop (timeloop.h:389-393).
+__global__ void k_init_lrtb_acc(DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t k = v.pid[n];
+  D3 cur = ld3(v.pos, n, v.Ncap) + ld3(v.disp, n, v.Ncap);
+  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+  atomicMin(&L[0], ord_key(cur.x));
+  atomicMin(&L[1], ord_key(cur.y));
+  atomicMin(&L[2], ord_key(cur.z));
+  atomicMax(&L[3], ord_key(cur.x));
+  atomicMax(&L[4], ord_key(cur.y));
+  atomicMax(&L[5], ord_key(cur.z));
+}
+__global__ void k_init_lrtb_fin(DevView v) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= v.P) return;
+  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+  for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
+  for (int c = 0; c < 3; ++c) {
+    L[c] = ord_key(INFINITY);
+    L[3 + c] = ord_key(-INFINITY);
+  }
+  if (v.disp32) {
+    const DevPart &P = v.parts[k];
+    double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
+    an[0] = v.disp[P.g0];
+    an[1] = v.disp[P.g0 + v.Ncap];
+    an[2] = v.disp[P.g0 + 2 * v.Ncap];
+  }
+}
+__global__ void k_reset_lrtb_next(DevView v) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= v.P) return;
+  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+  for (int c = 0; c < 3; ++c) {
+    L[c] = ord_key(INFINITY);
+    L[3 + c] = ord_key(-INFINITY);
+  }
+}
+
+void launch_init_lrtb(const DevView &v, cudaStream_t s) {
+  if (!v.P) return;
+  k_reset_lrtb_next<<<(v.P + 127) / 128, 128, 0, s>>>(v);
+  uint64_t blocks = (v.N + 127) / 128;
+  if (blocks) k_init_lrtb_acc<<<(unsigned)blocks, 128, 0, s>>>(v);
+  k_init_lrtb_fin<<<(v.P + 127) / 128, 128, 0, s>>>(v);
+}
+
+// Number of particle pairs the pair loop evaluates (timeloop.h:641-649), for the
+// progress line's "#contacts" column.
+__global__ void k_pairwise(DevView v) {
+  const uint32_t s = blockIdx.y;
+  if (s >= v.S) return;
+  const DevSimParams &sp = v.sp[s];
+  if (!v.ss[s].active) return;
+  const uint64_t np = sp.np;
+  const uint64_t total = np * (np - 1) / 2;
+  unsigned long long cnt = 0;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    // invert idx -> (i, j), i < j, lexicographic
+    uint64_t i = (uint64_t)((2.0 * np - 1 - sqrt((2.0 * np - 1) * (2.0 * np - 1) - 8.0 * idx)) / 2);
+    while (i > 0 && i * (2 * np - i - 1) / 2 > idx) --i;
+    while ((i + 1) * (2 * np - i - 2) / 2 <= idx) ++i;
+    uint64_t j = idx - i * (2 * np - i - 1) / 2 + i + 1;
+    const uint32_t a = sp.p0 + (uint32_t)i, b = sp.p0 + (uint32_t)j;
+    if (!(v.parts[a].movable || v.parts[b].movable)) continue;
+    if (intersects_fext(v.lrtb + 6 * (uint64_t)a, v.lrtb + 6 * (uint64_t)b, sp.Rc)) ++cnt;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&v.cnt->pairwise, cnt);
+}
+
+void launch_pairwise_count(const DevView &v, cudaStream_t s) {
+  if (!v.S) return;
+  dim3 grid(64, v.S);
+  k_pairwise<<<grid, 256, 0, s>>>(v);
+}
+
+}  // namespace pdg

@@ -1,0 +1,213 @@
+"""Synthetic aggregate setups in PeriDEM's setup schema.
+
+Particles are jittered cubic lattices clipped to a shape, with nodal volume h^3. Bonds follow
+exp_dict.py:544-567: every node pair with distance <= delta, as
+sorted(cKDTree(pos).query_pairs(delta)). Material constants use the 3D Silling-Askari
+formulas of material_dict.py:266-277 (cnot = 18K/(pi delta^4), snot = sqrt(5 G0/(9 K delta)),
+K = E/(3(1-2 nu))). The contact stiffness follows the examples' rule
+normal_stiffness = peridem_3d(contact_radius).cnot / contact_radius
+(examples/3D-HPC-aggregate-particle-breakage/setup.py:160), lowered when it would make the
+explicit contact update unstable at the configured dt; the value used is stored in the setup.
+
+Named workloads (seeded):
+  two_sphere   two R = 1 mm glass spheres, h = 0.1 mm, B moving at 20 m/s, dt 1e-8, 2000 steps
+  cubes125     5x5x5 randomly rotated 1 mm glass cubes, h = 0.125 mm, box walls, gravity
+               x1e4, dt 2e-8, 20000 steps
+  crush512     512 spheres/cubes/ellipsoids, sizes U[0.6, 1.4] mm, h from {0.05, 0.075, 0.1}
+               mm, 12 mm box whose top wall moves down at 1 m/s, dt 5e-9, 10000 steps
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .setupdata import Setup, concat
+
+GLASS = dict(E=72e9, nu=0.25, rho=2440.0, G0=135.0)
+STEEL = dict(E=190e9, nu=0.3, rho=8000.0, G0=22170.0)
+MM = 1e-3
+
+
+def material_3d(mat: dict, delta: float) -> dict:
+    K = mat["E"] / (3 * (1 - 2 * mat["nu"]))
+    return dict(rho=mat["rho"], delta=delta, cnot=18 * K / (np.pi * delta ** 4),
+                snot=float(np.sqrt(5 * mat["G0"] / (9 * K * delta))))
+
+
+def kn_rule(Rc: float) -> float:
+    """peridem_3d(Rc).cnot / Rc with the bulk modulus 2e9 of material_dict.peridem_3d."""
+    return (18 * 2.0e9 / (np.pi * Rc ** 4)) / Rc
+
+
+def stable_kn(Kn: float, rho_min: float, vol_max: float, dt: float, frac: float = 0.1) -> float:
+    return float(min(Kn, frac * rho_min / (vol_max * dt * dt)))
+
+
+def random_rotation(rng: np.random.Generator) -> np.ndarray:
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def lattice(kind: str, size, h: float) -> np.ndarray:
+    """Cubic lattice points of spacing h inside a shape centred at the origin.
+    kind: 'sphere' (size = diameter), 'cube' (edge), 'ellipsoid' (3 diameters),
+    'box' (3 edges)."""
+    if kind in ("cube", "box"):
+        e = np.broadcast_to(np.asarray(size, dtype=np.float64), (3,))
+        ax = [(np.arange(max(1, int(round(ek / h)))) + 0.5) * h - ek / 2 for ek in e]
+        X, Y, Z = np.meshgrid(*ax, indexing="ij")
+        return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    d = np.broadcast_to(np.asarray(size, dtype=np.float64), (3,))
+    r = d / 2
+    n = [int(math.ceil(rk / h)) for rk in r]
+    ax = [np.arange(-nk, nk + 1) * h for nk in n]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    P = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    keep = ((P / r) ** 2).sum(axis=1) <= 1.0 + 1e-12
+    return P[keep]
+
+
+def bonds(pos: np.ndarray, delta: float) -> np.ndarray:
+    """sorted(cKDTree(pos).query_pairs(delta)) as an (M,2) array (exp_dict.py:544-567)."""
+    from scipy.spatial import cKDTree
+    pr = cKDTree(pos).query_pairs(delta, output_type="ndarray")
+    if len(pr) == 0:
+        return np.zeros((0, 2), dtype=np.uint32)
+    order = np.lexsort((pr[:, 1], pr[:, 0]))
+    return pr[order].astype(np.uint32)
+
+
+def boundary_nodes(pos: np.ndarray, conn: np.ndarray, Rc: float) -> np.ndarray:
+    """Nodes within Rc of a surface node (gen_nonlocal_boundry_nodes, exp_dict.py:1231-1248);
+    surface nodes are those with a degree below 90% of the particle's maximum."""
+    from scipy.spatial import cKDTree
+    n = len(pos)
+    deg = np.bincount(conn.reshape(-1).astype(np.int64), minlength=n) if len(conn) else np.zeros(n, int)
+    edge = np.nonzero(deg < 0.9 * max(1, deg.max()))[0]
+    if len(edge) == 0:
+        return np.zeros(0, np.uint32)
+    t = cKDTree(pos)
+    hits = t.query_ball_point(pos[edge], Rc)
+    s = sorted(set(int(j) for lst in hits for j in lst))
+    return np.asarray(s, dtype=np.uint32)
+
+
+def make_particle(local: np.ndarray, h: float, mat: dict, delta_factor: float, rng, jitter: float,
+                  center, rotation=None, vel=(0, 0, 0), Rc: float | None = None, **flags) -> dict:
+    P = local.copy()
+    if rotation is not None:
+        P = P @ rotation.T
+    if jitter:
+        P = P + rng.uniform(-jitter * h, jitter * h, size=P.shape)
+    P = P + np.asarray(center, dtype=np.float64)
+    delta = delta_factor * h
+    m = material_3d(mat, delta)
+    conn = bonds(P, delta)
+    n = len(P)
+    part = dict(pos=P, vol=np.full(n, h ** 3), conn=conn, vel=np.tile(np.asarray(vel, float), (n, 1)), **m)
+    part["h"] = h
+    if Rc is not None:
+        part["bdry"] = boundary_nodes(P, conn, Rc)
+    part.update(flags)
+    return part
+
+
+def finish(parts, Rc, dt, zeta=0.8, mu=0.3, wall=None, kn=None) -> Setup:
+    vol_max = max(float(np.max(p["vol"])) for p in parts)
+    rho_min = min(p["rho"] for p in parts)
+    Kn = kn if kn is not None else stable_kn(kn_rule(Rc), rho_min, vol_max, dt)
+    if wall is None:
+        # walls off, but with a geometry: load_wall<3> leaves the wall fields unset when
+        # geom_wall_info has a single entry (load_hdf5.h:159-177)
+        wall = dict(allow=0, geom=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0])
+    s = concat(parts, dict(contact_radius=Rc, normal_stiffness=Kn, damping_ratio=zeta,
+                           friction_coefficient=mu), wall)
+    s.meta["h"] = [p["h"] for p in parts]
+    return s
+
+
+# ---------------------------------------------------------------------------------------
+# named workloads: (Setup, config overrides)
+
+def base_config(dt: float, steps: int, **over) -> dict:
+    c = dict(dt=dt, timesteps=steps, modulo=max(1, steps // 10), enable_fracture=1, self_contact=1,
+             nl_bdry_only=0, allow_damping=1, allow_friction=1, save_file=0)
+    c.update(over)
+    return c
+
+
+def two_sphere(R=1.0 * MM, h=0.1 * MM, v=20.0, gap=0.2, seed=0, steps=2000, dt=1e-8, walls=False):
+    """Config 0: sphere B moves at -v along x towards sphere A at rest; surface gap gap*h."""
+    rng = np.random.default_rng(seed)
+    Rc = 0.5 * h
+    loc = lattice("sphere", 2 * R, h)
+    A = make_particle(loc, h, GLASS, 3.0, rng, 0.05, (0, 0, 0), Rc=Rc)
+    B = make_particle(loc, h, GLASS, 3.0, rng, 0.05, (2 * R + gap * h, 0, 0), vel=(-v, 0, 0), Rc=Rc)
+    wall = None
+    if walls:
+        L = 3 * R
+        wall = dict(allow=1, geom=[-1.5 * R, -1.02 * R, -1.02 * R, L + 0.5 * R, 1.02 * R, 1.02 * R])
+    s = finish([A, B], Rc, dt, wall=wall)
+    s.meta["name"] = "two_sphere"
+    return s, base_config(dt, steps)
+
+
+def cubes125(n=5, edge=1.0 * MM, h=0.125 * MM, seed=1, steps=20000, dt=2e-8, g=9.81 * 1e4, gap=0.9 * MM):
+    """Config 1: n^3 randomly rotated cubes in a walled box under scaled gravity."""
+    rng = np.random.default_rng(seed)
+    Rc = 0.5 * h
+    loc = lattice("cube", edge, h)
+    pitch = edge * math.sqrt(3) + gap * 0.2
+    parts = []
+    for iz in range(n):
+        for iy in range(n):
+            for ix in range(n):
+                c = ((ix - (n - 1) / 2) * pitch, (iy - (n - 1) / 2) * pitch, (iz - (n - 1) / 2) * pitch)
+                p = make_particle(loc, h, GLASS, 3.0, rng, 0.05, c, rotation=random_rotation(rng), Rc=Rc)
+                npn = len(p["pos"])
+                # gravity as extforce = rho*g (force density) and initial acc = g, the convention
+                # of examples/3D-HPC-aggregate-particle-breakage/setup.py:135-152
+                p["extforce"] = np.tile([0.0, 0.0, -g * p["rho"]], (npn, 1))
+                p["acc"] = np.tile([0.0, 0.0, -g], (npn, 1))
+                parts.append(p)
+    half = n * pitch / 2 + 0.5 * Rc
+    wall = dict(allow=1, geom=[-half, -half, -half, half, half, half + pitch])
+    s = finish(parts, Rc, dt, wall=wall)
+    s.meta["name"] = "cubes125"
+    return s, base_config(dt, steps)
+
+
+def crush512(n=8, box=12.0 * MM, seed=2, steps=10000, dt=5e-9, hs=(0.05 * MM, 0.075 * MM, 0.1 * MM),
+             smin=0.6 * MM, smax=1.4 * MM, wall_speed=-1.0):
+    """Config 2: n^3 particles of random shape/size/resolution in a box; top wall moves down."""
+    rng = np.random.default_rng(seed)
+    Rc = 0.5 * min(hs)
+    pitch = box / n
+    parts = []
+    for iz in range(n):
+        for iy in range(n):
+            for ix in range(n):
+                kind = ("sphere", "cube", "ellipsoid")[int(rng.integers(3))]
+                h = float(hs[int(rng.integers(len(hs)))])
+                if kind == "ellipsoid":
+                    size = rng.uniform(smin, smax, size=3)
+                else:
+                    size = float(rng.uniform(smin, smax))
+                loc = lattice(kind, size, h)
+                c = np.array([(ix + 0.5) * pitch, (iy + 0.5) * pitch, (iz + 0.5) * pitch]) - box / 2
+                c = c + rng.uniform(-0.02, 0.02, size=3) * pitch
+                p = make_particle(loc, h, GLASS, 3.0, rng, 0.05, c, rotation=random_rotation(rng), Rc=None)
+                parts.append(p)
+    half = box / 2
+    wall = dict(allow=1, geom=[-half, -half, -half, half, half, half])
+    s = finish(parts, Rc, dt, wall=wall)
+    s.meta["name"] = "crush512"
+    return s, base_config(dt, steps, speed_wall_z_max=wall_speed)
+
+
+WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512}

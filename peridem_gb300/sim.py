@@ -1,0 +1,118 @@
+"""Python handle over the C-ABI (include/peridem_gb300.h): the in-process counterpart of
+run_timeloop<3> (src/particle/timeloop.h:231-965). Arrays are numpy, N*3 row vectors in
+particle file order, like the reference's vector<Matrix<double,1,3>>."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import PdError, PD_FP64, PD_FP32C, default_config, lib, ptr, setup_struct
+from .setupdata import Setup
+
+PRECISIONS = {"fp64": PD_FP64, "fp32c": PD_FP32C}
+
+
+def make_config(over: dict | None = None) -> _capi.PdConfig:
+    return default_config(**(over or {}))
+
+
+class Sim:
+    """One simulation resident on the GPU."""
+
+    def __init__(self, setup: Setup, config: dict | _capi.PdConfig | None = None, precision: str = "fp64",
+                 handle=None):
+        self.setup = setup
+        self.cfg = config if isinstance(config, _capi.PdConfig) else make_config(config)
+        self.precision = precision
+        L = lib()
+        if handle is not None:
+            self.h = handle
+        else:
+            st, keep = setup_struct(setup)
+            h = C.c_void_p()
+            rc = L.pd_create_from_arrays(C.byref(st), C.byref(self.cfg), PRECISIONS[precision], C.byref(h))
+            del keep
+            if rc != 0:
+                raise PdError(rc, L.pd_global_error().decode())
+            self.h = h
+        n = C.c_uint64()
+        p = C.c_uint32()
+        L.pd_num_nodes(self.h, C.byref(n), C.byref(p))
+        self.N = n.value
+        self.P = p.value
+
+    # -- lifecycle ------------------------------------------------------------------------
+    def _ck(self, rc: int):
+        if rc != 0:
+            raise PdError(rc, lib().pd_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pd_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- stepping --------------------------------------------------------------------------
+    def step(self, n: int = 1, sync: bool = True, timeout_ms: int = -1):
+        self._ck(lib().pd_step(self.h, int(n)))
+        if sync:
+            self.sync(timeout_ms)
+
+    def sync(self, timeout_ms: int = -1):
+        self._ck(lib().pd_sync(self.h, int(timeout_ms)))
+
+    def set_stream(self, stream_ptr: int | None):
+        self._ck(lib().pd_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def tune(self, skin_frac: float = 0.0, cand_cap: int = 0, tpb: int = 0, stats: int = -1, graphs: int = -1):
+        self._ck(lib().pd_set_tuning(self.h, float(skin_frac), int(cand_cap), int(tpb), int(stats), int(graphs)))
+
+    # -- state -----------------------------------------------------------------------------
+    def state(self) -> dict:
+        out = {k: np.empty((self.N, 3)) for k in ("curpos", "vel", "acc", "force", "disp")}
+        self._ck(lib().pd_get_state(self.h, ptr(out["curpos"]), ptr(out["vel"]), ptr(out["acc"]), ptr(out["force"])))
+        self._ck(lib().pd_get_disp(self.h, ptr(out["disp"])))
+        return out
+
+    def set_state(self, disp=None, vel=None, acc=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (disp, vel, acc)]
+        self._ck(lib().pd_set_state(self.h, *(ptr(a) for a in arrs)))
+
+    def connectivity(self, p: int) -> np.ndarray:
+        n = C.c_uint64()
+        self._ck(lib().pd_get_connectivity(self.h, p, None, 0, C.byref(n)))
+        out = np.empty((n.value, 2), dtype=np.uint32)
+        self._ck(lib().pd_get_connectivity(self.h, p, ptr(out), n.value, C.byref(n)))
+        return out
+
+    def wall(self) -> tuple[np.ndarray, np.ndarray]:
+        w = np.empty(6)
+        r = np.empty((6, 3))
+        self._ck(lib().pd_get_wall(self.h, ptr(w), ptr(r)))
+        return w, r
+
+    def aabb(self) -> np.ndarray:
+        out = np.empty((self.P, 6))
+        self._ck(lib().pd_get_aabb(self.h, ptr(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = _capi.PdStats()
+        self._ck(lib().pd_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def step_bytes(self) -> float:
+        return float(lib().pd_step_bytes(self.h))

@@ -1,0 +1,111 @@
+"""GPU parity against the CPU oracle, through the C-ABI (peridem_gb300.sim.Sim wraps
+include/peridem_gb300.h).
+
+FP64 form: bit-exact. Every saved quantity of the reference's frames (CurrPos, vel, acc,
+force, Connectivity, wall position) must be identical; the wall reaction, which the GPU sums
+with atomics in a different order, must agree to 1e-12 relative.
+FP32-compensated form: displacements within 1e-5 of the largest displacement magnitude and
+broken-bond sets within 0.1% of the FP64 oracle's."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from peridem_gb300.sim import Sim
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare_exact(name, s, sim, orc, t):
+    a = sim.state()
+    b = orc.state()
+    for k in ("curpos", "vel", "acc", "force", "disp"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=f"{name} t={t} {k}")
+    for p in range(s.n_particles):
+        np.testing.assert_array_equal(sim.connectivity(p), orc.connectivity(p), err_msg=f"{name} t={t} conn {p}")
+    wg, rg = sim.wall()
+    wo, ro = orc.wall()
+    np.testing.assert_array_equal(wg, wo)
+    scale = max(1e-300, np.abs(ro).max())
+    assert np.abs(rg - ro).max() <= 1e-12 * scale, f"{name} reaction"
+    np.testing.assert_array_equal(sim.aabb(), orc.aabb())
+
+
+@pytest.mark.parametrize("name", sorted(cases.CASES))
+def test_fp64_bitexact(name):
+    s, cfg = cases.CASES[name]()
+    steps = cfg["timesteps"]
+    sim = Sim(s, cfg, "fp64")
+    sim.tune(stats=1)
+    orc = O.Oracle(s, cfg)
+    chunk = max(1, steps // 3)
+    t = 0
+    while t < steps:
+        k = min(chunk, steps - t)
+        sim.step(k)
+        orc.step(k)
+        t += k
+        _compare_exact(name, s, sim, orc, t)
+        st = sim.stats()
+        oc = orc.counts()
+        assert st["live_bonds"] == oc["live_bonds"]
+        assert st["contacts"] == oc["contacts"]
+    sim.close()
+
+
+@pytest.mark.parametrize("name", ["impact_walls", "cubes_gravity"])
+def test_fp64_no_graph_same_as_graph(name):
+    s, cfg = cases.CASES[name]()
+    a = Sim(s, cfg, "fp64")
+    b = Sim(s, cfg, "fp64")
+    b.tune(graphs=0)
+    a.step(25)
+    b.step(25)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k])
+
+
+@pytest.mark.parametrize("skin", [0.05, 0.2, 1.0])
+def test_fp64_skin_does_not_change_results(skin):
+    s, cfg = cases.impact_free()
+    a = Sim(s, cfg, "fp64")
+    a.tune(skin_frac=skin)
+    orc = O.Oracle(s, cfg)
+    a.step(cfg["timesteps"])
+    orc.step(cfg["timesteps"])
+    np.testing.assert_array_equal(a.state()["curpos"], orc.state()["curpos"])
+
+
+def test_two_sphere_full_size_bitexact():
+    """Config 0 at full size (2 x 4169 nodes, 7.4e5 bonds), first 60 steps."""
+    from peridem_gb300 import gen
+    s, cfg = gen.two_sphere()
+    sim = Sim(s, cfg, "fp64")
+    orc = O.Oracle(s, cfg)
+    sim.step(60)
+    orc.step(60)
+    a, b = sim.state(), orc.state()
+    for k in ("curpos", "vel", "acc", "force"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("name", ["impact_free", "cubes_gravity", "impact_walls"])
+def test_fp32c_within_tolerance(name):
+    s, cfg = cases.CASES[name]()
+    steps = cfg["timesteps"]
+    sim = Sim(s, cfg, "fp32c")
+    orc = O.Oracle(s, cfg)
+    sim.step(steps)
+    orc.step(steps)
+    a, b = sim.state(), orc.state()
+    dref = max(np.abs(b["disp"]).max(), 1e-300)
+    err = np.abs(a["disp"] - b["disp"]).max() / dref
+    assert err <= 1e-5, f"{name}: relative displacement error {err:.3e}"
+    n_or = sum(len(orc.connectivity(p)) for p in range(s.n_particles))
+    mism = 0
+    for p in range(s.n_particles):
+        ca = {tuple(r) for r in sim.connectivity(p)}
+        cb = {tuple(r) for r in orc.connectivity(p)}
+        mism += len(ca ^ cb)
+    assert mism <= 1e-3 * max(1, n_or), f"{name}: {mism} bond mismatches of {n_or}"
