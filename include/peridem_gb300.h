@@ -200,6 +200,13 @@ int pd_clear_device_errors(pd_sim *sim);
 
 /* Algorithmic byte count of one step (4.125 B per live directed bond + 224 B per node). */
 double pd_step_bytes(const pd_sim *sim);
+/* Phase timing (the reference's per-block wall clock, timeloop.h:909-947, per kernel
+ * phase): runs nsteps real steps as separate launches with CUDA events between phases and
+ * returns the summed device milliseconds in phase_ms[4] = {predictor, broad phase, fused
+ * force+corrector kernel, end-of-step}. */
+int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
+/* Live directed bonds of movable particles (the bond-update count of the next step). */
+int pd_count_live_bonds(pd_sim *sim, uint64_t *live);
 
 #ifdef __cplusplus
 }

@@ -110,6 +110,8 @@ SIGNATURES = [
     ("pd_set_tuning", C.c_int, [_P, _f64, _u32, C.c_int, C.c_int, C.c_int]),
     ("pd_clear_device_errors", C.c_int, [_P]),
     ("pd_step_bytes", _f64, [_P]),
+    ("pd_profile_steps", C.c_int, [_P, _u32, _P]),
+    ("pd_count_live_bonds", C.c_int, [_P, C.POINTER(_u64)]),
 ]
 
 _lib = None

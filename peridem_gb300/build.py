@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("pd_kernels.cu", ["-fmad=false"]),
     ("pd_broadphase.cu", []),
+    ("pd_fp32c.cu", []),
     ("pd_engine.cu", ["-fmad=false"]),
     ("pd_capi.cpp", []),
     ("pd_config.cpp", []),

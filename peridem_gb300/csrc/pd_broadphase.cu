@@ -54,6 +54,8 @@ __global__ void k_bp_decide(DevView v, double half_skin) {
     DevCounters &c = *v.cnt;
     double stepmax = __longlong_as_double((long long)c.stepmax_bits);
     c.rebuild = (c.moved + stepmax > half_skin) ? 1u : 0u;
+    c.contacts = 0;    // per-step counters
+    c.live_bonds = 0;
   }
   for (uint32_t s = t; s < v.S; s += gridDim.x * blockDim.x)
     for (int k = 0; k < 18; ++k) v.ss[s].react[k] = 0.0;

@@ -228,3 +228,18 @@ double pd_step_bytes(const pd_sim *s) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int pd_profile_steps(pd_sim *s, uint32_t nsteps, double *phase_ms) {
+  if (!s || !phase_ms) return fail_global(PD_EINVAL, "null argument");
+  for (int i = 0; i < 4; ++i) phase_ms[i] = 0.0;
+  return s->eng.profile(nsteps, phase_ms);
+}
+
+int pd_count_live_bonds(pd_sim *s, uint64_t *live) {
+  if (!s || !live) return fail_global(PD_EINVAL, "null argument");
+  return s->eng.count_live_bonds(live);
+}
+
+}  // extern "C"

@@ -1,0 +1,196 @@
+// pd_device.cuh -- device helpers shared by the step kernels: SoA loads/stores and the
+// reference's contact, wall and box tests (contact.h), written in its FP64 evaluation order.
+#ifndef PD_DEVICE_CUH
+#define PD_DEVICE_CUH
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+
+#include "pd_engine.h"
+#include "pd_math.cuh"
+
+namespace pdg {
+
+
+__device__ __forceinline__ D3 ld3(const double *a, uint64_t n, uint64_t cap) {
+  return d3(a[n], a[n + cap], a[n + 2 * cap]);
+}
+__device__ __forceinline__ void st3(double *a, uint64_t n, uint64_t cap, D3 v) {
+  a[n] = v.x;
+  a[n + cap] = v.y;
+  a[n + 2 * cap] = v.z;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// intersects_box_fext<3> (contact.h:1143-1183): only box A is extended by c.
+__device__ __forceinline__ bool intersects_fext(const double *A, const double *B, double c) {
+  double A_min_x = A[0] - c, A_min_y = A[1] - c, A_min_z = A[2] - c;
+  double A_max_x = A[3] + c, A_max_y = A[4] + c, A_max_z = A[5] + c;
+  return (A_min_x <= B[3]) && (A_max_x >= B[0]) && (A_max_y >= B[1]) && (A_min_y <= B[4]) &&
+         (A_min_z <= B[5]) && (A_max_z >= B[2]);
+}
+
+// within_interior_fext (contact.h:1229-1243) with its 2D indexing of 3D boxes.
+__device__ __forceinline__ bool within_interior(const double *A, const double *B, double c) {
+  double A_Left = A[0] - c, A_Right = A[1] + c, A_Top = A[2] + c, A_Bottom = A[3] - c;
+  return (B[0] < A_Left) && (A_Right < B[1]) && (B[2] > A_Top) && (B[3] < A_Bottom);
+}
+
+// Normal, damping and friction force densities of one node-node contact, computed from
+// the point of view of the "C" node as update_contact_force_by_boundary does
+// (contact.h:798-934). fc is always set; fd/ff only when has_fd/has_ff.
+struct PairForce {
+  D3 fc, fd, ff;
+  bool has_fd, has_ff;
+};
+
+__device__ __forceinline__ void pair_force(D3 dir, double dn, double len_ref, double sc,
+                                           double N_vol, double rho_C, D3 velC, D3 velN,
+                                           const DevSimParams &sp, const DevSimState &st,
+                                           PairForce &o) {
+  D3 unit = dir / dn;
+  double s = (dn - len_ref) / len_ref;
+  double fmag = (sc * s) * N_vol;
+  o.fc = fmag * unit;
+  double fcn = norm3(o.fc);
+  o.has_fd = false;
+  o.has_ff = false;
+  if (st.damping) {
+    D3 rel = velC - velN;
+    double rvp = dot3(rel, unit);
+    D3 rvn = rvp * unit;
+    double dc = (sp.zeta2 * sqrt(sc * rho_C)) * sqrt(N_vol);
+    o.fd = (-dc) * rvn;
+    o.has_fd = true;
+  }
+  if (st.friction) {
+    D3 rel = velC - velN;
+    double rd = dot3(rel, unit);
+    D3 rvt = rel - rd * unit;
+    double rvtn = norm3(rvt);
+    if (rvtn > 0) {
+      D3 tu = rvt / norm3(rvt);
+      double fm = (-sp.mu) * fcn;
+      if (rvtn < ((sp.mu * fcn) * sp.dt) / rho_C) fm = ((-rvtn) / rho_C) / sp.dt;
+      o.ff = fm * tu;
+      o.has_ff = true;
+    }
+  }
+}
+
+// segment_mass<3> + wall_side_force_update<3> (contact.h:14-39, 381-502) for one face.
+__device__ __forceinline__ void wall_face(double dist, int dir, D3 vel, double vol, double rho,
+                                          D3 &f, double wspeed, int face,
+                                          const DevSimParams &sp, DevSimState &st, bool reaction) {
+  const double R = sp.Rc;
+  if (!(fabs(dist) <= R)) return;
+  double d = fabs(dist);
+  double rd = R - d;
+  double area = (sp.pi3 * (rd * rd)) * (2 * R - d);
+  double w = R * R - d * d;
+  double I = sp.pi4 * (w * w);
+  double cen = I / area;
+  double crc = R - cen;
+  double pcrc = (crc > 0 ? crc : 0);
+  double F = (sp.Kn * pcrc) * area;
+  double c_sign = (dist > 0 ? 1.0 : -1.0);
+  double r0 = 0, r1 = 0, r2 = 0;  // reaction contributions in dir, t1, t2
+  {
+    double a = c_sign * F;
+    set_comp(f, dir, comp(f, dir) + a);
+    r0 -= ((vol * c_sign) * F);
+  }
+  D3 rel = vel;
+  set_comp(rel, dir, comp(rel, dir) - wspeed);
+  const int t1 = (dir + 1) % 3, t2 = (dir + 2) % 3;
+  if (st.friction) {
+    double v1 = comp(rel, t1), v2 = comp(rel, t2);
+    double vn = sqrt(v1 * v1 + v2 * v2);
+    if (vn > 0) {
+      double u1 = v1 / vn, u2 = v2 / vn;
+      double aF = fabs(F);
+      double ff1 = ((-sp.mu) * aF) * u1;
+      double ff2 = ((-sp.mu) * aF) * u2;
+      if (vn < ((sp.mu * aF) * sp.dt) / rho) {
+        double g = ((-vn) / rho) / sp.dt;
+        ff1 = g * u1;
+        ff2 = g * u2;
+      }
+      set_comp(f, t1, comp(f, t1) + ff1);
+      set_comp(f, t2, comp(f, t2) + ff2);
+      r1 -= (vol * ff1);
+      r2 -= (vol * ff2);
+    }
+  }
+  if (st.damping) {
+    double dc = ((sp.zeta2) * sqrt(sp.Kn * rho)) * sqrt(fabs(area));
+    double df = (-dc) * comp(rel, dir);
+    set_comp(f, dir, comp(f, dir) + df);
+    r0 -= (vol * df);
+  }
+  if (reaction) {
+    atomicAdd(&st.react[3 * face + dir], r0);
+    if (r1 != 0) atomicAdd(&st.react[3 * face + t1], r1);
+    if (r2 != 0) atomicAdd(&st.react[3 * face + t2], r2);
+  }
+}
+
+// Does row n hold a live bond to global node m? (std::find over NbdArr, contact.h:783)
+__device__ __forceinline__ bool row_has_live(const DevView &v, uint64_t n, uint32_t m) {
+  const uint64_t s = n >> 5;
+  const uint32_t lane = (uint32_t)(n & 31);
+  const uint64_t base = v.slice_ptr[s] + lane;
+  const uint64_t mbase = v.slice_ptr[s] >> 5;
+  const int dg = v.deg[n];
+  for (int j = 0; j < dg; ++j) {
+    if (v.col[base + 32ull * j] == m) return (v.mask[mbase + j] >> lane) & 1u;
+  }
+  return false;
+}
+
+
+__device__ __forceinline__ unsigned int fkey(float x) {
+  unsigned int u = __float_as_uint(x);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fval(unsigned int k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+__device__ __forceinline__ bool nonfinite(double x) {
+  return ((__double2hiint(x) >> 20) & 0x7FF) == 0x7FF;
+}
+
+// End-of-step work of the FP32 form for one particle: AABB from the local-frame keys
+// (widened by a few float ulps each way), new anchor, walls in the new local frame.
+__device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const DevPart &P, const DevSimState &st) {
+  double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
+  unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
+  if (P.movable) {
+    for (int c = 0; c < 3; ++c) {
+      const float lo = fval(L[c]), hi = fval(L[3 + c]);
+      const double base = P.anchor_pos[c] + an[c];
+      const double e = 8.0 * (double)FLT_EPSILON * fmax(fabs((double)lo), fabs((double)hi)) + 1e-30;
+      v.lrtb[6 * (uint64_t)k + c] = base + (double)lo - e;
+      v.lrtb[6 * (uint64_t)k + 3 + c] = base + (double)hi + e;
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    L[c] = fkey(INFINITY);
+    L[3 + c] = fkey(-INFINITY);
+  }
+  an[0] = v.disp[P.g0];
+  an[1] = v.disp[P.g0 + v.Ncap];
+  an[2] = v.disp[P.g0 + 2 * v.Ncap];
+  float *wl = v.wall_local + 6 * (uint64_t)k;
+  for (int f = 0; f < 6; ++f) {
+    const int c = f % 3;
+    wl[f] = (float)(st.wall[f] - (P.anchor_pos[c] + an[c]));
+  }
+}
+
+}  // namespace pdg
+#endif

@@ -78,6 +78,10 @@ DevView Engine::view(int cur) const {
   v.disp32 = d_disp32_;
   v.anchor = d_anchor_;
   v.break_band = 1e-4;
+  v.f_extra = d_f_extra_;
+  v.extra_flag = d_extra_flag_;
+  v.wall_local = d_wall_local_;
+  v.lrtb_local_next = d_lrtb_local_;
   v.parts = d_parts_;
   v.lrtb = d_lrtb_;
   v.lrtb_next = d_lrtb_next_;
@@ -249,6 +253,9 @@ int Engine::alloc_and_upload() {
       P.breakable = s.breakable[p];
       P.stoppable = s.stoppable[p];
       P.break_bonds = 1;  // simulate3d.cpp:137-139
+      P.has_ext = 0;
+      for (uint64_t q = s.node_offset[p]; q < s.node_offset[p + 1] && !P.has_ext; ++q)
+        if (s.ext[3 * q] != 0.0 || s.ext[3 * q + 1] != 0.0 || s.ext[3 * q + 2] != 0.0) P.has_ext = 1;
       if (P.n == 0) {
         err = "particle " + std::to_string(p) + " has no nodes";
         return PD_EINVAL;
@@ -412,6 +419,11 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_pos32_, C, err));
     PD_TRY(dalloc(this, allocs_, &d_disp32_, C, err));
     PD_TRY(dalloc(this, allocs_, &d_anchor_, 3ull * P_, err));
+    PD_TRY(dalloc(this, allocs_, &d_f_extra_, 3 * C, err));
+    PD_TRY(dalloc(this, allocs_, &d_extra_flag_, C, err));
+    PD_TRY(dalloc(this, allocs_, &d_wall_local_, 6ull * P_, err));
+    PD_TRY(dalloc(this, allocs_, &d_lrtb_local_, 6ull * P_, err));
+    PD_TRY(check(cudaMemset(d_extra_flag_, 0, C), "memset extra flag"));
     PD_TRY(up(d_pos32_, p32.data(), C * sizeof(float4), "upload pos32"));
     PD_TRY(check(cudaMemset(d_disp32_, 0, C * sizeof(float4)), "memset disp32"));
   }
@@ -735,6 +747,58 @@ int Engine::clear_device_errors() {
 
 double Engine::step_bytes(uint64_t live) const {
   return 4.125 * (double)live + 224.0 * (double)N_;
+}
+
+}  // namespace pdg
+
+namespace pdg {
+
+int Engine::profile(uint32_t nsteps, double *phase_ms) {
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; ++i)
+    if (cudaEventCreate(&ev[i]) != cudaSuccess) return check(cudaGetLastError(), "event create");
+  int rc = PD_OK;
+  for (uint32_t k = 0; k < nsteps && rc == PD_OK; ++k) {
+    DevView v = view(cur_);
+    cudaStream_t s = stream_;
+    cudaEventRecord(ev[0], s);
+    launch_predict(v, tpb_, s);
+    if (torque_possible_) launch_centroids(v, s);
+    cudaEventRecord(ev[1], s);
+    launch_bp_decide(v, half_skin_, s);
+    launch_broadphase(v, bp_, s);
+    cudaEventRecord(ev[2], s);
+    launch_step_kernel(v, precision_, tpb_, s);
+    cudaEventRecord(ev[3], s);
+    if (stats_) launch_pairwise_count(v, s);
+    launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, s);
+    cudaEventRecord(ev[4], s);
+    rc = check(cudaEventSynchronize(ev[4]), "profile step");
+    if (rc != PD_OK) break;
+    for (int i = 0; i < 4; ++i) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+      phase_ms[i] += ms;
+    }
+    cur_ ^= 1;
+    ++steps_done_;
+  }
+  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  return rc;
+}
+
+int Engine::count_live_bonds(uint64_t *live) {
+  unsigned long long *d = nullptr;
+  PD_TRY(check(cudaMalloc(&d, 8), "alloc"));
+  cudaMemsetAsync(d, 0, 8, stream_);
+  launch_count_live(view(cur_), d, stream_);
+  unsigned long long h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  cudaFree(d);
+  PD_TRY(check(e, "count live bonds"));
+  *live = h;
+  return PD_OK;
 }
 
 }  // namespace pdg

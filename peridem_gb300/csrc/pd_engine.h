@@ -41,6 +41,8 @@ struct DevPart {
   double rho, irho, cnot, snot, tval;
   int32_t movable, breakable, stoppable, break_bonds;
   double anchor_pos[3];  // FP32 form: position of the anchor node
+  int32_t has_ext;       // any non-zero extforce in this particle
+  int32_t pad_;
 };
 
 // Per-simulation constants (Contact, RectWall and Timeloop fields after apply_config).
@@ -106,6 +108,10 @@ struct DevView {
   float4 *pos32, *disp32;
   const double *anchor;  // [P][3] anchor displacement for the current step
   double break_band;     // relative band around snot where the FP64 stretch decides
+  double *f_extra;       // [3][Ncap] FP64 non-bond force density of flagged nodes
+  uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
+  float *wall_local;     // [P][6] wall planes in each particle's local frame
+  unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
   // particles / sims
   DevPart *parts;
   double *lrtb, *lrtb_next;  // [P][6]; lrtb_next holds ordered-integer min/max keys
@@ -167,6 +173,12 @@ class Engine {
   // skin_frac <= 0, cand_cap == 0, tpb <= 0, stats < 0, use_graphs < 0 keep the setting
   int set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, int use_graphs);
   int clear_device_errors();
+  // Runs nsteps steps as separate launches with CUDA events between the phases and adds the
+  // per-phase device time (ms) to phase_ms[0..3]: predictor, broad phase, fused step
+  // kernel, end-of-step kernels.
+  int profile(uint32_t nsteps, double *phase_ms);
+  // Live directed bonds of movable particles (popcount of the live masks).
+  int count_live_bonds(uint64_t *live);
   double step_bytes(uint64_t live_bonds) const;
   uint64_t initial_bonds() const { return initial_bonds_; }
   uint64_t num_nodes() const { return N_; }
@@ -220,6 +232,10 @@ class Engine {
   double *d_bxi_ = nullptr, *d_bxin_ = nullptr, *d_brxin_ = nullptr;
   float4 *d_pos32_ = nullptr, *d_disp32_ = nullptr;
   double *d_anchor_ = nullptr;
+  double *d_f_extra_ = nullptr;
+  uint8_t *d_extra_flag_ = nullptr;
+  float *d_wall_local_ = nullptr;
+  unsigned int *d_lrtb_local_ = nullptr;
   DevPart *d_parts_ = nullptr;
   double *d_lrtb_ = nullptr, *d_lrtb_next_ = nullptr, *d_centroid_ = nullptr;
   DevSimParams *d_sp_ = nullptr;
@@ -237,6 +253,7 @@ class Engine {
 // kernel launchers (pd_kernels.cu / pd_broadphase.cu)
 void launch_predict(const DevView &v, int tpb, cudaStream_t s);
 void launch_step_kernel(const DevView &v, int precision, int tpb, cudaStream_t s);
+void launch_step_fp32c(const DevView &v, cudaStream_t s);
 void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
                      cudaStream_t s);
 void launch_centroids(const DevView &v, cudaStream_t s);
@@ -245,6 +262,7 @@ void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s);
 void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s);
 void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
+void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
 
 }  // namespace pdg
 #endif

@@ -1,0 +1,271 @@
+// pd_fp32c.cu -- the FP32-compensated form of the fused step (compiled with contraction on).
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate, so this form keeps FP64 to what needs it:
+//   k_extra32  the non-bond force density of the nodes that have any this step -- contact
+//              partners, a wall face within reach, extforce, torque -- in FP64 with the
+//              reference's formulas (contact.h:744-942, 1057-1124; timeloop.h:582-633). A
+//              float test in each particle's local frame skips faces that are out of reach.
+//   k_bond32   per node: PD bond forces in FP32 with the cancellation-free stretch
+//              s = (2 xi.eta + eta.eta) / ((|xi+eta| + |xi|) |xi|) on anchor-relative FP32
+//              positions and displacements, Kahan-compensated FP32 sums; the stretch-vs-snot
+//              decision is re-taken in FP64 inside a relative band around snot; then the
+//              FP64 velocity-Verlet corrector (timeloop.h:661-781) and the particle AABB in the
+//              local frame (FP32, widened outwards when converted back).
+// The summation order is not the reference's (bonds, then the FP64 extras); results agree
+// with the FP64 form within the stated tolerance.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+
+#include "pd_device.cuh"
+#include "pd_engine.h"
+#include "pd_math.cuh"
+
+namespace pdg {
+
+__global__ void __launch_bounds__(128) k_extra32(DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t k = v.pid[n];
+  const DevPart &P = v.parts[k];
+  const DevSimParams &sp = v.sp[P.sim];
+  DevSimState &st = v.ss[P.sim];
+  if (!st.active) {
+    v.extra_flag[n] = 0;
+    return;
+  }
+  const int nc = v.cand_n[n];
+  const bool mov = P.movable != 0;
+  bool wall_near = false;
+  if (mov && P.stoppable && sp.allow_wall) {
+    const float4 pl = v.pos32[n], ul = v.disp32[n];
+    const float cx = pl.x + ul.x, cy = pl.y + ul.y, cz = pl.z + ul.z;
+    const float *wl = v.wall_local + 6 * (uint64_t)k;
+    const float lim = (float)sp.Rc * 1.001f;
+    wall_near = fabsf(cx - wl[0]) <= lim || fabsf(cx - wl[3]) <= lim || fabsf(cy - wl[1]) <= lim ||
+                fabsf(cy - wl[4]) <= lim || fabsf(cz - wl[2]) <= lim || fabsf(cz - wl[5]) <= lim;
+  }
+  const bool ext = mov && P.has_ext;
+  if (nc == 0 && !wall_near && !ext && !st.torque) {
+    v.extra_flag[n] = 0;
+    return;
+  }
+  const uint64_t C3 = v.Ncap;
+  const D3 di = ld3(v.disp, n, C3), pi = ld3(v.pos, n, C3), vi = ld3(v.vel_in, n, C3);
+  const double voli = v.vol[n];
+  const bool bdry_i = v.bdry[n] != 0;
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (mov) {
+    if (nc && st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || bdry_i)) {
+      const uint32_t *cl = v.cand + n * v.cand_cap;
+      for (int c = 0; c < nc; ++c) {
+        const uint32_t m = cl[c];
+        if (m < P.g0) continue;
+        if (m >= P.g0 + P.n) break;
+        if (sp.nl_bdry_only && !v.bdry[m]) continue;
+        D3 xi = ld3(v.pos, m, C3) - pi;
+        D3 dir = (ld3(v.disp, m, C3) - di) + xi;
+        double dn = norm3(dir);
+        if (!(dn <= sp.Rc)) continue;
+        double xin = norm3(xi);
+        double len_ref = sp.Rc, sc = sp.sc;
+        if (row_has_live(v, n, m)) continue;
+        if (xin < sp.Rc) {
+          len_ref = xin;
+          sc = P.cnot;
+        }
+        if (!(dn < len_ref)) continue;
+        PairForce pf;
+        pair_force(dir, dn, len_ref, sc, v.vol[m], P.rho, vi, ld3(v.vel_in, m, C3), sp, st, pf);
+        if (P.stoppable) {
+          f = f + pf.fc;
+          if (pf.has_fd) f = f + pf.fd;
+          if (pf.has_ff) f = f + pf.ff;
+        }
+      }
+    }
+    if (wall_near && !within_interior(v.lrtb + 6 * (uint64_t)k, st.wall, sp.Rc) && (!sp.nl_bdry_only || bdry_i)) {
+      D3 cur = pi + di;
+      const bool rx = sp.compute_wall_reaction != 0;
+      wall_face(cur.x - st.wall[0], 0, vi, voli, P.rho, f, st.spd[0], 0, sp, st, rx);
+      wall_face(cur.x - st.wall[3], 0, vi, voli, P.rho, f, st.spd[3], 3, sp, st, rx);
+      wall_face(cur.y - st.wall[1], 1, vi, voli, P.rho, f, st.spd[1], 1, sp, st, rx);
+      wall_face(cur.y - st.wall[4], 1, vi, voli, P.rho, f, st.spd[4], 4, sp, st, rx);
+      wall_face(cur.z - st.wall[2], 2, vi, voli, P.rho, f, st.spd[2], 2, sp, st, rx);
+      wall_face(cur.z - st.wall[5], 2, vi, voli, P.rho, f, st.spd[5], 5, sp, st, rx);
+    }
+    if (ext) {
+      D3 ex = ld3(v.ext, n, C3);
+      if (sp.gradient_extforce) ex = st.extf_scale * ex;
+      f = f + ex;
+    }
+  }
+  if (st.torque) {
+    const double *c = v.centroid + 3 * (uint64_t)k;
+    D3 r = (pi + di) - d3(c[0], c[1], c[2]);
+    double rn = norm3(r);
+    double r_inv = (rn != 0.0 ? 1 / rn : 0);
+    const int ta = (int)P.taxis;
+    set_comp(r, ta, 0.0);
+    D3 perp = d3(0.0, 0.0, 0.0);
+    set_comp(perp, (ta + 1) % 3, -comp(r, (ta + 2) % 3));
+    set_comp(perp, (ta + 2) % 3, comp(r, (ta + 1) % 3));
+    double pn = norm3(perp);
+    if (pn > 0) {
+      perp = perp / pn;
+    } else {
+      set_comp(perp, (ta + 1) % 3, 0.0);
+      set_comp(perp, (ta + 2) % 3, 0.0);
+    }
+    f = f + (r_inv * P.tval) * perp;
+  }
+  if (nc && P.stoppable && (!sp.nl_bdry_only || bdry_i)) {
+    const uint32_t *cl = v.cand + n * v.cand_cap;
+    for (int c = 0; c < nc; ++c) {
+      const uint32_t m = cl[c];
+      if (m >= P.g0 && m < P.g0 + P.n) continue;
+      const uint32_t km = v.pid[m];
+      const uint32_t a = km < k ? km : k, b = km < k ? k : km;
+      if (!(v.parts[a].movable || v.parts[b].movable)) continue;
+      if (!intersects_fext(v.lrtb + 6 * (uint64_t)a, v.lrtb + 6 * (uint64_t)b, sp.Rc)) continue;
+      if (sp.nl_bdry_only && !v.bdry[m]) continue;
+      const D3 pm = ld3(v.pos, m, C3), dm = ld3(v.disp, m, C3);
+      if (km > k) {
+        D3 dir = (dm - di) + (pm - pi);
+        double dn = norm3(dir);
+        if (!(dn < sp.Rc)) continue;
+        PairForce pf;
+        pair_force(dir, dn, sp.Rc, sp.sc, v.vol[m], P.rho, vi, ld3(v.vel_in, m, C3), sp, st, pf);
+        f = f + pf.fc;
+        if (pf.has_fd) f = f + pf.fd;
+        if (pf.has_ff) f = f + pf.ff;
+        if (v.stats) atomicAdd(&v.cnt->contacts, 1ull);
+      } else {
+        D3 dir = (di - dm) + (pi - pm);
+        double dn = norm3(dir);
+        if (!(dn < sp.Rc)) continue;
+        const double volm = v.vol[m];
+        PairForce pf;
+        pair_force(dir, dn, sp.Rc, sp.sc, voli, v.parts[km].rho, ld3(v.vel_in, m, C3), vi, sp, st, pf);
+        f = f - (pf.fc / voli) * volm;
+        if (pf.has_fd) f = f - (pf.fd / sqrt(voli)) * sqrt(volm);
+        if (pf.has_ff) f = f - pf.ff;
+      }
+    }
+  }
+  st3(v.f_extra, n, C3, f);
+  v.extra_flag[n] = 1;
+}
+
+__global__ void __launch_bounds__(128) k_bond32(DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  const uint32_t k = v.pid[nn];
+  const DevPart &P = v.parts[k];
+  const int32_t movable = P.movable;
+  const DevSimState &st = v.ss[P.sim];
+  const bool run = valid && st.active;
+  const uint64_t C3 = v.Ncap;
+  const float4 pi4 = v.pos32[nn];
+  const float4 ui4 = v.disp32[nn];
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  unsigned long long live = 0;
+  if (run && movable) {
+    const uint64_t s = nn >> 5;
+    const uint32_t lane = (uint32_t)(nn & 31);
+    const uint64_t sbase = v.slice_ptr[s];
+    const uint32_t *colp = v.col + sbase + lane;
+    uint32_t *maskp = v.mask + (sbase >> 5);
+    const int dg = v.deg[nn];
+    const bool brk = st.fracture && P.breakable && P.break_bonds;
+    const float cn = (float)P.cnot;
+    const float snot_lo = (float)(P.snot * (1.0 - v.break_band));
+    const float snot_hi = (float)(P.snot * (1.0 + v.break_band));
+    for (int j = 0; j < dg; ++j) {
+      const uint32_t mw = maskp[j];
+      if (!((mw >> lane) & 1u)) continue;
+      const uint32_t q = colp[32 * j];
+      ++live;
+      const float4 pq = v.pos32[q];
+      const float4 uq = v.disp32[q];
+      const float xx = pq.x - pi4.x, xy = pq.y - pi4.y, xz = pq.z - pi4.z;
+      const float ex = uq.x - ui4.x, ey = uq.y - ui4.y, ez = uq.z - ui4.z;
+      const float yx = xx + ex, yy = xy + ey, yz = xz + ez;
+      const float xin = sqrtf(fmaf(xx, xx, fmaf(xy, xy, xz * xz)));
+      const float yn = sqrtf(fmaf(yx, yx, fmaf(yy, yy, yz * yz)));
+      const float xe = fmaf(xx, ex, fmaf(xy, ey, xz * ez));
+      const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+      const float str = __fdividef(fmaf(2.f, xe, ee), (yn + xin) * xin);
+      const float g = __fdividef(cn * str * pq.w, yn);
+      float t, y;
+      y = fmaf(g, yx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
+      y = fmaf(g, yy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
+      y = fmaf(g, yz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
+      if (brk && str > snot_lo) {
+        bool cut = str > snot_hi;
+        if (!cut) {
+          const D3 di = ld3(v.disp, nn, C3), pi = ld3(v.pos, nn, C3);
+          D3 xi64 = ld3(v.pos, q, C3) - pi;
+          D3 eta = (ld3(v.disp, q, C3) - di) + xi64;
+          double en = norm3(eta), xn = norm3(xi64);
+          cut = ((en - xn) / xn) > P.snot;
+        }
+        if (cut) atomicAnd(&maskp[j], ~(1u << lane));
+      }
+    }
+  }
+  if (run) {
+    D3 f = d3((double)sx - (double)cx, (double)sy - (double)cy, (double)sz - (double)cz);
+    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, C3);
+    st3(v.force, nn, C3, f);
+    if (nonfinite(f.x) || nonfinite(f.y) || nonfinite(f.z)) atomicOr(&v.cnt->err, PD_DERR_NONFINITE);
+    const D3 vi = ld3(v.vel_in, nn, C3);
+    D3 vo = vi;
+    if (movable) {
+      const D3 ao = ld3(v.acc, nn, C3);
+      const D3 an = P.irho * f;
+      vo = vi + v.sp[P.sim].hdt * (ao + an);
+      st3(v.acc, nn, C3, an);
+    }
+    st3(v.vel_out, nn, C3, vo);
+  }
+  // particle AABB of this step's positions in the particle's local frame
+  {
+    const bool contrib = run && movable;
+    const float px = pi4.x + ui4.x, py = pi4.y + ui4.y, pz = pi4.z + ui4.z;
+    float lo[3] = {contrib ? px : INFINITY, contrib ? py : INFINITY, contrib ? pz : INFINITY};
+    float hi[3] = {contrib ? px : -INFINITY, contrib ? py : -INFINITY, contrib ? pz : -INFINITY};
+    const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+    const bool uniform = __all_sync(0xffffffffu, k == k0);
+    if (uniform) {
+      for (int o = 16; o > 0; o >>= 1) {
+        for (int c = 0; c < 3; ++c) {
+          lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+          hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+      }
+    }
+    const bool writer = uniform ? ((threadIdx.x & 31) == 0) : contrib;
+    if (writer && lo[0] <= hi[0]) {
+      unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
+      for (int c = 0; c < 3; ++c) {
+        atomicMin(&L[c], fkey(lo[c]));
+        atomicMax(&L[3 + c], fkey(hi[c]));
+      }
+    }
+  }
+  if (v.stats) {
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, live);
+  }
+}
+
+void launch_step_fp32c(const DevView &v, cudaStream_t s) {
+  const uint64_t blocks = (v.N + 127) / 128;
+  if (!blocks) return;
+  k_extra32<<<(unsigned)blocks, 128, 0, s>>>(v);
+  k_bond32<<<(unsigned)blocks, 128, 0, s>>>(v);
+}
+
+}  // namespace pdg

@@ -4,7 +4,7 @@
 //   k_predict        predictor for all nodes (timeloop.h:537-540), step-max displacement
 //                    increment for the broad-phase rebuild test, FP32 local displacement
 //   [broad phase]    pd_broadphase.cu, runs only when a rebuild is due
-//   k_step<PREC>     fused per-node force and corrector: PD bond sum with breaking
+//   k_step           FP64 fused per-node force and corrector: PD bond sum with breaking
 //                    (particle2.h:107-237), self-contact, walls, extforce, torque
 //                    (timeloop.h:544-634), node-node contact of particle pairs in
 //                    ascending partner order (timeloop.h:636-651, contact.h:744-942) and
@@ -17,160 +17,18 @@
 #include <math.h>
 #include <string.h>
 
+#include "pd_device.cuh"
 #include "pd_engine.h"
 #include "pd_math.cuh"
 
 namespace pdg {
 
 // ------------------------------------------------------------------------------------
-// small helpers
-
-__device__ __forceinline__ D3 ld3(const double *a, uint64_t n, uint64_t cap) {
-  return d3(a[n], a[n + cap], a[n + 2 * cap]);
-}
-__device__ __forceinline__ void st3(double *a, uint64_t n, uint64_t cap, D3 v) {
-  a[n] = v.x;
-  a[n + cap] = v.y;
-  a[n + 2 * cap] = v.z;
-}
-
-__device__ __forceinline__ double warp_max(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-// intersects_box_fext<3> (contact.h:1143-1183): only box A is extended by c.
-__device__ __forceinline__ bool intersects_fext(const double *A, const double *B, double c) {
-  double A_min_x = A[0] - c, A_min_y = A[1] - c, A_min_z = A[2] - c;
-  double A_max_x = A[3] + c, A_max_y = A[4] + c, A_max_z = A[5] + c;
-  return (A_min_x <= B[3]) && (A_max_x >= B[0]) && (A_max_y >= B[1]) && (A_min_y <= B[4]) &&
-         (A_min_z <= B[5]) && (A_max_z >= B[2]);
-}
-
-// within_interior_fext (contact.h:1229-1243) with its 2D indexing of 3D boxes.
-__device__ __forceinline__ bool within_interior(const double *A, const double *B, double c) {
-  double A_Left = A[0] - c, A_Right = A[1] + c, A_Top = A[2] + c, A_Bottom = A[3] - c;
-  return (B[0] < A_Left) && (A_Right < B[1]) && (B[2] > A_Top) && (B[3] < A_Bottom);
-}
-
-// Normal, damping and friction force densities of one node-node contact, computed from
-// the point of view of the "C" node as update_contact_force_by_boundary does
-// (contact.h:798-934). fc is always set; fd/ff only when has_fd/has_ff.
-struct PairForce {
-  D3 fc, fd, ff;
-  bool has_fd, has_ff;
-};
-
-__device__ __forceinline__ void pair_force(D3 dir, double dn, double len_ref, double sc,
-                                           double N_vol, double rho_C, D3 velC, D3 velN,
-                                           const DevSimParams &sp, const DevSimState &st,
-                                           PairForce &o) {
-  D3 unit = dir / dn;
-  double s = (dn - len_ref) / len_ref;
-  double fmag = (sc * s) * N_vol;
-  o.fc = fmag * unit;
-  double fcn = norm3(o.fc);
-  o.has_fd = false;
-  o.has_ff = false;
-  if (st.damping) {
-    D3 rel = velC - velN;
-    double rvp = dot3(rel, unit);
-    D3 rvn = rvp * unit;
-    double dc = (sp.zeta2 * sqrt(sc * rho_C)) * sqrt(N_vol);
-    o.fd = (-dc) * rvn;
-    o.has_fd = true;
-  }
-  if (st.friction) {
-    D3 rel = velC - velN;
-    double rd = dot3(rel, unit);
-    D3 rvt = rel - rd * unit;
-    double rvtn = norm3(rvt);
-    if (rvtn > 0) {
-      D3 tu = rvt / norm3(rvt);
-      double fm = (-sp.mu) * fcn;
-      if (rvtn < ((sp.mu * fcn) * sp.dt) / rho_C) fm = ((-rvtn) / rho_C) / sp.dt;
-      o.ff = fm * tu;
-      o.has_ff = true;
-    }
-  }
-}
-
-// segment_mass<3> + wall_side_force_update<3> (contact.h:14-39, 381-502) for one face.
-__device__ __forceinline__ void wall_face(double dist, int dir, D3 vel, double vol, double rho,
-                                          D3 &f, double wspeed, int face,
-                                          const DevSimParams &sp, DevSimState &st, bool reaction) {
-  const double R = sp.Rc;
-  if (!(fabs(dist) <= R)) return;
-  double d = fabs(dist);
-  double rd = R - d;
-  double area = (sp.pi3 * (rd * rd)) * (2 * R - d);
-  double w = R * R - d * d;
-  double I = sp.pi4 * (w * w);
-  double cen = I / area;
-  double crc = R - cen;
-  double pcrc = (crc > 0 ? crc : 0);
-  double F = (sp.Kn * pcrc) * area;
-  double c_sign = (dist > 0 ? 1.0 : -1.0);
-  double r0 = 0, r1 = 0, r2 = 0;  // reaction contributions in dir, t1, t2
-  {
-    double a = c_sign * F;
-    set_comp(f, dir, comp(f, dir) + a);
-    r0 -= ((vol * c_sign) * F);
-  }
-  D3 rel = vel;
-  set_comp(rel, dir, comp(rel, dir) - wspeed);
-  const int t1 = (dir + 1) % 3, t2 = (dir + 2) % 3;
-  if (st.friction) {
-    double v1 = comp(rel, t1), v2 = comp(rel, t2);
-    double vn = sqrt(v1 * v1 + v2 * v2);
-    if (vn > 0) {
-      double u1 = v1 / vn, u2 = v2 / vn;
-      double aF = fabs(F);
-      double ff1 = ((-sp.mu) * aF) * u1;
-      double ff2 = ((-sp.mu) * aF) * u2;
-      if (vn < ((sp.mu * aF) * sp.dt) / rho) {
-        double g = ((-vn) / rho) / sp.dt;
-        ff1 = g * u1;
-        ff2 = g * u2;
-      }
-      set_comp(f, t1, comp(f, t1) + ff1);
-      set_comp(f, t2, comp(f, t2) + ff2);
-      r1 -= (vol * ff1);
-      r2 -= (vol * ff2);
-    }
-  }
-  if (st.damping) {
-    double dc = ((sp.zeta2) * sqrt(sp.Kn * rho)) * sqrt(fabs(area));
-    double df = (-dc) * comp(rel, dir);
-    set_comp(f, dir, comp(f, dir) + df);
-    r0 -= (vol * df);
-  }
-  if (reaction) {
-    atomicAdd(&st.react[3 * face + dir], r0);
-    if (r1 != 0) atomicAdd(&st.react[3 * face + t1], r1);
-    if (r2 != 0) atomicAdd(&st.react[3 * face + t2], r2);
-  }
-}
-
-// Does row n hold a live bond to global node m? (std::find over NbdArr, contact.h:783)
-__device__ __forceinline__ bool row_has_live(const DevView &v, uint64_t n, uint32_t m) {
-  const uint64_t s = n >> 5;
-  const uint32_t lane = (uint32_t)(n & 31);
-  const uint64_t base = v.slice_ptr[s] + lane;
-  const uint64_t mbase = v.slice_ptr[s] >> 5;
-  const int dg = v.deg[n];
-  for (int j = 0; j < dg; ++j) {
-    if (v.col[base + 32ull * j] == m) return (v.mask[mbase + j] >> lane) & 1u;
-  }
-  return false;
-}
-
-// ------------------------------------------------------------------------------------
 // predictor
 
 __global__ void k_predict(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double inc = 0.0;
+  float inc2 = 0.f;
   if (n < v.N) {
     const uint32_t k = v.pid[n];
     const DevPart &P = v.parts[k];
@@ -183,16 +41,20 @@ __global__ void k_predict(DevView v) {
       D3 in = dv + da;
       d = d + in;
       st3(v.disp, n, v.Ncap, d);
-      inc = norm3(in);
+      // squared increment in FP32 (only bounds the broad-phase rebuild test)
+      const float ix = (float)in.x, iy = (float)in.y, iz = (float)in.z;
+      inc2 = ix * ix + iy * iy + iz * iz;
       if (v.disp32) {
         const double *an = v.anchor + 3 * (uint64_t)k;
         v.disp32[n] = make_float4((float)(d.x - an[0]), (float)(d.y - an[1]), (float)(d.z - an[2]), 0.f);
       }
     }
   }
-  inc = warp_max(inc);
-  if ((threadIdx.x & 31) == 0 && inc > 0)
+  for (int o = 16; o > 0; o >>= 1) inc2 = fmaxf(inc2, __shfl_xor_sync(0xffffffffu, inc2, o));
+  if ((threadIdx.x & 31) == 0 && inc2 > 0.f) {
+    const double inc = sqrt((double)inc2) * (1.0 + 1e-5);
     atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(inc));
+  }
 }
 
 void launch_predict(const DevView &v, int tpb, cudaStream_t s) {
@@ -203,7 +65,6 @@ void launch_predict(const DevView &v, int tpb, cudaStream_t s) {
 // ------------------------------------------------------------------------------------
 // fused force + corrector
 
-template <int PREC>
 __global__ void __launch_bounds__(128) k_step(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
@@ -231,74 +92,25 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
     const uint64_t mbase = v.slice_ptr[s] >> 5;
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
-    if (PREC == PD_FP64) {
-      D3 acc = d3(0.0, 0.0, 0.0);
-      for (int j = 0; j < dg; ++j) {
-        const uint32_t mw = v.mask[mbase + j];
-        if (!((mw >> lane) & 1u)) continue;
-        const uint64_t e = base + 32ull * j;
-        const uint32_t q = v.col[e];
-        ++live;
-        D3 dq = ld3(v.disp, q, C3);
-        D3 eta = (dq - di) + d3(v.bxi[e], v.bxi[e + v.E], v.bxi[e + 2 * v.E]);
-        double en = norm3(eta);
-        double xn = v.bxin[e];
-        double str = div_rcp(en - xn, xn, v.brxin[e]);
-        double mag = (P.cnot * str) * v.vol[q];
-        double ren = __drcp_rn(en);
-        D3 unit = d3(div_rcp(eta.x, en, ren), div_rcp(eta.y, en, ren), div_rcp(eta.z, en, ren));
-        acc = acc + mag * unit;
-        if (brk && str > P.snot) atomicAnd(&v.mask[mbase + j], ~(1u << lane));
-      }
-      f = d3(0.0, 0.0, 0.0) + acc;
-    } else {
-      // FP32 bond forces: cancellation-free stretch s = (2 xi.eta + eta.eta) /
-      // ((|xi+eta| + |xi|) |xi|) on anchor-relative FP32 positions/displacements, and
-      // Kahan-compensated FP32 sums. The stretch-vs-snot decision falls back to the FP64
-      // formula inside a relative band around snot.
-      const float4 pi4 = v.pos32[nn];
-      const float4 ui4 = v.disp32[nn];
-      const float cn = (float)P.cnot;
-      const float snot_lo = (float)(P.snot * (1.0 - v.break_band));
-      const float snot_hi = (float)(P.snot * (1.0 + v.break_band));
-      float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-      for (int j = 0; j < dg; ++j) {
-        const uint32_t mw = v.mask[mbase + j];
-        if (!((mw >> lane) & 1u)) continue;
-        const uint64_t e = base + 32ull * j;
-        const uint32_t q = v.col[e];
-        ++live;
-        const float4 pq = v.pos32[q];
-        const float4 uq = v.disp32[q];
-        const float xx = pq.x - pi4.x, xy = pq.y - pi4.y, xz = pq.z - pi4.z;
-        const float ex = uq.x - ui4.x, ey = uq.y - ui4.y, ez = uq.z - ui4.z;
-        const float yx = xx + ex, yy = xy + ey, yz = xz + ez;
-        const float xin = sqrtf(__fmaf_rn(xx, xx, __fmaf_rn(xy, xy, xz * xz)));
-        const float yn = sqrtf(__fmaf_rn(yx, yx, __fmaf_rn(yy, yy, yz * yz)));
-        const float xe = __fmaf_rn(xx, ex, __fmaf_rn(xy, ey, xz * ez));
-        const float ee = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, ez * ez));
-        const float str = __fdividef(__fmaf_rn(2.f, xe, ee), (yn + xin) * xin);
-        const float g = __fdividef(cn * str * pq.w, yn);
-        // Kahan-compensated accumulation of g * (xi + eta)
-        float t, y;
-        y = __fmaf_rn(g, yx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
-        y = __fmaf_rn(g, yy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
-        y = __fmaf_rn(g, yz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
-        if (brk && str > snot_lo) {
-          bool cut = str > snot_hi;
-          if (!cut) {
-            // FP64 stretch of the reference formula for bonds near the threshold
-            D3 dq = ld3(v.disp, q, C3);
-            D3 xi64 = ld3(v.pos, q, C3) - pi;
-            D3 eta = (dq - di) + xi64;
-            double en = norm3(eta), xn = norm3(xi64);
-            cut = ((en - xn) / xn) > P.snot;
-          }
-          if (cut) atomicAnd(&v.mask[mbase + j], ~(1u << lane));
-        }
-      }
-      f = d3((double)sx - (double)cx, (double)sy - (double)cy, (double)sz - (double)cz);
+    D3 acc = d3(0.0, 0.0, 0.0);
+    for (int j = 0; j < dg; ++j) {
+      const uint32_t mw = v.mask[mbase + j];
+      if (!((mw >> lane) & 1u)) continue;
+      const uint64_t e = base + 32ull * j;
+      const uint32_t q = v.col[e];
+      ++live;
+      D3 dq = ld3(v.disp, q, C3);
+      D3 eta = (dq - di) + d3(v.bxi[e], v.bxi[e + v.E], v.bxi[e + 2 * v.E]);
+      double en = norm3(eta);
+      double xn = v.bxin[e];
+      double str = div_rcp(en - xn, xn, v.brxin[e]);
+      double mag = (P.cnot * str) * v.vol[q];
+      double ren = __drcp_rn(en);
+      D3 unit = d3(div_rcp(eta.x, en, ren), div_rcp(eta.y, en, ren), div_rcp(eta.z, en, ren));
+      acc = acc + mag * unit;
+      if (brk && str > P.snot) atomicAnd(&v.mask[mbase + j], ~(1u << lane));
     }
+    f = d3(0.0, 0.0, 0.0) + acc;
 
     // ---- self-contact (timeloop.h:554-557, contact.h:779-796), C side only
     if (st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || bdry_i)) {
@@ -474,9 +286,9 @@ void launch_step_kernel(const DevView &v, int precision, int tpb, cudaStream_t s
   (void)tpb;
   if (!blocks) return;
   if (precision == PD_FP32C)
-    k_step<PD_FP32C><<<(unsigned)blocks, 128, 0, s>>>(v);
+    launch_step_fp32c(v, s);
   else
-    k_step<PD_FP64><<<(unsigned)blocks, 128, 0, s>>>(v);
+    k_step<<<(unsigned)blocks, 128, 0, s>>>(v);
 }
 
 // ------------------------------------------------------------------------------------
@@ -489,21 +301,18 @@ __global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const ui
   DevPart &P = v.parts[k];
   const DevSimState &st = v.ss[P.sim];
   const DevSimParams &sp = v.sp[P.sim];
-  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
   if (!st.active) return;
-  if (P.movable) {
-    for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
-  }
-  for (int c = 0; c < 3; ++c) {
-    L[c] = ord_key(INFINITY);
-    L[3 + c] = ord_key(-INFINITY);
-  }
-  // anchor of the FP32 local frame: this step's displacement of the particle's first node
   if (v.disp32) {
-    double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
-    an[0] = v.disp[P.g0];
-    an[1] = v.disp[P.g0 + v.Ncap];
-    an[2] = v.disp[P.g0 + 2 * v.Ncap];
+    end_particle_fp32c(v, k, P, st);
+  } else {
+    unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+    if (P.movable) {
+      for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
+    }
+    for (int c = 0; c < 3; ++c) {
+      L[c] = ord_key(INFINITY);
+      L[3 + c] = ord_key(-INFINITY);
+    }
   }
   // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
   // keeps this step's predicted displacement, saved for the readback
@@ -524,8 +333,9 @@ __global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const ui
     }
     if (jump > 0) atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(jump));
   }
-  // per-particle toggles for the next step (timeloop.h:481-498)
-  const uint32_t tn = st.t + 1;
+  // per-particle toggles for the next step (timeloop.h:481-498); k_end_sims has already
+  // advanced st.t to the next step's index
+  const uint32_t tn = st.t;
   const uint32_t kl = k - sp.p0;
   if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
     P.movable = 1;
@@ -558,7 +368,6 @@ __global__ void k_end_sims(DevView v, double half_skin) {
       for (int c = 0; c < 6; ++c) st.wall[c] += st.spd[c] * sp.dt;  // timeloop.h:791-796
       st.t += 1;
       apply_sim_toggles(sp, st, st.t);
-      for (int c = 0; c < 18; ++c) st.react[c] = 0.0;  // Wall.setzero_reaction (timeloop.h:397)
     }
   }
   if (s == 0) {
@@ -581,8 +390,8 @@ void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamp
                      cudaStream_t s) {
   const uint32_t *cptr = n_clamped ? clamped : nullptr;
   const uint32_t *clist = n_clamped ? clamped + (v.P + 1) : nullptr;
-  k_end_particles<<<(v.P + 127) / 128, 128, 0, s>>>(v, cptr, clist, clamped_disp);
   k_end_sims<<<(v.S + 127) / 128, 128, 0, s>>>(v, 0.0);
+  k_end_particles<<<(v.P + 127) / 128, 128, 0, s>>>(v, cptr, clist, clamped_disp);
 }
 
 // ------------------------------------------------------------------------------------
@@ -657,10 +466,18 @@ __global__ void k_init_lrtb_fin(DevView v) {
   }
   if (v.disp32) {
     const DevPart &P = v.parts[k];
+    const DevSimState &st = v.ss[P.sim];
     double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
     an[0] = v.disp[P.g0];
     an[1] = v.disp[P.g0 + v.Ncap];
     an[2] = v.disp[P.g0 + 2 * v.Ncap];
+    unsigned int *Lf = v.lrtb_local_next + 6 * (uint64_t)k;
+    float *wl = v.wall_local + 6 * (uint64_t)k;
+    for (int c = 0; c < 3; ++c) {
+      Lf[c] = fkey(INFINITY);
+      Lf[3 + c] = fkey(-INFINITY);
+    }
+    for (int f = 0; f < 6; ++f) wl[f] = (float)(st.wall[f] - (P.anchor_pos[f % 3] + an[f % 3]));
   }
 }
 __global__ void k_reset_lrtb_next(DevView v) {
@@ -710,6 +527,30 @@ void launch_pairwise_count(const DevView &v, cudaStream_t s) {
   if (!v.S) return;
   dim3 grid(64, v.S);
   k_pairwise<<<grid, 256, 0, s>>>(v);
+}
+
+}  // namespace pdg
+
+namespace pdg {
+
+// Live directed bonds of movable particles: popcount of each node's live bits.
+__global__ void k_count_live(DevView v, unsigned long long *out) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long c = 0;
+  if (n < v.N && v.parts[v.pid[n]].movable) {
+    const uint64_t s = n >> 5;
+    const uint32_t lane = (uint32_t)(n & 31);
+    const uint64_t mbase = v.slice_ptr[s] >> 5;
+    const int dg = v.deg[n];
+    for (int j = 0; j < dg; ++j) c += (v.mask[mbase + j] >> lane) & 1u;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s) {
+  uint64_t blocks = (v.N + 255) / 256;
+  if (blocks) k_count_live<<<(unsigned)blocks, 256, 0, s>>>(v, out);
 }
 
 }  // namespace pdg

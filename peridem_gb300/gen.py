@@ -194,8 +194,12 @@ def crush512(n=8, box=12.0 * MM, seed=2, steps=10000, dt=5e-9, hs=(0.05 * MM, 0.
             for ix in range(n):
                 kind = ("sphere", "cube", "ellipsoid")[int(rng.integers(3))]
                 h = float(hs[int(rng.integers(len(hs)))])
+                # sizes are bounding diameters, so that randomly rotated particles on the
+                # 1.5 mm pitch never overlap: a cube of size d has edge d / sqrt(3)
                 if kind == "ellipsoid":
                     size = rng.uniform(smin, smax, size=3)
+                elif kind == "cube":
+                    size = float(rng.uniform(smin, smax)) / math.sqrt(3.0)
                 else:
                     size = float(rng.uniform(smin, smax))
                 loc = lattice(kind, size, h)

@@ -63,6 +63,57 @@ class Setup:
             return np.zeros(0, dtype=np.uint32)
         return arr[int(off[p]):int(off[p + 1])]
 
+    def subset(self, particles) -> "Setup":
+        """A setup holding only the listed particles (same contact constants and walls)."""
+        parts = []
+        for p in particles:
+            sl = self.particle_slice(p)
+            parts.append(dict(pos=self.pos[sl], vol=self.vol[sl], disp=self.disp[sl], vel=self.vel[sl],
+                              acc=self.acc[sl], extforce=self.extforce[sl], conn=self.particle_conn(p),
+                              delta=self.delta[p], rho=self.rho[p], cnot=self.cnot[p], snot=self.snot[p],
+                              torque_val=self.torque_val[p], movable=self.movable[p],
+                              breakable=self.breakable[p], stoppable=self.stoppable[p],
+                              torque_axis=self.torque_axis[p],
+                              bdry=self.particle_list(self.bdry_offset, self.bdry, p),
+                              clamped=self.particle_list(self.clamped_offset, self.clamped, p)))
+        wall = dict(allow=self.allow_wall, geom=self.geom_wall_info) if self.geom_wall_info is not None else None
+        s = concat(parts, dict(contact_radius=self.contact_radius, normal_stiffness=self.normal_stiffness,
+                               damping_ratio=self.damping_ratio, friction_coefficient=self.friction_coefficient),
+                   wall)
+        s.meta = dict(self.meta, subset=list(map(int, particles)))
+        return s
+
+    def nbytes(self) -> int:
+        """Bytes of the host arrays a caller hands to pd_create_from_arrays."""
+        tot = 0
+        for k in ("node_offset", "pos", "vol", "disp", "vel", "acc", "extforce", "conn_offset", "conn"):
+            tot += getattr(self, k).nbytes
+        return int(tot)
+
+    def save_npz(self, path):
+        d = {k: getattr(self, k) for k in ("node_offset", "pos", "vol", "disp", "vel", "acc", "extforce",
+                                           "conn_offset", "conn", "delta", "rho", "cnot", "snot", "torque_val",
+                                           "movable", "breakable", "stoppable", "torque_axis", "bdry_offset",
+                                           "bdry", "clamped_offset", "clamped")}
+        d["scalars"] = np.array([self.contact_radius, self.normal_stiffness, self.damping_ratio,
+                                 self.friction_coefficient, float(self.allow_wall)])
+        d["geom_wall_info"] = self.geom_wall_info if self.geom_wall_info is not None else np.zeros(0)
+        np.savez(path, **d)
+
+    @staticmethod
+    def load_npz(path) -> "Setup":
+        z = np.load(path)
+        sc = z["scalars"]
+        g = z["geom_wall_info"]
+        return Setup(node_offset=z["node_offset"], pos=z["pos"], vol=z["vol"], disp=z["disp"], vel=z["vel"],
+                     acc=z["acc"], extforce=z["extforce"], conn_offset=z["conn_offset"], conn=z["conn"],
+                     delta=z["delta"], rho=z["rho"], cnot=z["cnot"], snot=z["snot"], torque_val=z["torque_val"],
+                     movable=z["movable"], breakable=z["breakable"], stoppable=z["stoppable"],
+                     torque_axis=z["torque_axis"], contact_radius=float(sc[0]), normal_stiffness=float(sc[1]),
+                     damping_ratio=float(sc[2]), friction_coefficient=float(sc[3]), allow_wall=int(sc[4]),
+                     geom_wall_info=g if len(g) else None, bdry_offset=z["bdry_offset"], bdry=z["bdry"],
+                     clamped_offset=z["clamped_offset"], clamped=z["clamped"])
+
 
 def concat(parts: list[dict], contact: dict, wall: dict | None) -> Setup:
     """Assemble particles (dicts with pos, vol, conn, material scalars, ...) into a Setup."""

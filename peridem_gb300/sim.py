@@ -116,3 +116,15 @@ class Sim:
 
     def step_bytes(self) -> float:
         return float(lib().pd_step_bytes(self.h))
+
+    def profile(self, nsteps: int) -> np.ndarray:
+        """Device ms per phase summed over nsteps real steps:
+        [predictor, broad phase, fused force+corrector, end of step]."""
+        out = np.zeros(4)
+        self._ck(lib().pd_profile_steps(self.h, int(nsteps), ptr(out)))
+        return out
+
+    def live_bonds(self) -> int:
+        n = C.c_uint64()
+        self._ck(lib().pd_count_live_bonds(self.h, C.byref(n)))
+        return int(n.value)
