@@ -164,10 +164,13 @@ __device__ __forceinline__ bool nonfinite(double x) {
   return ((__double2hiint(x) >> 20) & 0x7FF) == 0x7FF;
 }
 
-// End-of-step work of the FP32 form for one particle: AABB from the local-frame keys
-// (widened by a few float ulps each way), new anchor, walls in the new local frame.
-__device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const DevPart &P, const DevSimState &st) {
+// End-of-step work of the FP32 form for one particle: AABB from the local-frame keys of this
+// step (widened by a few float ulps each way), anchors moved on by one step, walls expressed in
+// the frame of the next step's disp32.
+__device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const DevPart &P,
+                                                   const DevSimState &st) {
   double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
+  double *ann = v.anchor_next + 3 * (uint64_t)k;
   unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
   if (P.movable) {
     for (int c = 0; c < 3; ++c) {
@@ -182,9 +185,11 @@ __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k,
     L[c] = fkey(INFINITY);
     L[3 + c] = fkey(-INFINITY);
   }
-  an[0] = v.disp[P.g0];
-  an[1] = v.disp[P.g0 + v.Ncap];
-  an[2] = v.disp[P.g0 + 2 * v.Ncap];
+  // disp_next holds the next step's predicted displacement of the anchor node
+  for (int c = 0; c < 3; ++c) {
+    an[c] = ann[c];
+    ann[c] = v.disp_next[P.g0 + c * v.Ncap];
+  }
   float *wl = v.wall_local + 6 * (uint64_t)k;
   for (int f = 0; f < 6; ++f) {
     const int c = f % 3;

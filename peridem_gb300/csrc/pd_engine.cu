@@ -77,6 +77,15 @@ DevView Engine::view(int cur) const {
   v.pos32 = d_pos32_;
   v.disp32 = d_disp32_;
   v.anchor = d_anchor_;
+  if (precision_ == PD_FP32C) {
+    v.disp = d_dispb_[cur];
+    v.disp_next = d_dispb_[cur ^ 1];
+    v.disp32 = d_disp32b_[cur];
+    v.disp32_next = d_disp32b_[cur ^ 1];
+    v.anchor_next = d_anchor_next_;
+    v.clamp_flag = d_clamp_flag_;
+    v.fused = 1;
+  }
   v.break_band = 1e-4;
   v.f_extra = d_f_extra_;
   v.extra_flag = d_extra_flag_;
@@ -254,6 +263,9 @@ int Engine::alloc_and_upload() {
       P.stoppable = s.stoppable[p];
       P.break_bonds = 1;  // simulate3d.cpp:137-139
       P.has_ext = 0;
+      P.cnot32 = (float)P.cnot;
+      P.snot_lo32 = (float)(P.snot * (1.0 - 1e-4));
+      P.snot_hi32 = (float)(P.snot * (1.0 + 1e-4));
       for (uint64_t q = s.node_offset[p]; q < s.node_offset[p + 1] && !P.has_ext; ++q)
         if (s.ext[3 * q] != 0.0 || s.ext[3 * q + 1] != 0.0 || s.ext[3 * q + 2] != 0.0) P.has_ext = 1;
       if (P.n == 0) {
@@ -418,7 +430,19 @@ int Engine::alloc_and_upload() {
     }
     PD_TRY(dalloc(this, allocs_, &d_pos32_, C, err));
     PD_TRY(dalloc(this, allocs_, &d_disp32_, C, err));
+    d_disp32b_[0] = d_disp32_;
+    PD_TRY(dalloc(this, allocs_, &d_disp32b_[1], C, err));
+    PD_TRY(check(cudaMemset(d_disp32b_[1], 0, C * sizeof(float4)), "memset disp32"));
+    d_dispb_[0] = d_disp_;
+    PD_TRY(dalloc(this, allocs_, &d_dispb_[1], 3 * C, err));
     PD_TRY(dalloc(this, allocs_, &d_anchor_, 3ull * P_, err));
+    PD_TRY(dalloc(this, allocs_, &d_anchor_next_, 3ull * P_, err));
+    {
+      std::vector<uint8_t> cf(C, 0);
+      for (uint32_t g : clamped_list) cf[g] = 1;
+      PD_TRY(dalloc(this, allocs_, &d_clamp_flag_, C, err));
+      PD_TRY(up(d_clamp_flag_, cf.data(), C, "upload clamp flags"));
+    }
     PD_TRY(dalloc(this, allocs_, &d_f_extra_, 3 * C, err));
     PD_TRY(dalloc(this, allocs_, &d_extra_flag_, C, err));
     PD_TRY(dalloc(this, allocs_, &d_wall_local_, 6ull * P_, err));
@@ -442,12 +466,32 @@ int Engine::alloc_and_upload() {
   PD_TRY(dalloc(this, allocs_, &bp_.block_sums, (T + 4095) / 4096 + 1, err));
   PD_TRY(alloc_candidates());
 
-  DevView v = view(0);
-  if (precision_ == PD_FP64) launch_bond_constants(v, d_bxi_, d_bxin_, d_brxin_, stream_);
-  launch_init_lrtb(v, stream_);
-  PD_TRY(check(cudaGetLastError(), "init kernels"));
+  if (precision_ == PD_FP64) {
+    DevView v = view(0);
+    launch_bond_constants(v, d_bxi_, d_bxin_, d_brxin_, stream_);
+    launch_init_lrtb(v, stream_);
+    PD_TRY(check(cudaGetLastError(), "init kernels"));
+  } else {
+    cur_ = 1;
+    PD_TRY(prepare_fused(cur_));
+  }
   PD_TRY(check(cudaStreamSynchronize(stream_), "init sync"));
   return PD_OK;
+}
+
+// FP32 form: disp[cur^1] holds the displacement of the last completed step (or the initial
+// one); derive this step's AABBs, anchors and wall frames from it, then run the predictor
+// into disp[cur]/disp32[cur] and set the anchors of the next step's disp32.
+int Engine::prepare_fused(int cur) {
+  // AABBs from pos + disp (timeloop.h:389-393), anchors := disp of each anchor node, walls in
+  // the anchors' frame
+  launch_init_lrtb(view(cur ^ 1), stream_);
+  PD_TRY(check(cudaMemcpyAsync(d_dispb_[cur], d_dispb_[cur ^ 1], 3 * Ncap_ * 8, cudaMemcpyDeviceToDevice, stream_),
+               "copy disp"));
+  DevView v = view(cur);
+  launch_predict(v, tpb_, stream_);
+  launch_anchor_next(v, stream_);
+  return check(cudaGetLastError(), "prepare fused");
 }
 
 int Engine::alloc_candidates() {
@@ -467,7 +511,7 @@ int Engine::alloc_candidates() {
 
 int Engine::launch_step_seq(int cur, cudaStream_t s) {
   DevView v = view(cur);
-  launch_predict(v, tpb_, s);
+  if (precision_ == PD_FP64) launch_predict(v, tpb_, s);
   if (torque_possible_) launch_centroids(v, s);
   launch_bp_decide(v, half_skin_, s);
   launch_broadphase(v, bp_, s);
@@ -565,10 +609,16 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
   };
   if (curpos || disp) {
     std::vector<double> dsp(3 * N_);
-    PD_TRY(fetch(d_disp_, dsp.data()));
-    if (disp) std::memcpy(disp, dsp.data(), 3 * N_ * 8);
+    const bool fused = precision_ == PD_FP32C;
+    PD_TRY(fetch(fused ? d_dispb_[cur_ ^ 1] : d_disp_, dsp.data()));
+    if (disp) {
+      std::memcpy(disp, dsp.data(), 3 * N_ * 8);
+      if (fused && steps_done_ > 0)  // clamped nodes end each step at zero (timeloop.h:767-774)
+        for (uint32_t g : h_clamped_)
+          for (int c = 0; c < 3; ++c) disp[3 * (uint64_t)g + c] = 0.0;
+    }
     if (curpos) {
-      if (n_clamped_ && steps_done_ > 0) {
+      if (n_clamped_ && steps_done_ > 0 && !fused) {
         // CurrPos of clamped nodes keeps the predicted displacement (zeroed afterwards)
         std::vector<double> cd(3 * n_clamped_);
         PD_TRY(check(cudaMemcpy(cd.data(), d_clamped_disp_, 3 * n_clamped_ * 8, cudaMemcpyDeviceToHost), "read clamped"));
@@ -599,12 +649,16 @@ int Engine::set_state(const double *disp, const double *vel, const double *acc) 
       for (int c = 0; c < 3; ++c) buf[c * C + n] = src[3 * n + c];
     return check(cudaMemcpy(d, buf.data(), 3 * C * 8, cudaMemcpyHostToDevice), "write state");
   };
-  if (disp) PD_TRY(put(d_disp_, disp));
+  const bool fused = precision_ == PD_FP32C;
+  if (disp) PD_TRY(put(fused ? d_dispb_[cur_ ^ 1] : d_disp_, disp));
   if (vel) PD_TRY(put(d_vel_[cur_], vel));
   if (acc) PD_TRY(put(d_acc_, acc));
   // a resumed state re-derives CurrPos/AABBs (timeloop.h:389-393) and the contact lists
-  DevView v = view(cur_);
-  launch_init_lrtb(v, stream_);
+  if (fused) {
+    PD_TRY(prepare_fused(cur_));
+  } else {
+    launch_init_lrtb(view(cur_), stream_);
+  }
   double big = 1e300;
   PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
   return check(cudaStreamSynchronize(stream_), "set_state");
@@ -762,7 +816,7 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
     DevView v = view(cur_);
     cudaStream_t s = stream_;
     cudaEventRecord(ev[0], s);
-    launch_predict(v, tpb_, s);
+    if (precision_ == PD_FP64) launch_predict(v, tpb_, s);
     if (torque_possible_) launch_centroids(v, s);
     cudaEventRecord(ev[1], s);
     launch_bp_decide(v, half_skin_, s);

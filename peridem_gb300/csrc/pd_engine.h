@@ -42,7 +42,7 @@ struct DevPart {
   int32_t movable, breakable, stoppable, break_bonds;
   double anchor_pos[3];  // FP32 form: position of the anchor node
   int32_t has_ext;       // any non-zero extforce in this particle
-  int32_t pad_;
+  float cnot32, snot_lo32, snot_hi32;  // FP32 form: cnot and the band around snot
 };
 
 // Per-simulation constants (Contact, RectWall and Timeloop fields after apply_config).
@@ -104,9 +104,14 @@ struct DevView {
   uint32_t *mask;
   const double *bxi, *bxin, *brxin;  // FP64 form, [3][E], [E], [E]
   uint64_t E;
-  // FP32-compensated form
-  float4 *pos32, *disp32;
-  const double *anchor;  // [P][3] anchor displacement for the current step
+  // FP32-compensated form (the predictor of the next step runs in the bond kernel's tail:
+  // disp/disp32 are read for this step while disp_next/disp32_next receive the next one)
+  float4 *pos32, *disp32, *disp32_next;
+  double *disp_next;
+  const uint8_t *clamp_flag;  // 1 for nodes listed in clamped_nodes
+  int fused;                  // 1: FP32 form with the fused predictor
+  const double *anchor;       // [P][3] anchor of disp32 (this step)
+  double *anchor_next;        // [P][3] anchor of disp32_next
   double break_band;     // relative band around snot where the FP64 stretch decides
   double *f_extra;       // [3][Ncap] FP64 non-bond force density of flagged nodes
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
@@ -194,6 +199,7 @@ class Engine {
   int alloc_candidates();
   int build_bonds();
   int launch_step_seq(int cur, cudaStream_t s);
+  int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
   int check(cudaError_t e, const char *what);
   DevView view(int cur) const;
@@ -223,6 +229,10 @@ class Engine {
 
   // device buffers
   double *d_pos_ = nullptr, *d_disp_ = nullptr, *d_vel_[2] = {nullptr, nullptr}, *d_acc_ = nullptr;
+  double *d_dispb_[2] = {nullptr, nullptr};  // FP32 form: double-buffered displacement
+  float4 *d_disp32b_[2] = {nullptr, nullptr};
+  double *d_anchor_next_ = nullptr;
+  uint8_t *d_clamp_flag_ = nullptr;
   double *d_force_ = nullptr, *d_ext_ = nullptr, *d_vol_ = nullptr;
   uint32_t *d_pid_ = nullptr;
   uint8_t *d_bdry_ = nullptr;
@@ -263,6 +273,7 @@ void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s);
 void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
+void launch_anchor_next(const DevView &v, cudaStream_t s);
 
 }  // namespace pdg
 #endif

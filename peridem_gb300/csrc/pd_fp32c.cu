@@ -157,6 +157,46 @@ __global__ void __launch_bounds__(128) k_extra32(DevView v) {
   v.extra_flag[n] = 1;
 }
 
+// FP64 stretch of the reference formula (particle2.h:139-149) for a bond whose FP32 stretch
+// lies in the band around snot; clears the bond's live bit when it exceeds snot. Kept out of
+// line so that the compiler does not predicate its FP64 work into the bond loop.
+__device__ __noinline__ void band_check(const DevView &v, uint64_t n, uint32_t q, uint32_t *word, uint32_t lane,
+                                        double snot) {
+  const uint64_t C3 = v.Ncap;
+  const D3 di = ld3(v.disp, n, C3), pi = ld3(v.pos, n, C3);
+  D3 xi64 = ld3(v.pos, q, C3) - pi;
+  D3 eta = (ld3(v.disp, q, C3) - di) + xi64;
+  double en = norm3(eta), xn = norm3(xi64);
+  if (((en - xn) / xn) > snot) atomicAnd(word, ~(1u << lane));
+}
+
+__device__ __noinline__ void cut_bond(uint32_t *word, uint32_t lane) { atomicAnd(word, ~(1u << lane)); }
+
+// One bond in FP32: cancellation-free stretch and Kahan-compensated accumulation.
+struct Acc32 {
+  float sx, sy, sz, cx, cy, cz;
+};
+
+__device__ __forceinline__ float bond32(const float4 &pi, const float4 &ui, const float4 &pq, const float4 &uq,
+                                        float cn, Acc32 &a) {
+  const float xx = pq.x - pi.x, xy = pq.y - pi.y, xz = pq.z - pi.z;
+  const float ex = uq.x - ui.x, ey = uq.y - ui.y, ez = uq.z - ui.z;
+  const float yx = xx + ex, yy = xy + ey, yz = xz + ez;
+  const float xin = sqrtf(fmaf(xx, xx, fmaf(xy, xy, xz * xz)));
+  const float yn = sqrtf(fmaf(yx, yx, fmaf(yy, yy, yz * yz)));
+  const float xe = fmaf(xx, ex, fmaf(xy, ey, xz * ez));
+  const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+  const float str = __fdividef(fmaf(2.f, xe, ee), (yn + xin) * xin);
+  const float g = __fdividef(cn * str * pq.w, yn);
+  float t, y;
+  y = fmaf(g, yx, -a.cx); t = a.sx + y; a.cx = (t - a.sx) - y; a.sx = t;
+  y = fmaf(g, yy, -a.cy); t = a.sy + y; a.cy = (t - a.sy) - y; a.sy = t;
+  y = fmaf(g, yz, -a.cz); t = a.sz + y; a.cz = (t - a.sz) - y; a.sz = t;
+  return str;
+}
+
+constexpr int kUnroll = 4;
+
 __global__ void __launch_bounds__(128) k_bond32(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
@@ -169,66 +209,93 @@ __global__ void __launch_bounds__(128) k_bond32(DevView v) {
   const uint64_t C3 = v.Ncap;
   const float4 pi4 = v.pos32[nn];
   const float4 ui4 = v.disp32[nn];
-  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  unsigned long long live = 0;
+  Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  uint32_t live = 0;
   if (run && movable) {
-    const uint64_t s = nn >> 5;
     const uint32_t lane = (uint32_t)(nn & 31);
-    const uint64_t sbase = v.slice_ptr[s];
+    const uint64_t sbase = v.slice_ptr[nn >> 5];
     const uint32_t *colp = v.col + sbase + lane;
     uint32_t *maskp = v.mask + (sbase >> 5);
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
-    const float cn = (float)P.cnot;
-    const float snot_lo = (float)(P.snot * (1.0 - v.break_band));
-    const float snot_hi = (float)(P.snot * (1.0 + v.break_band));
-    for (int j = 0; j < dg; ++j) {
+    const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
+    const float4 *__restrict__ p32 = v.pos32;
+    const float4 *__restrict__ d32 = v.disp32;
+    int j = 0;
+    for (; j + kUnroll <= dg; j += kUnroll) {
+      uint32_t q[kUnroll], m[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        q[u] = __ldg(colp + 32 * (j + u));
+        m[u] = maskp[j + u];
+      }
+      float4 pq[kUnroll], uq[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        pq[u] = __ldg(p32 + q[u]);
+        uq[u] = __ldg(d32 + q[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        if ((m[u] >> lane) & 1u) {
+          ++live;
+          const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
+          if (brk && str > slo) {
+            if (str > shi) cut_bond(&maskp[j + u], lane);
+            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot);
+          }
+        }
+      }
+    }
+    for (; j < dg; ++j) {
       const uint32_t mw = maskp[j];
       if (!((mw >> lane) & 1u)) continue;
-      const uint32_t q = colp[32 * j];
+      const uint32_t q = __ldg(colp + 32 * j);
       ++live;
-      const float4 pq = v.pos32[q];
-      const float4 uq = v.disp32[q];
-      const float xx = pq.x - pi4.x, xy = pq.y - pi4.y, xz = pq.z - pi4.z;
-      const float ex = uq.x - ui4.x, ey = uq.y - ui4.y, ez = uq.z - ui4.z;
-      const float yx = xx + ex, yy = xy + ey, yz = xz + ez;
-      const float xin = sqrtf(fmaf(xx, xx, fmaf(xy, xy, xz * xz)));
-      const float yn = sqrtf(fmaf(yx, yx, fmaf(yy, yy, yz * yz)));
-      const float xe = fmaf(xx, ex, fmaf(xy, ey, xz * ez));
-      const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-      const float str = __fdividef(fmaf(2.f, xe, ee), (yn + xin) * xin);
-      const float g = __fdividef(cn * str * pq.w, yn);
-      float t, y;
-      y = fmaf(g, yx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
-      y = fmaf(g, yy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
-      y = fmaf(g, yz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
-      if (brk && str > snot_lo) {
-        bool cut = str > snot_hi;
-        if (!cut) {
-          const D3 di = ld3(v.disp, nn, C3), pi = ld3(v.pos, nn, C3);
-          D3 xi64 = ld3(v.pos, q, C3) - pi;
-          D3 eta = (ld3(v.disp, q, C3) - di) + xi64;
-          double en = norm3(eta), xn = norm3(xi64);
-          cut = ((en - xn) / xn) > P.snot;
-        }
-        if (cut) atomicAnd(&maskp[j], ~(1u << lane));
+      const float str = bond32(pi4, ui4, __ldg(p32 + q), __ldg(d32 + q), cn, a);
+      if (brk && str > slo) {
+        if (str > shi) cut_bond(&maskp[j], lane);
+        else band_check(v, nn, q, &maskp[j], lane, P.snot);
       }
     }
   }
+  float i2 = 0.f;  // squared displacement increment of the next step (broad-phase bound)
   if (run) {
-    D3 f = d3((double)sx - (double)cx, (double)sy - (double)cy, (double)sz - (double)cz);
+    D3 f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
     if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, C3);
     st3(v.force, nn, C3, f);
     if (nonfinite(f.x) || nonfinite(f.y) || nonfinite(f.z)) atomicOr(&v.cnt->err, PD_DERR_NONFINITE);
     const D3 vi = ld3(v.vel_in, nn, C3);
     D3 vo = vi;
+    D3 an = ld3(v.acc, nn, C3);
+    const DevSimParams &sp = v.sp[P.sim];
+    const bool clamped = movable && v.clamp_flag[nn];
     if (movable) {
-      const D3 ao = ld3(v.acc, nn, C3);
-      const D3 an = P.irho * f;
-      vo = vi + v.sp[P.sim].hdt * (ao + an);
+      // velocity-Verlet corrector (timeloop.h:670-682)
+      const D3 ao = an;
+      an = P.irho * f;
+      vo = vi + sp.hdt * (ao + an);
+      if (clamped) {  // timeloop.h:767-774
+        vo = d3(0.0, 0.0, 0.0);
+        an = d3(0.0, 0.0, 0.0);
+      }
       st3(v.acc, nn, C3, an);
     }
     st3(v.vel_out, nn, C3, vo);
+    // predictor of the next step (timeloop.h:537-540)
+    const D3 d = ld3(v.disp, nn, C3);
+    D3 dn;
+    if (clamped) {
+      dn = d3(0.0, 0.0, 0.0);
+    } else {
+      const D3 inc = sp.dt * vo + sp.hdt2 * an;
+      dn = d + inc;
+    }
+    st3(v.disp_next, nn, C3, dn);
+    const float ix = (float)(dn.x - d.x), iy = (float)(dn.y - d.y), iz = (float)(dn.z - d.z);
+    i2 = ix * ix + iy * iy + iz * iz;
+    const double *anx = v.anchor_next + 3 * (uint64_t)k;
+    v.disp32_next[nn] = make_float4((float)(dn.x - anx[0]), (float)(dn.y - anx[1]), (float)(dn.z - anx[2]), 0.f);
   }
   // particle AABB of this step's positions in the particle's local frame
   {
@@ -255,10 +322,27 @@ __global__ void __launch_bounds__(128) k_bond32(DevView v) {
       }
     }
   }
+  for (int o = 16; o > 0; o >>= 1) i2 = fmaxf(i2, __shfl_xor_sync(0xffffffffu, i2, o));
+  if ((threadIdx.x & 31) == 0 && i2 > 0.f) {
+    const double inc = sqrt((double)i2) * (1.0 + 1e-5);
+    atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(inc));
+  }
   if (v.stats) {
     for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
-    if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, live);
+    if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
   }
+}
+
+// A_next := this step's predicted displacement of each particle's anchor node.
+__global__ void k_anchor_next(DevView v) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= v.P) return;
+  const uint32_t g0 = v.parts[k].g0;
+  for (int c = 0; c < 3; ++c) v.anchor_next[3 * (uint64_t)k + c] = v.disp[g0 + c * v.Ncap];
+}
+
+void launch_anchor_next(const DevView &v, cudaStream_t s) {
+  if (v.P) k_anchor_next<<<(v.P + 127) / 128, 128, 0, s>>>(v);
 }
 
 void launch_step_fp32c(const DevView &v, cudaStream_t s) {

@@ -315,8 +315,9 @@ __global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const ui
     }
   }
   // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
-  // keeps this step's predicted displacement, saved for the readback
-  if (clamped_ptr) {
+  // keeps this step's predicted displacement, saved for the readback (the fused FP32 form
+  // zeroes them in its corrector and keeps this step's displacement buffer intact)
+  if (clamped_ptr && !v.fused) {
     double jump = 0;
     for (uint32_t c = clamped_ptr[k]; c < clamped_ptr[k + 1]; ++c) {
       uint64_t g = clamped[c];
@@ -374,7 +375,8 @@ __global__ void k_end_sims(DevView v, double half_skin) {
     DevCounters &c = *v.cnt;
     double stepmax = __longlong_as_double((long long)c.stepmax_bits);
     if (c.rebuild) {
-      c.moved = 0.0;
+      // with the fused predictor, stepmax already bounds the next step's movement
+      c.moved = v.fused ? stepmax : 0.0;
       c.rebuilds += 1;
     } else {
       c.moved += stepmax;
