@@ -207,6 +207,15 @@ double pd_step_bytes(const pd_sim *sim);
 int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 /* Live directed bonds of movable particles (the bond-update count of the next step). */
 int pd_count_live_bonds(pd_sim *sim, uint64_t *live);
+/* Same count as pd_count_live_bonds, but allocating nothing: for callers that must not call
+ * cudaMalloc -- a monitor polling a running simulation (cudaMalloc would synchronise the
+ * device under the step pipeline) or an application that has handed all free HBM to resident
+ * simulations. Scratch lives in a static 32 KB device array shared by all calls on a device
+ * (concurrent calls race; each call overwrites what it reads). At most 1,048,576 nodes, larger
+ * handles get PD_EINVAL. The first call on a device looks up the array's address; make it
+ * before any stream capture, with the simulation's device current. This entry point has no
+ * counterpart in the reference. */
+int pd_count_live_bonds_noalloc(pd_sim *sim, uint64_t *live);
 
 #ifdef __cplusplus
 }

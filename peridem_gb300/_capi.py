@@ -112,6 +112,7 @@ SIGNATURES = [
     ("pd_step_bytes", _f64, [_P]),
     ("pd_profile_steps", C.c_int, [_P, _u32, _P]),
     ("pd_count_live_bonds", C.c_int, [_P, C.POINTER(_u64)]),
+    ("pd_count_live_bonds_noalloc", C.c_int, [_P, C.POINTER(_u64)]),
 ]
 
 _lib = None

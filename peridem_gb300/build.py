@@ -27,6 +27,7 @@ UNITS = [
     ("pd_kernels.cu", ["-fmad=false"]),
     ("pd_broadphase.cu", []),
     ("pd_fp32c.cu", []),
+    ("pd_noalloc.cu", []),
     ("pd_engine.cu", ["-fmad=false"]),
     ("pd_capi.cpp", []),
     ("pd_config.cpp", []),

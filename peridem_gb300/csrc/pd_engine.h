@@ -191,6 +191,8 @@ class Engine {
   uint64_t steps_done() const { return steps_done_; }
   cudaStream_t stream() const { return stream_; }
   int precision() const { return precision_; }
+  // Device view of the state between steps (what the next step reads).
+  DevView current_view() const { return view(cur_); }
   std::string err;
   const std::vector<HostSim> &sims() const { return sims_; }
 
