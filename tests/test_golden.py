@@ -1,0 +1,58 @@
+"""Checks against golden frames written by PeriDEM's own code (tests/golden/make_golden.py):
+the CPU oracle everywhere (it must reproduce the reference bit for bit), and the GPU FP64 form
+through the C-ABI on a GPU."""
+import numpy as np
+import pytest
+
+from tests.golden.make_golden import load
+from tests import cases
+
+NAMES = sorted(cases.CASES)
+
+
+def _check(name, g, t, counter, curpos, vel, acc, force, conn_fn, wall, reaction):
+    f = g["frames"][counter]
+    np.testing.assert_array_equal(curpos, f["CurrPos"], err_msg=f"{name} frame {counter} CurrPos")
+    np.testing.assert_array_equal(vel, f["vel"], err_msg=f"{name} frame {counter} vel")
+    np.testing.assert_array_equal(acc, f["acc"], err_msg=f"{name} frame {counter} acc")
+    np.testing.assert_array_equal(force, f["force"], err_msg=f"{name} frame {counter} force")
+    s = g["setup"]
+    co = f["conn_offset"]
+    for p in range(s.n_particles):
+        np.testing.assert_array_equal(conn_fn(p).astype(np.int64), f["conn"][co[p]:co[p + 1]])
+    np.testing.assert_array_equal(wall, f["wall_info"])
+    if "reaction" in f and reaction is not None:
+        scale = max(1e-300, np.abs(f["reaction"]).max())
+        assert np.abs(reaction - f["reaction"]).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference_golden(name):
+    from oracle import oracle as O
+    g = load(name)
+    cfg = g["config"]
+    orc = O.Oracle(g["setup"], cfg)
+    t = 0
+    for counter in sorted(g["frames"]):
+        orc.step(cfg["modulo"])
+        t += cfg["modulo"]
+        st = orc.state()
+        w, r = orc.wall()
+        _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], orc.connectivity, w, r)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_fp64_matches_reference_golden(name):
+    from peridem_gb300.sim import Sim
+    g = load(name)
+    cfg = g["config"]
+    sim = Sim(g["setup"], cfg, "fp64")
+    t = 0
+    for counter in sorted(g["frames"]):
+        sim.step(cfg["modulo"])
+        t += cfg["modulo"]
+        st = sim.state()
+        w, r = sim.wall()
+        _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], sim.connectivity, w, r)
+    sim.close()
