@@ -184,6 +184,23 @@ int pd_get_aabb(pd_sim *sim, double *lrtb);
 int pd_get_stats(pd_sim *sim, pd_stats *stats);
 /* Writes tc_%05u.h5 and wall_%05u.h5 for `counter` into the output dir. */
 int pd_write_frame(pd_sim *sim, uint32_t counter);
+/* Loads CurrPos/vel/acc (and, with enable_fracture, Connectivity) of tc_%05u.h5 and, with
+ * wall_resume, wall_%05u.h5 from the output dir (run_timeloop's resume, timeloop.h:262-312). */
+int pd_resume(pd_sim *sim, uint32_t resume_ind, int wall_resume);
+/* Text of the last error of pd_open / pd_run / pd_write_frame / pd_resume / pd_h5_*. */
+const char *pd_files_error(void);
+
+/* ---- HDF5 files of the schema (subset reader/writer, no libhdf5 needed) ---------------
+ * dtype codes: 1 f64, 2 i32, 3 u32, 4 i64, 5 u64, 6 f32. Paths like "P_00000/Pos". */
+void *pd_h5_writer_new(void);
+int pd_h5_writer_add(void *w, const char *path, int dtype, int rank, const uint64_t *dims, const void *data);
+int pd_h5_writer_write(void *w, const char *filename);
+void pd_h5_writer_free(void *w);
+void *pd_h5_open(const char *filename);
+size_t pd_h5_list(void *h, char *buf, size_t cap);
+int pd_h5_info(void *h, const char *path, int *rank, uint64_t *dims);
+int pd_h5_read(void *h, const char *path, int dtype, void *out, uint64_t cap_bytes);
+void pd_h5_close(void *h);
 /* Text of the last error on this handle (never NULL). */
 const char *pd_last_error(const pd_sim *sim);
 /* Text of the last error of a call that could not return a handle. */

@@ -47,6 +47,8 @@ def oracle_lib() -> C.CDLL:
         L.or_get_counts.argtypes = [_P, _P]
         L.or_get_stretch.restype = _u64
         L.or_get_stretch.argtypes = [_P, _u32, _P, _u64]
+        L.or_set_state.argtypes = [_P, _P, _P, _P]
+        L.or_set_connectivity.argtypes = [_P, _u32, _P, _u64]
         L.or_destroy.argtypes = [_P]
         _olib = L
     return _olib
@@ -118,6 +120,14 @@ class Oracle:
         c = np.zeros(4, dtype=np.uint64)
         oracle_lib().or_get_counts(self.h, _ptr(c))
         return dict(pairwise=int(c[0]), contacts=int(c[1]), live_bonds=int(c[2]), step=int(c[3]))
+
+    def set_state(self, disp=None, vel=None, acc=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (disp, vel, acc)]
+        oracle_lib().or_set_state(self.h, *(_ptr(a) for a in arrs))
+
+    def set_connectivity(self, p: int, pairs):
+        a = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+        oracle_lib().or_set_connectivity(self.h, p, _ptr(a), len(a))
 
     def stretch(self, p: int) -> np.ndarray:
         L = oracle_lib()

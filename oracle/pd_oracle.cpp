@@ -777,6 +777,39 @@ uint64_t or_get_stretch(or_sim *S, uint32_t particle, double *out, uint64_t cap)
   return c;
 }
 
+// Resume support (timeloop.h:274-293): new disp/vel/acc (N*3, any may be NULL), then the
+// CurrPos/AABB initialisation that precedes the loop (timeloop.h:389-393).
+int or_set_state(or_sim *S, const double *disp, const double *vel, const double *acc) {
+  for (Part &p : S->P) {
+    for (uint32_t k = 0; k < p.n; ++k) {
+      const uint64_t n = p.g0 + k;
+      for (int c = 0; c < 3; ++c) {
+        if (disp) p.disp[k].c[c] = disp[3 * n + c];
+        if (vel) p.vel[k].c[c] = vel[3 * n + c];
+        if (acc) p.acc[k].c[c] = acc[3 * n + c];
+      }
+    }
+    for (uint32_t k = 0; k < p.n; ++k) p.cur[k] = vadd(p.pos[k], p.disp[k]);
+    if (p.n) get_minmax(p.cur, p.lrtb);
+  }
+  return PD_OK;
+}
+
+// Connectivity of one particle replaced: conn2NArr + gen_xi (timeloop.h:285-291).
+int or_set_connectivity(or_sim *S, uint32_t particle, const uint32_t *pairs, uint64_t n) {
+  if (particle >= S->P.size()) return PD_EINVAL;
+  Part &p = S->P[particle];
+  p.nbr.assign(p.n, {});
+  for (uint64_t l = 0; l < n; ++l) {
+    const uint32_t i = pairs[2 * l], j = pairs[2 * l + 1];
+    if (i >= p.n || j >= p.n) return PD_EINVAL;
+    p.nbr[i].push_back(j);
+    p.nbr[j].push_back(i);
+  }
+  gen_xi(p);
+  return PD_OK;
+}
+
 void or_destroy(or_sim *S) { delete S; }
 
 }  // extern "C"

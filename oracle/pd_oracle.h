@@ -37,6 +37,8 @@ int or_get_counts(or_sim *s, uint64_t *counts);
 /* Stretch of every live bond of a particle from the last force evaluation, in NbdArr
  * order (row i ascending, neighbours ascending); returns the count. */
 uint64_t or_get_stretch(or_sim *s, uint32_t particle, double *out, uint64_t cap);
+int or_set_state(or_sim *s, const double *disp, const double *vel, const double *acc);
+int or_set_connectivity(or_sim *s, uint32_t particle, const uint32_t *pairs, uint64_t n);
 void or_destroy(or_sim *s);
 
 #ifdef __cplusplus

@@ -856,3 +856,72 @@ int Engine::count_live_bonds(uint64_t *live) {
 }
 
 }  // namespace pdg
+
+namespace pdg {
+
+int Engine::set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t n) {
+  if (particle >= P_) {
+    err = "particle index out of range";
+    return PD_EINVAL;
+  }
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t g0 = h_g0_[particle];
+  uint64_t nloc = 0;
+  {
+    uint32_t pacc = 0;
+    for (auto &s : sims_) {
+      if (particle < pacc + s.np) {
+        nloc = s.node_offset[particle - pacc + 1] - s.node_offset[particle - pacc];
+        break;
+      }
+      pacc += s.np;
+    }
+  }
+  std::vector<uint64_t> keys(n);
+  for (uint64_t l = 0; l < n; ++l) {
+    uint64_t a = pairs[2 * l], b = pairs[2 * l + 1];
+    if (a >= nloc || b >= nloc) {
+      err = "connectivity index out of range";
+      return PD_EINVAL;
+    }
+    if (a > b) std::swap(a, b);
+    keys[l] = a * nloc + b;
+  }
+  std::sort(keys.begin(), keys.end());
+  const uint64_t s0 = g0 >> 5, s1 = std::min<uint64_t>((g0 + nloc + 31) >> 5, nslices_);
+  const uint64_t e0 = h_slice_ptr_[s0], e1 = h_slice_ptr_[s1];
+  if (e1 == e0) return PD_OK;
+  std::vector<uint32_t> col(e1 - e0), mask((e1 - e0) / 32);
+  PD_TRY(check(cudaMemcpy(col.data(), d_col_ + e0, (e1 - e0) * 4, cudaMemcpyDeviceToHost), "read col"));
+  PD_TRY(check(cudaMemcpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, cudaMemcpyDeviceToHost), "read mask"));
+  for (uint64_t i = 0; i < nloc; ++i) {
+    const uint64_t g = g0 + i;
+    const uint64_t base = h_slice_ptr_[g >> 5] - e0 + (g & 31);
+    const uint64_t mbase = (h_slice_ptr_[g >> 5] - e0) >> 5;
+    const uint32_t bit = 1u << (g & 31);
+    for (uint32_t j = 0; j < h_deg_[g]; ++j) {
+      uint64_t q = col[base + 32ull * j] - g0;
+      uint64_t a = std::min<uint64_t>(i, q), b = std::max<uint64_t>(i, q);
+      const bool live = std::binary_search(keys.begin(), keys.end(), a * nloc + b);
+      if (live)
+        mask[mbase + j] |= bit;
+      else
+        mask[mbase + j] &= ~bit;
+    }
+  }
+  PD_TRY(check(cudaMemcpy(d_mask_ + e0 / 32, mask.data(), (e1 - e0) / 32 * 4, cudaMemcpyHostToDevice), "write mask"));
+  return PD_OK;
+}
+
+int Engine::set_wall(uint32_t sim, const double *wall_info) {
+  if (sim >= S_) return PD_EINVAL;
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  DevSimState st;
+  PD_TRY(check(cudaMemcpy(&st, d_ss_ + sim, sizeof(st), cudaMemcpyDeviceToHost), "read sim state"));
+  for (int k = 0; k < 6; ++k) st.wall[k] = wall_info[k];
+  PD_TRY(check(cudaMemcpy(d_ss_ + sim, &st, sizeof(st), cudaMemcpyHostToDevice), "write sim state"));
+  if (precision_ == PD_FP32C) PD_TRY(prepare_fused(cur_));  // walls in the local frames
+  return check(cudaStreamSynchronize(stream_), "set_wall");
+}
+
+}  // namespace pdg

@@ -172,6 +172,9 @@ class Engine {
   int get_state(double *curpos, double *vel, double *acc, double *force, double *disp);
   int set_state(const double *disp, const double *vel, const double *acc);
   int get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, uint64_t *n);
+  // Keeps exactly the listed bonds (local i<q pairs) of a particle alive (resume).
+  int set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t n);
+  int set_wall(uint32_t sim, const double *wall_info);
   int get_wall(uint32_t sim, double *wall_info, double *reaction);
   int get_aabb(double *lrtb);
   int get_stats(pd_stats *st);

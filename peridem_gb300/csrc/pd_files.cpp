@@ -1,28 +1,450 @@
-// pd_files.cpp -- file boundary (setup.h5 in, plotinfo/tc/wall frames out).
+// pd_files.cpp -- the file boundary: setup.h5 in (load_particles/load_contact/load_wall,
+// src/read/load_hdf5.h:41-181), plotinfo.h5 / tc_%05u.h5 / wall_%05u.h5 / run_time.h5 out
+// (src/particle/timeloop.h:321-350, 801-964), the resume path (timeloop.h:262-312), the
+// whole time loop with saves and the progress table (timeloop.h:352-369, 909-947), plus a
+// small C API over h5lite so that scripts can write setup files and read frames.
+#include <sys/stat.h>
+
+#include <chrono>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <sstream>
 #include <string>
 
+#include "h5lite.h"
 #include "pd_sim.h"
+
+namespace {
+
+thread_local std::string g_ferr;
+
+int fail(int rc, const std::string &m) {
+  g_ferr = m;
+  return rc;
+}
+
+std::string pnum(unsigned p) {
+  char b[32];
+  std::snprintf(b, sizeof(b), "P_%05u", p);
+  return b;
+}
+
+bool read_col_f64(const h5lite::Reader &r, const std::string &path, std::vector<double> &v, std::string &err) {
+  std::vector<uint64_t> dims;
+  return r.read_vec<double>(path, h5lite::F64, v, dims, err);
+}
+
+template <typename T>
+bool read_any(const h5lite::Reader &r, const std::string &path, int dt, std::vector<T> &v, std::string &err) {
+  std::vector<uint64_t> dims;
+  return r.read_vec<T>(path, dt, v, dims, err);
+}
+
+// load_particles<3> + load_contact + load_wall<3> (load_hdf5.h:41-181)
+int load_setup(const std::string &fn, pdg::HostSim &hs, std::string &err) {
+  h5lite::Reader r;
+  if (!r.open(fn, err)) return PD_EIO;
+  std::vector<uint32_t> tp;
+  if (!read_any<uint32_t>(r, "total_particles_univ", h5lite::U32, tp, err) || tp.empty()) return PD_EIO;
+  const uint32_t np = tp[0];
+  hs.np = np;
+  hs.node_offset.assign(1, 0);
+  hs.conn_offset.assign(1, 0);
+  hs.bdry_offset.assign(1, 0);
+  hs.clamped_offset.assign(1, 0);
+  for (uint32_t p = 0; p < np; ++p) {
+    const std::string g = pnum(p) + "/";
+    std::vector<double> pos, vol, disp, vel, acc, ext, sc;
+    std::vector<uint64_t> dims;
+    if (!r.read_vec<double>(g + "Pos", h5lite::F64, pos, dims, err)) return PD_EIO;
+    if (dims.size() != 2 || dims[1] != 3) {
+      err = g + "Pos is not an (N,3) array";
+      return PD_EIO;
+    }
+    const uint64_t n = dims[0];
+    if (!read_col_f64(r, g + "Vol", vol, err) || vol.size() != n) {
+      if (err.empty()) err = g + "Vol size mismatch";
+      return PD_EIO;
+    }
+    for (const char *k : {"disp", "vel", "acc", "extforce"}) {
+      std::vector<double> *dst = (std::strcmp(k, "disp") == 0) ? &disp
+                                 : (std::strcmp(k, "vel") == 0) ? &vel
+                                 : (std::strcmp(k, "acc") == 0) ? &acc : &ext;
+      if (!r.read_vec<double>(g + k, h5lite::F64, *dst, dims, err)) return PD_EIO;
+      if (dst->size() != 3 * n) {
+        err = g + k + " size mismatch";
+        return PD_EIO;
+      }
+    }
+    std::vector<uint32_t> conn, bdry, clamped;
+    if (!r.read_vec<uint32_t>(g + "Connectivity", h5lite::U32, conn, dims, err)) return PD_EIO;
+    if (!conn.empty() && (dims.size() != 2 || dims[1] != 2)) {
+      err = g + "Connectivity is not an (M,2) array";
+      return PD_EIO;
+    }
+    if (r.has(g + "bdry_nodes") && !r.read_vec<uint32_t>(g + "bdry_nodes", h5lite::U32, bdry, dims, err)) return PD_EIO;
+    if (r.has(g + "clamped_nodes") && !r.read_vec<uint32_t>(g + "clamped_nodes", h5lite::U32, clamped, dims, err))
+      return PD_EIO;
+    auto scalar = [&](const char *k, double &out) -> bool {
+      std::vector<double> v;
+      if (!read_col_f64(r, g + k, v, err) || v.empty()) {
+        if (err.empty()) err = g + k + " is empty";
+        return false;
+      }
+      out = v[0];
+      return true;
+    };
+    double delta, rho, cnot, snot, tval = 0, mov = 1, brk = 1, stp = 1, tax = 2;
+    if (!scalar("delta", delta) || !scalar("rho", rho) || !scalar("cnot", cnot) || !scalar("snot", snot) ||
+        !scalar("movable", mov) || !scalar("breakable", brk) || !scalar("stoppable", stp) ||
+        !scalar("torque_axis", tax) || !scalar("torque_val", tval))
+      return PD_EIO;
+    hs.pos.insert(hs.pos.end(), pos.begin(), pos.end());
+    hs.vol.insert(hs.vol.end(), vol.begin(), vol.end());
+    hs.disp.insert(hs.disp.end(), disp.begin(), disp.end());
+    hs.vel.insert(hs.vel.end(), vel.begin(), vel.end());
+    hs.acc.insert(hs.acc.end(), acc.begin(), acc.end());
+    hs.ext.insert(hs.ext.end(), ext.begin(), ext.end());
+    hs.conn.insert(hs.conn.end(), conn.begin(), conn.end());
+    hs.bdry.insert(hs.bdry.end(), bdry.begin(), bdry.end());
+    hs.clamped.insert(hs.clamped.end(), clamped.begin(), clamped.end());
+    hs.node_offset.push_back(hs.node_offset.back() + n);
+    hs.conn_offset.push_back(hs.conn_offset.back() + conn.size() / 2);
+    hs.bdry_offset.push_back(hs.bdry_offset.back() + bdry.size());
+    hs.clamped_offset.push_back(hs.clamped_offset.back() + clamped.size());
+    hs.delta.push_back(delta);
+    hs.rho.push_back(rho);
+    hs.cnot.push_back(cnot);
+    hs.snot.push_back(snot);
+    hs.tval.push_back(tval);
+    hs.movable.push_back((int32_t)mov);
+    hs.breakable.push_back((int32_t)brk);
+    hs.stoppable.push_back((int32_t)stp);
+    hs.taxis.push_back((uint32_t)tax);
+  }
+  std::vector<double> v;
+  if (!read_col_f64(r, "pairwise/contact_radius", v, err) || v.empty()) return PD_EIO;
+  hs.Rc = v[0];
+  if (!read_col_f64(r, "pairwise/normal_stiffness", v, err) || v.empty()) return PD_EIO;
+  hs.Kn = v[0];
+  if (!read_col_f64(r, "pairwise/friction_coefficient", v, err) || v.empty()) return PD_EIO;
+  hs.mu = v[0];
+  if (!read_col_f64(r, "pairwise/damping_ratio", v, err) || v.empty()) return PD_EIO;
+  hs.zeta = v[0];
+  std::vector<uint32_t> aw;
+  if (!read_any<uint32_t>(r, "wall/allow_wall", h5lite::U32, aw, err) || aw.empty()) return PD_EIO;
+  hs.allow_wall = aw[0] != 0;
+  if (!read_col_f64(r, "wall/geom_wall_info", v, err)) return PD_EIO;
+  hs.n_geom_wall = (int32_t)v.size();
+  if (v.size() != 1) {
+    if (v.size() < 6) {
+      err = "wall/geom_wall_info has " + std::to_string(v.size()) + " entries (3D needs 6)";
+      return PD_EIO;
+    }
+    for (int k = 0; k < 6; ++k) hs.geom[k] = v[k];
+  }
+  return PD_OK;
+}
+
+bool is_dir(const std::string &p) {
+  struct stat st;
+  return stat(p.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
+std::string format_ms(int ms) {
+  int s = ms / 1000, mi = s / 60, rs = s % 60, hr = mi / 60, rm = mi % 60;
+  std::stringstream ss;
+  ss << hr << ":" << std::setfill('0') << std::setw(2) << rm << ":" << std::setfill('0') << std::setw(2) << rs;
+  return ss.str();
+}
+
+}  // namespace
 
 extern "C" {
 
+const char *pd_files_error(void) { return g_ferr.c_str(); }
+
 int pd_open(const char *conf, const char *setup_h5, const char *outdir, int precision, pd_sim **out) {
-  (void)conf;
-  (void)setup_h5;
-  (void)outdir;
-  (void)precision;
-  if (out) *out = nullptr;
-  return PD_EIO;
+  if (!out) return fail(PD_EINVAL, "null output handle");
+  *out = nullptr;
+  pd_config cfg;
+  pd_config_default(&cfg);
+  if (setup_h5) std::strncpy(cfg.setup_filename, setup_h5, sizeof(cfg.setup_filename) - 1);
+  if (outdir) std::strncpy(cfg.output_dir, outdir, sizeof(cfg.output_dir) - 1);
+  if (conf) {
+    int rc = pd_config_read(conf, &cfg);
+    if (rc != PD_OK && rc != PD_ECONFIG) return fail(rc, "config read failed");
+    if (rc == PD_ECONFIG) {
+      // the reference carries on with defaults when the file cannot be opened
+      std::ifstream probe(conf);
+      if (probe.good()) return fail(PD_ECONFIG, std::string("bad value in config file ") + conf);
+    }
+  }
+  std::vector<pdg::HostSim> sims(1);
+  std::string err;
+  int rc = load_setup(cfg.setup_filename, sims[0], err);
+  if (rc != PD_OK) return fail(rc, "setup: " + err);
+  sims[0].cfg = cfg;
+  pd_sim *s = new pd_sim();
+  s->cfg = cfg;
+  s->outdir = cfg.output_dir;
+  rc = s->eng.init(sims, precision);
+  if (rc != PD_OK) {
+    std::string e = s->eng.err;
+    delete s;
+    return fail(rc, e);
+  }
+  *out = s;
+  return PD_OK;
 }
 
-int pd_run(pd_sim *sim) {
-  (void)sim;
-  return PD_EIO;
+int pd_write_frame(pd_sim *s, uint32_t counter) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  const uint64_t N = s->eng.num_nodes();
+  const uint32_t P = s->eng.num_particles();
+  std::vector<double> cur(3 * N), vel(3 * N), acc(3 * N), force(3 * N);
+  int rc = s->eng.get_state(cur.data(), vel.data(), acc.data(), force.data(), nullptr);
+  if (rc != PD_OK) return rc;
+  const auto &hs = s->eng.sims()[0];
+  h5lite::Writer w;
+  for (uint32_t p = 0; p < P; ++p) {
+    const uint64_t a = hs.node_offset[p], n = hs.node_offset[p + 1] - a;
+    const std::string g = pnum(p) + "/";
+    w.add(g + "CurrPos", h5lite::F64, {n, 3}, cur.data() + 3 * a);
+    w.add(g + "vel", h5lite::F64, {n, 3}, vel.data() + 3 * a);
+    w.add(g + "acc", h5lite::F64, {n, 3}, acc.data() + 3 * a);
+    w.add(g + "force", h5lite::F64, {n, 3}, force.data() + 3 * a);
+    uint64_t m = 0;
+    rc = s->eng.get_connectivity(p, nullptr, 0, &m);
+    if (rc != PD_OK) return rc;
+    std::vector<uint32_t> conn(2 * m);
+    rc = s->eng.get_connectivity(p, conn.data(), m, &m);
+    if (rc != PD_OK) return rc;
+    w.add(g + "Connectivity", h5lite::U32, {m, 2}, conn.data());
+  }
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "/tc_%05u.h5", counter);
+  std::string err;
+  if (!w.write(s->outdir + buf, err)) return fail(PD_EIO, err);
+  double wall[6], react[18];
+  rc = s->eng.get_wall(0, wall, react);
+  if (rc != PD_OK) return rc;
+  h5lite::Writer ww;
+  ww.add("wall_info", h5lite::F64, {6, 1}, wall);
+  if (s->cfg.compute_wall_reaction) ww.add("reaction", h5lite::F64, {6, 3}, react);
+  std::snprintf(buf, sizeof(buf), "/wall_%05u.h5", counter);
+  if (!ww.write(s->outdir + buf, err)) return fail(PD_EIO, err);
+  return PD_OK;
 }
 
-int pd_write_frame(pd_sim *sim, uint32_t counter) {
-  (void)sim;
-  (void)counter;
-  return PD_EIO;
+// Sets the kinematic state (and, with enable_fracture, the surviving bonds) from a saved
+// frame, like the resume branch of run_timeloop (timeloop.h:262-312).
+int pd_resume(pd_sim *s, uint32_t resume_ind, int wall_resume) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "/tc_%05u.h5", resume_ind);
+  h5lite::Reader r;
+  std::string err;
+  if (!r.open(s->outdir + buf, err)) return fail(PD_EIO, err);
+  const auto &hs = s->eng.sims()[0];
+  const uint64_t N = s->eng.num_nodes();
+  std::vector<double> disp(3 * N), vel(3 * N), acc(3 * N);
+  for (uint32_t p = 0; p < hs.np; ++p) {
+    const std::string g = pnum(p) + "/";
+    const uint64_t a = hs.node_offset[p], n = hs.node_offset[p + 1] - a;
+    std::vector<double> cp, v, ac;
+    std::vector<uint64_t> dims;
+    if (!r.read_vec<double>(g + "CurrPos", h5lite::F64, cp, dims, err) || cp.size() != 3 * n ||
+        !r.read_vec<double>(g + "vel", h5lite::F64, v, dims, err) || v.size() != 3 * n ||
+        !r.read_vec<double>(g + "acc", h5lite::F64, ac, dims, err) || ac.size() != 3 * n)
+      return fail(PD_EIO, "resume frame: " + (err.empty() ? g + " size mismatch" : err));
+    for (uint64_t k = 0; k < 3 * n; ++k) {
+      disp[3 * a + k] = cp[k] - hs.pos[3 * a + k];  // disp = CurrPos - pos (timeloop.h:279-281)
+      vel[3 * a + k] = v[k];
+      acc[3 * a + k] = ac[k];
+    }
+    if (s->cfg.enable_fracture) {
+      std::vector<uint32_t> conn;
+      if (!r.read_vec<uint32_t>(g + "Connectivity", h5lite::U32, conn, dims, err))
+        return fail(PD_EIO, "resume frame: " + err);
+      int rc = s->eng.set_connectivity(p, conn.data(), conn.size() / 2);
+      if (rc != PD_OK) return rc;
+    }
+  }
+  int rc = s->eng.set_state(disp.data(), vel.data(), acc.data());
+  if (rc != PD_OK) return rc;
+  if (wall_resume) {
+    std::snprintf(buf, sizeof(buf), "/wall_%05u.h5", resume_ind);
+    h5lite::Reader rw;
+    if (!rw.open(s->outdir + buf, err)) return fail(PD_EIO, err);
+    std::vector<double> wi;
+    std::vector<uint64_t> dims;
+    if (!rw.read_vec<double>("wall_info", h5lite::F64, wi, dims, err) || wi.size() < 6)
+      return fail(PD_EIO, "wall resume: " + err);
+    rc = s->eng.set_wall(0, wi.data());
+    if (rc != PD_OK) return rc;
+  }
+  return PD_OK;
 }
+
+// run_timeloop's loop with saves, progress table and run_time.h5 (timeloop.h:314-964).
+int pd_run(pd_sim *s) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  pd_config &cf = s->cfg;
+  const std::string out = s->outdir;
+  if (!is_dir(out)) return fail(PD_EIO, "output directory does not exist: " + out);
+  std::cout << "Output data dir: " << out << std::endl;
+  uint32_t counter, first_counter, last_counter;
+  if (cf.do_resume) {
+    counter = cf.resume_ind + 1;
+    first_counter = counter;
+    last_counter = cf.resume_ind + cf.timesteps / cf.modulo;
+    char b[64];
+    std::snprintf(b, sizeof(b), "/tc_%05u.h5", cf.resume_ind);
+    std::cout << "Loading from file: " << out + b << std::endl;
+    int rc = pd_resume(s, cf.resume_ind, cf.wall_resume);
+    if (rc != PD_OK) return rc;
+    std::cout << "Resuming from counter " << counter << std::endl;
+  } else {
+    counter = 1;
+    first_counter = counter;
+    last_counter = cf.timesteps / cf.modulo;
+  }
+  {  // plotinfo.h5 (timeloop.h:320-350)
+    double wall[6];
+    s->eng.get_wall(0, wall, nullptr);
+    h5lite::Writer w;
+    uint32_t flc[2] = {first_counter, last_counter}, dim = 3, mod = cf.modulo;
+    int32_t aw = s->eng.sims()[0].allow_wall ? 1 : 0;
+    w.add("f_l_counter", h5lite::U32, {2, 1}, flc);
+    w.add("dimension", h5lite::U32, {1, 1}, &dim);
+    w.add("dt", h5lite::F64, {1, 1}, &cf.dt);
+    w.add("modulo", h5lite::U32, {1, 1}, &mod);
+    w.add("wall/allow_wall", h5lite::I32, {1, 1}, &aw);
+    w.add("wall/geom_wall_info", h5lite::F64, {6, 1}, wall);
+    std::string err;
+    std::cout << "Output plotinfo: " << out + "/plotinfo.h5" << std::endl;
+    if (!w.write(out + "/plotinfo.h5", err)) return fail(PD_EIO, err);
+  }
+  const unsigned cw = 12;
+  time_t now = time(nullptr);
+  char sc[64];
+  std::snprintf(sc, sizeof(sc), "ct[%d:%d]", (int)first_counter, (int)last_counter);
+  std::cout << "----------------------------------------------------------------------" << std::endl;
+  std::cout << "Starting time loop (Parallel=" << cf.is_parallel << "): " << ctime(&now);
+  std::cout << std::left << std::setw(cw) << "t " << std::setw(cw) << std::string(sc) << std::setw(cw + 5)
+            << "duration(s)" << std::setw(cw) << "rem(h:m:s)" << std::setw(cw) << "#contacts" << std::setw(cw)
+            << "time" << std::endl;
+  s->eng.set_tuning(0, 0, 0, cf.save_file ? 1 : 0, -1);
+  auto t0 = std::chrono::system_clock::now();
+  std::vector<double> run_time, t_ind;
+  std::vector<uint32_t> pw_vec;
+  uint32_t t = 0;
+  while (t < cf.timesteps) {
+    uint32_t n = cf.timesteps - t;
+    if (cf.save_file && cf.modulo) n = std::min<uint32_t>(n, cf.modulo - (t % cf.modulo));
+    int rc = s->eng.step(n);
+    if (rc == PD_OK) rc = s->eng.sync(-1);
+    if (rc != PD_OK) return rc;
+    t += n;
+    if (cf.save_file && cf.modulo && t % cf.modulo == 0) {
+      rc = pd_write_frame(s, counter);
+      if (rc != PD_OK) return rc;
+      pd_stats st;
+      s->eng.get_stats(&st);
+      auto t1 = std::chrono::system_clock::now();
+      const int ms = (int)std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count();
+      t0 = t1;
+      double avg = 0;
+      const int start = (int)run_time.size() - 10;
+      if (start > 0)
+        for (int c = start; c < (int)run_time.size(); ++c) avg += run_time[c];
+      avg /= 10;
+      const int rem = (int)((int)(last_counter - counter) * avg);
+      char ts[80];
+      time_t nt = time(nullptr);
+      strftime(ts, sizeof(ts), "%F-%T", localtime(&nt));
+      std::cout << std::left << std::setw(cw) << t << std::setw(cw) << counter << std::setw(cw + 5)
+                << (double)ms / 1000 << std::setw(cw) << format_ms(rem) << std::setw(cw) << st.pairwise_computations
+                << std::setw(cw) << ts << std::endl;
+      run_time.push_back(ms);
+      t_ind.push_back(t);
+      pw_vec.push_back((uint32_t)st.pairwise_computations);
+      ++counter;
+    }
+  }
+  if (is_dir("output/hdf5")) {  // run_time.h5 at the reference's fixed path (timeloop.h:957-964)
+    h5lite::Writer w;
+    w.add("run_time", h5lite::F64, {run_time.size(), 1}, run_time.data());
+    w.add("t_ind", h5lite::F64, {t_ind.size(), 1}, t_ind.data());
+    w.add("pairwise_computations", h5lite::U32, {pw_vec.size(), 1}, pw_vec.data());
+    std::string err;
+    w.write("output/hdf5/run_time.h5", err);
+  }
+  return PD_OK;
+}
+
+// ---- generic HDF5 access for scripts (setup writing, frame reading) -------------------
+
+void *pd_h5_writer_new(void) { return new h5lite::Writer(); }
+int pd_h5_writer_add(void *w, const char *path, int dtype, int rank, const uint64_t *dims, const void *data) {
+  if (!w || !path || rank < 0 || rank > 8) return PD_EINVAL;
+  static_cast<h5lite::Writer *>(w)->add(path, dtype, std::vector<uint64_t>(dims, dims + rank), data);
+  return PD_OK;
+}
+int pd_h5_writer_write(void *w, const char *filename) {
+  std::string err;
+  if (!w || !filename) return PD_EINVAL;
+  if (!static_cast<h5lite::Writer *>(w)->write(filename, err)) return fail(PD_EIO, err);
+  return PD_OK;
+}
+void pd_h5_writer_free(void *w) { delete static_cast<h5lite::Writer *>(w); }
+
+void *pd_h5_open(const char *filename) {
+  auto *r = new h5lite::Reader();
+  std::string err;
+  if (!filename || !r->open(filename, err)) {
+    g_ferr = err;
+    delete r;
+    return nullptr;
+  }
+  return r;
+}
+// Newline-separated dataset paths; returns the length needed (including the NUL).
+size_t pd_h5_list(void *h, char *buf, size_t cap) {
+  if (!h) return 0;
+  std::string all;
+  for (auto &p : static_cast<h5lite::Reader *>(h)->paths()) all += p + "\n";
+  if (buf && cap) {
+    size_t n = std::min(all.size(), cap - 1);
+    std::memcpy(buf, all.data(), n);
+    buf[n] = 0;
+  }
+  return all.size() + 1;
+}
+int pd_h5_info(void *h, const char *path, int *rank, uint64_t *dims) {
+  if (!h || !path) return PD_EINVAL;
+  const h5lite::Info *in = static_cast<h5lite::Reader *>(h)->info(path);
+  if (!in) return fail(PD_EIO, std::string("no dataset ") + path);
+  *rank = in->rank;
+  for (int i = 0; i < in->rank && i < 8; ++i) dims[i] = in->dims[i];
+  return PD_OK;
+}
+int pd_h5_read(void *h, const char *path, int dtype, void *out, uint64_t cap_bytes) {
+  if (!h || !path) return PD_EINVAL;
+  std::vector<uint8_t> b;
+  std::vector<uint64_t> dims;
+  std::string err;
+  if (!static_cast<h5lite::Reader *>(h)->read(path, dtype, b, dims, err)) return fail(PD_EIO, err);
+  if (b.size() > cap_bytes) return fail(PD_EINVAL, "buffer too small");
+  if (!b.empty()) std::memcpy(out, b.data(), b.size());
+  return PD_OK;
+}
+void pd_h5_close(void *h) { delete static_cast<h5lite::Reader *>(h); }
 
 }  // extern "C"
