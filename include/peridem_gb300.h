@@ -222,6 +222,16 @@ double pd_step_bytes(const pd_sim *sim);
  * returns the summed device milliseconds in phase_ms[4] = {predictor, broad phase, fused
  * force+corrector kernel, end-of-step}. */
 int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
+/* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM)
+ * for steps_per_variant steps from the same snapshot of the live state, restores the state
+ * and keeps the fastest. Results do not depend on the variant (same per-node summation
+ * order). variant_ms (may be NULL) receives pd_num_variants() timings in ms per step. */
+int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
+int pd_set_variant(pd_sim *sim, int variant);
+int pd_num_variants(void);
+/* Copy of all device state that stepping changes, and its restore (checkpoint in HBM). */
+int pd_snapshot(pd_sim *sim);
+int pd_restore(pd_sim *sim);
 /* Live directed bonds of movable particles (the bond-update count of the next step). */
 int pd_count_live_bonds(pd_sim *sim, uint64_t *live);
 /* Same count as pd_count_live_bonds, but allocating nothing: for callers that must not call

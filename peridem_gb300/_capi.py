@@ -113,6 +113,22 @@ SIGNATURES = [
     ("pd_profile_steps", C.c_int, [_P, _u32, _P]),
     ("pd_count_live_bonds", C.c_int, [_P, C.POINTER(_u64)]),
     ("pd_count_live_bonds_noalloc", C.c_int, [_P, C.POINTER(_u64)]),
+    ("pd_autotune", C.c_int, [_P, _u32, C.POINTER(C.c_int), _P]),
+    ("pd_set_variant", C.c_int, [_P, C.c_int]),
+    ("pd_num_variants", C.c_int, []),
+    ("pd_snapshot", C.c_int, [_P]),
+    ("pd_restore", C.c_int, [_P]),
+    ("pd_resume", C.c_int, [_P, _u32, C.c_int]),
+    ("pd_files_error", C.c_char_p, []),
+    ("pd_h5_writer_new", _P, []),
+    ("pd_h5_writer_add", C.c_int, [_P, C.c_char_p, C.c_int, C.c_int, C.POINTER(_u64), _P]),
+    ("pd_h5_writer_write", C.c_int, [_P, C.c_char_p]),
+    ("pd_h5_writer_free", None, [_P]),
+    ("pd_h5_open", _P, [C.c_char_p]),
+    ("pd_h5_list", C.c_size_t, [_P, C.c_char_p, C.c_size_t]),
+    ("pd_h5_info", C.c_int, [_P, C.c_char_p, C.POINTER(C.c_int), C.POINTER(_u64)]),
+    ("pd_h5_read", C.c_int, [_P, C.c_char_p, C.c_int, _P, _u64]),
+    ("pd_h5_close", None, [_P]),
 ]
 
 _lib = None

@@ -243,3 +243,29 @@ int pd_count_live_bonds(pd_sim *s, uint64_t *live) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int pd_autotune(pd_sim *s, uint32_t steps_per_variant, int *chosen, double *variant_ms) {
+  if (!s) return fail_global(PD_EINVAL, "null handle");
+  return s->eng.autotune(steps_per_variant, chosen, variant_ms);
+}
+
+int pd_set_variant(pd_sim *s, int variant) {
+  if (!s) return fail_global(PD_EINVAL, "null handle");
+  return s->eng.set_variant(variant);
+}
+
+int pd_num_variants(void) { return pdg::num_bond_variants(); }
+
+int pd_snapshot(pd_sim *s) {
+  if (!s) return fail_global(PD_EINVAL, "null handle");
+  return s->eng.snapshot();
+}
+
+int pd_restore(pd_sim *s) {
+  if (!s) return fail_global(PD_EINVAL, "null handle");
+  return s->eng.restore();
+}
+
+}  // extern "C"

@@ -515,7 +515,7 @@ int Engine::launch_step_seq(int cur, cudaStream_t s) {
   if (torque_possible_) launch_centroids(v, s);
   launch_bp_decide(v, half_skin_, s);
   launch_broadphase(v, bp_, s);
-  launch_step_kernel(v, precision_, tpb_, s);
+  launch_step_kernel(v, precision_, variant_, s);
   if (stats_) launch_pairwise_count(v, s);
   launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, s);
   return check(cudaGetLastError(), "step launch");
@@ -822,7 +822,7 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
     launch_bp_decide(v, half_skin_, s);
     launch_broadphase(v, bp_, s);
     cudaEventRecord(ev[2], s);
-    launch_step_kernel(v, precision_, tpb_, s);
+    launch_step_kernel(v, precision_, variant_, s);
     cudaEventRecord(ev[3], s);
     if (stats_) launch_pairwise_count(v, s);
     launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, s);
@@ -922,6 +922,120 @@ int Engine::set_wall(uint32_t sim, const double *wall_info) {
   PD_TRY(check(cudaMemcpy(d_ss_ + sim, &st, sizeof(st), cudaMemcpyHostToDevice), "write sim state"));
   if (precision_ == PD_FP32C) PD_TRY(prepare_fused(cur_));  // walls in the local frames
   return check(cudaStreamSynchronize(stream_), "set_wall");
+}
+
+}  // namespace pdg
+
+namespace pdg {
+
+int Engine::snapshot() {
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t C = Ncap_;
+  mutable_.clear();
+  auto reg = [&](void *p, size_t b) {
+    if (p && b) mutable_.push_back({p, b});
+  };
+  reg(d_disp_, 3 * C * 8);
+  if (d_dispb_[1]) reg(d_dispb_[1], 3 * C * 8);
+  reg(d_vel_[0], 3 * C * 8);
+  reg(d_vel_[1], 3 * C * 8);
+  reg(d_acc_, 3 * C * 8);
+  reg(d_force_, 3 * C * 8);
+  reg(d_mask_, std::max<uint64_t>(E_ / 32, 1) * 4);
+  reg(d_lrtb_, 6ull * P_ * 8);
+  reg(d_lrtb_next_, 6ull * P_ * 8);
+  reg(d_parts_, (size_t)P_ * sizeof(DevPart));
+  reg(d_ss_, (size_t)S_ * sizeof(DevSimState));
+  reg(d_cnt_, sizeof(DevCounters));
+  reg(d_centroid_, 3ull * P_ * 8);
+  if (d_clamped_disp_) reg(d_clamped_disp_, 3 * n_clamped_ * 8);
+  if (precision_ == PD_FP32C) {
+    reg(d_disp32b_[0], C * sizeof(float4));
+    reg(d_disp32b_[1], C * sizeof(float4));
+    reg(d_anchor_, 3ull * P_ * 8);
+    reg(d_anchor_next_, 3ull * P_ * 8);
+    reg(d_wall_local_, 6ull * P_ * 4);
+    reg(d_lrtb_local_, 6ull * P_ * 4);
+    reg(d_extra_flag_, C);
+    reg(d_f_extra_, 3 * C * 8);
+  }
+  reg(bp_.cand, (size_t)C * bp_.cand_cap * 4);
+  reg(bp_.cand_n, (size_t)C * 2);
+  size_t total = 0;
+  for (auto &m : mutable_) total += (m.second + 255) & ~(size_t)255;
+  if (total > backup_bytes_) {
+    if (backup_) {
+      cudaFree(backup_);
+      allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), backup_), allocs_.end());
+      backup_ = nullptr;
+    }
+    char *b = nullptr;
+    PD_TRY(dalloc(this, allocs_, &b, total, err));
+    backup_ = b;
+    backup_bytes_ = total;
+  }
+  size_t off = 0;
+  for (auto &m : mutable_) {
+    PD_TRY(check(cudaMemcpyAsync((char *)backup_ + off, m.first, m.second, cudaMemcpyDeviceToDevice, stream_),
+                 "snapshot"));
+    off += (m.second + 255) & ~(size_t)255;
+  }
+  backup_cur_ = cur_;
+  backup_steps_ = steps_done_;
+  return check(cudaStreamSynchronize(stream_), "snapshot");
+}
+
+int Engine::restore() {
+  if (!backup_) {
+    err = "restore without a snapshot";
+    return PD_ESTATE;
+  }
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  size_t off = 0;
+  for (auto &m : mutable_) {
+    PD_TRY(check(cudaMemcpyAsync(m.first, (char *)backup_ + off, m.second, cudaMemcpyDeviceToDevice, stream_),
+                 "restore"));
+    off += (m.second + 255) & ~(size_t)255;
+  }
+  cur_ = backup_cur_;
+  steps_done_ = backup_steps_;
+  return check(cudaStreamSynchronize(stream_), "restore");
+}
+
+int Engine::set_variant(int variant) {
+  if (variant < 0 || variant >= num_bond_variants()) {
+    err = "bond kernel variant out of range";
+    return PD_EINVAL;
+  }
+  variant_ = variant;
+  graphs_ok_ = false;
+  return PD_OK;
+}
+
+int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms) {
+  const int nv = precision_ == PD_FP32C ? num_bond_variants() : 1;
+  if (steps_per_variant == 0) steps_per_variant = 8;
+  PD_TRY(snapshot());
+  int best = variant_;
+  double best_ms = 1e300;
+  for (int v = 0; v < nv; ++v) {
+    variant_ = v;
+    double ph[4] = {0, 0, 0, 0};
+    PD_TRY(profile(2, ph));  // first launches of a variant
+    double pm[4] = {0, 0, 0, 0};
+    PD_TRY(profile(steps_per_variant, pm));
+    const double ms = pm[2] / steps_per_variant;
+    if (variant_ms) variant_ms[v] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+    PD_TRY(restore());  // every variant starts from the same state
+  }
+  variant_ = best;
+  graphs_ok_ = false;
+  if (chosen) *chosen = best;
+  return PD_OK;
 }
 
 }  // namespace pdg

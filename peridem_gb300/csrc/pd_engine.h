@@ -181,6 +181,12 @@ class Engine {
   // skin_frac <= 0, cand_cap == 0, tpb <= 0, stats < 0, use_graphs < 0 keep the setting
   int set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, int use_graphs);
   int clear_device_errors();
+  // Bond-kernel variant (FP32 form); autotune() times each on the live state and restores it.
+  int set_variant(int variant);
+  int autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms);
+  // Copy of every mutable device buffer (and the host step counters), and its restore.
+  int snapshot();
+  int restore();
   // Runs nsteps steps as separate launches with CUDA events between the phases and adds the
   // per-phase device time (ms) to phase_ms[0..3]: predictor, broad phase, fused step
   // kernel, end-of-step kernels.
@@ -221,6 +227,12 @@ class Engine {
   bool torque_possible_ = false;
   bool stats_ = false;
   bool use_graphs_ = true;
+  int variant_ = 0;
+  std::vector<std::pair<void *, size_t>> mutable_;  // device buffers that change while stepping
+  void *backup_ = nullptr;
+  size_t backup_bytes_ = 0;
+  int backup_cur_ = 0;
+  uint64_t backup_steps_ = 0;
   uint64_t steps_done_ = 0;
   uint64_t initial_bonds_ = 0;
   double half_skin_ = 0;
@@ -267,8 +279,9 @@ class Engine {
 
 // kernel launchers (pd_kernels.cu / pd_broadphase.cu)
 void launch_predict(const DevView &v, int tpb, cudaStream_t s);
-void launch_step_kernel(const DevView &v, int precision, int tpb, cudaStream_t s);
-void launch_step_fp32c(const DevView &v, cudaStream_t s);
+void launch_step_kernel(const DevView &v, int precision, int variant, cudaStream_t s);
+void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s);
+int num_bond_variants();
 void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
                      cudaStream_t s);
 void launch_centroids(const DevView &v, cudaStream_t s);

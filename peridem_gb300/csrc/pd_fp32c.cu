@@ -195,9 +195,9 @@ __device__ __forceinline__ float bond32(const float4 &pi, const float4 &ui, cons
   return str;
 }
 
-constexpr int kUnroll = 4;
-
-__global__ void __launch_bounds__(128) k_bond32(DevView v) {
+// U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register cap).
+template <int U, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
   const uint64_t nn = valid ? n : 0;
@@ -222,21 +222,21 @@ __global__ void __launch_bounds__(128) k_bond32(DevView v) {
     const float4 *__restrict__ p32 = v.pos32;
     const float4 *__restrict__ d32 = v.disp32;
     int j = 0;
-    for (; j + kUnroll <= dg; j += kUnroll) {
-      uint32_t q[kUnroll], m[kUnroll];
+    for (; j + U <= dg; j += U) {
+      uint32_t q[U], m[U];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
+      for (int u = 0; u < U; ++u) {
         q[u] = __ldg(colp + 32 * (j + u));
         m[u] = maskp[j + u];
       }
-      float4 pq[kUnroll], uq[kUnroll];
+      float4 pq[U], uq[U];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
+      for (int u = 0; u < U; ++u) {
         pq[u] = __ldg(p32 + q[u]);
         uq[u] = __ldg(d32 + q[u]);
       }
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
+      for (int u = 0; u < U; ++u) {
         if ((m[u] >> lane) & 1u) {
           ++live;
           const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
@@ -345,11 +345,25 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
   if (v.P) k_anchor_next<<<(v.P + 127) / 128, 128, 0, s>>>(v);
 }
 
-void launch_step_fp32c(const DevView &v, cudaStream_t s) {
+// Bond-kernel variants the autotuner chooses from: {positions per load group, min blocks/SM}.
+const int kBondVariants[][2] = {{4, 1}, {2, 8}, {4, 6}, {8, 1}, {8, 4}, {1, 8}};
+const int kNumBondVariants = 6;
+
+int num_bond_variants() { return kNumBondVariants; }
+
+void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   k_extra32<<<(unsigned)blocks, 128, 0, s>>>(v);
-  k_bond32<<<(unsigned)blocks, 128, 0, s>>>(v);
+  const unsigned b = (unsigned)blocks;
+  switch (variant) {
+    case 1: k_bond32<2, 8><<<b, 128, 0, s>>>(v); break;
+    case 2: k_bond32<4, 6><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<8, 1><<<b, 128, 0, s>>>(v); break;
+    case 4: k_bond32<8, 4><<<b, 128, 0, s>>>(v); break;
+    case 5: k_bond32<1, 8><<<b, 128, 0, s>>>(v); break;
+    default: k_bond32<4, 1><<<b, 128, 0, s>>>(v); break;
+  }
 }
 
 }  // namespace pdg

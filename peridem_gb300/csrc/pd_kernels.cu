@@ -281,12 +281,11 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
   }
 }
 
-void launch_step_kernel(const DevView &v, int precision, int tpb, cudaStream_t s) {
+void launch_step_kernel(const DevView &v, int precision, int variant, cudaStream_t s) {
   uint64_t blocks = (v.N + 127) / 128;
-  (void)tpb;
   if (!blocks) return;
   if (precision == PD_FP32C)
-    launch_step_fp32c(v, s);
+    launch_step_fp32c(v, variant, s);
   else
     k_step<<<(unsigned)blocks, 128, 0, s>>>(v);
 }

@@ -124,6 +124,24 @@ class Sim:
         self._ck(lib().pd_profile_steps(self.h, int(nsteps), ptr(out)))
         return out
 
+    def autotune(self, steps_per_variant: int = 8) -> tuple[int, np.ndarray]:
+        """Times every bond-kernel variant on the live state (restored afterwards); keeps the
+        fastest. Returns (chosen, ms per step of each variant)."""
+        nv = lib().pd_num_variants()
+        ms = np.zeros(nv)
+        ch = C.c_int()
+        self._ck(lib().pd_autotune(self.h, int(steps_per_variant), C.byref(ch), ptr(ms)))
+        return ch.value, ms
+
+    def set_variant(self, v: int):
+        self._ck(lib().pd_set_variant(self.h, int(v)))
+
+    def snapshot(self):
+        self._ck(lib().pd_snapshot(self.h))
+
+    def restore(self):
+        self._ck(lib().pd_restore(self.h))
+
     def live_bonds(self) -> int:
         n = C.c_uint64()
         self._ck(lib().pd_count_live_bonds(self.h, C.byref(n)))

@@ -109,3 +109,41 @@ def test_fp32c_within_tolerance(name):
         cb = {tuple(r) for r in orc.connectivity(p)}
         mism += len(ca ^ cb)
     assert mism <= 1e-3 * max(1, n_or), f"{name}: {mism} bond mismatches of {n_or}"
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_snapshot_restore_replays_identically(precision):
+    s, cfg = cases.impact_free()
+    sim = Sim(s, cfg, precision)
+    sim.step(10)
+    sim.snapshot()
+    sim.step(15)
+    a = sim.state()
+    ca = [sim.connectivity(p) for p in range(s.n_particles)]
+    sim.restore()
+    sim.step(15)
+    b = sim.state()
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+    for p in range(s.n_particles):
+        np.testing.assert_array_equal(ca[p], sim.connectivity(p))
+
+
+def test_autotune_is_result_neutral():
+    s, cfg = cases.cubes_gravity()
+    a = Sim(s, cfg, "fp32c")
+    b = Sim(s, cfg, "fp32c")
+    a.step(5)
+    b.step(5)
+    chosen, ms = a.autotune(4)
+    assert 0 <= chosen < len(ms) and np.all(ms > 0)
+    a.step(20)
+    b.step(20)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k])
+    for v in range(len(ms)):
+        c = Sim(s, cfg, "fp32c")
+        c.set_variant(v)
+        c.step(25)
+        np.testing.assert_array_equal(c.state()["curpos"], sa["curpos"])
