@@ -213,6 +213,107 @@ def cpu_sample_rate(s, cfg, threads: int, steps: int, warmup: int, budget_s: flo
     return bonds / dt, done, sub
 
 
+def compare_forms(a, b, setup, conn_a, conn_b):
+    """FP32-compensated state `a` against FP64 state `b` after the same steps."""
+    dref = max(np.abs(b["disp"]).max(), 1e-300)
+    err = float(np.abs(a["disp"] - b["disp"]).max() / dref)
+    mism = 0
+    nb = 0
+    for ca, cb in zip(conn_a, conn_b):
+        nb += len(cb)
+        if len(ca) != len(cb) or not np.array_equal(ca, cb):
+            mism += len({tuple(x) for x in ca} ^ {tuple(x) for x in cb})
+    rho = np.repeat(setup.rho, np.diff(setup.node_offset).astype(np.int64))
+    ke_a = 0.5 * float(np.sum(rho * setup.vol * (a["vel"] ** 2).sum(1)))
+    ke_b = 0.5 * float(np.sum(rho * setup.vol * (b["vel"] ** 2).sum(1)))
+    return {"max_rel_disp_err": err, "broken_bond_mismatch": mism / max(1, nb), "bond_mismatches": mism,
+            "live_pairs_fp64": nb, "kinetic_energy_fp64": ke_b,
+            "kinetic_energy_rel_diff": abs(ke_a - ke_b) / max(abs(ke_b), 1e-300)}
+
+
+def accuracy_run(name: str, nsteps: int, **over):
+    """Both forms of the same workload for `steps` steps; the FP64 form is bit-exact with the
+    CPU oracle (tests/test_gpu_parity.py), so it stands for the oracle here."""
+    from peridem_gb300 import gen
+    from peridem_gb300.sim import Sim
+    s, cfg = gen.WORKLOADS[name](**over)
+    a = Sim(s, cfg, "fp32c")
+    b = Sim(s, cfg, "fp64")
+    t0 = time.perf_counter()
+    a.step(nsteps)
+    t1 = time.perf_counter()
+    b.step(nsteps)
+    t2 = time.perf_counter()
+    n0 = s.n_bonds_directed // 2
+    ca = [a.connectivity(p) for p in range(s.n_particles)]
+    cb = [b.connectivity(p) for p in range(s.n_particles)]
+    out = compare_forms(a.state(), b.state(), s, ca, cb)
+    out.update(workload=name, steps=nsteps, nodes=s.n_nodes, initial_pairs=n0,
+               broken_pairs_fp64=n0 - out["live_pairs_fp64"], wall_s_fp32c=t1 - t0, wall_s_fp64=t2 - t1)
+    a.close()
+    b.close()
+    return out
+
+
+def serving_run(args):
+    """Config 4: the Poisson request stream served with continuous batching in the FP32-
+    compensated form, beside a one-at-a-time plain FP64 queue modelled from measured service
+    times of a sample of the same requests."""
+    import multiprocessing as mp
+
+    from peridem_gb300 import gen, serve
+    from peridem_gb300.sim import Sim
+    specs = gen.serving_stream(n=args.serve)
+    t0 = time.perf_counter()
+    nproc = max(1, min(16, (os.cpu_count() or 1)))
+    with mp.get_context("spawn").Pool(nproc) as pool:  # setups are the client's input files
+        built = pool.map(gen.build_aggregate, [sp["gen"] for sp in specs], chunksize=1)
+    t_gen = time.perf_counter() - t0
+    reqs = [serve.Request(sp["rid"], s, cfg, sp["gen"]["steps"], sp["arrival"])
+            for sp, (s, cfg) in zip(specs, built)]
+    srv = serve.Server("fp32c", chunk_steps=args.serve_chunk, max_batch=args.serve_max_batch, keep_state=False)
+    t0 = time.perf_counter()
+    res = srv.run(reqs)
+    wall = time.perf_counter() - t0
+    summ = serve.summarize(res, wall)
+    cohorts = [e for e in srv.log if e[1] == "admit"]
+    summ.update(cohorts=len(cohorts), max_cohort=max((len(e[2]) for e in cohorts), default=0),
+                peak_device_gb=srv.peak_used / 1e9, setup_gen_s=t_gen, chunk_steps=args.serve_chunk,
+                nodes_mean=float(np.mean([len(r.setup.pos) for r in reqs])),
+                steps_mean=float(np.mean([r.steps for r in reqs])))
+    # one at a time, plain FP64: measured per-step time and creation time on a sample spread
+    # over the sizes, fitted as linear in directed bonds, then a FIFO queue over the arrivals
+    order = np.argsort([2 * len(r.setup.conn) for r in reqs])
+    pick = sorted({int(order[int(q)]) for q in np.linspace(0, len(reqs) - 1, args.serve_fp64_sample)})
+    xs, per_step, create = [], [], []
+    for i in pick:
+        r = reqs[i]
+        tc = time.perf_counter()
+        sm = Sim(r.setup, dict(r.config, timesteps=r.steps), "fp64")
+        create.append(time.perf_counter() - tc)
+        sm.step(5)
+        tt = time.perf_counter()
+        sm.step(args.serve_fp64_steps)
+        per_step.append((time.perf_counter() - tt) / args.serve_fp64_steps)
+        xs.append(2 * len(r.setup.conn))
+        sm.close()
+    A = np.vstack([np.asarray(xs, float), np.ones(len(xs))]).T
+    coef, *_ = np.linalg.lstsq(A, np.asarray(per_step), rcond=None)
+    cf, *_ = np.linalg.lstsq(A, np.asarray(create), rcond=None)
+    svc = np.array([max(0.0, coef[0] * 2 * len(r.setup.conn) + coef[1]) * r.steps +
+                    max(0.0, cf[0] * 2 * len(r.setup.conn) + cf[1]) for r in reqs])
+    arr = np.array([r.arrival for r in reqs])
+    ttc64 = serve.sequential_ttc(arr, svc)
+    span = float(max(arr + ttc64))
+    bu = sum(r.bonds * r.steps for r in res if r.error is None)
+    summ["one_at_a_time_fp64"] = {
+        "ttc_p50_s": float(np.percentile(ttc64, 50)), "ttc_p99_s": float(np.percentile(ttc64, 99)),
+        "sims_per_hour": len(reqs) / span * 3600.0, "bond_updates_per_s": bu / span,
+        "modelled_from": f"{len(pick)} requests measured ({args.serve_fp64_steps} steps each, "
+                         "per-step and creation time linear in directed bonds)"}
+    return summ
+
+
 def reference_arm(args):
     r, w, _ = rank_info()
     if r != 0:
@@ -278,32 +379,15 @@ def ours(args):
         fp64 = {"value": v64, "unit": UNIT, "steps": K64, "ms_per_step": ms64 / K64,
                 "kernel_ms": ph64[2], "roofline_hbm_frac": ach64 / peak,
                 "note": "bound by FP64 issue rate (sqrt/div per bond), not HBM"}
-        # accuracy of FP32C vs FP64 after the same number of steps
+        # accuracy of FP32C vs FP64 after the same number of steps on this workload
         done64 = W + K64 + 3
         if steps32 > done64:
             sim64.step(steps32 - done64)
         elif done64 > steps32:
             sim.step(done64 - steps32)
-        a, b = sim.state(), sim64.state()
-        dref = max(np.abs(b["disp"]).max(), 1e-300)
-        err = float(np.abs(a["disp"] - b["disp"]).max() / dref)
-        mism = 0
-        nb = 0
-        for p in range(s.n_particles):
-            ca = sim.connectivity(p)
-            cb = sim64.connectivity(p)
-            nb += len(cb)
-            if len(ca) != len(cb) or not np.array_equal(ca, cb):
-                sa = {tuple(x) for x in ca}
-                sb = {tuple(x) for x in cb}
-                mism += len(sa ^ sb)
-        vol = s.vol
-        rho = np.repeat(s.rho, np.diff(s.node_offset).astype(np.int64))
-        ke_a = 0.5 * float(np.sum(rho * vol * (a["vel"] ** 2).sum(1)))
-        ke_b = 0.5 * float(np.sum(rho * vol * (b["vel"] ** 2).sum(1)))
-        acc = {"steps": max(steps32, done64), "max_rel_disp_err": err,
-               "broken_bond_mismatch": mism / max(1, nb),
-               "kinetic_energy_rel_diff": abs(ke_a - ke_b) / max(abs(ke_b), 1e-300)}
+        acc = compare_forms(sim.state(), sim64.state(), s, [sim.connectivity(p) for p in range(s.n_particles)],
+                            [sim64.connectivity(p) for p in range(s.n_particles)])
+        acc["steps"] = max(steps32, done64)
         sim64.close()
 
     # ---- end to end through the C-ABI: host arrays in, K steps, state back to host
@@ -333,6 +417,17 @@ def ours(args):
                "sample": f"first {sub.n_particles} particles of {args.workload} ({sub.n_nodes} nodes, "
                          f"{sub.n_bonds_directed} bonds), {done} steps, OpenMP round-robin like the MPI ranks"}
 
+    # ---- accuracy on dynamic workloads (impact, settling), both forms on the GPU
+    acc_dyn = []
+    if not args.no_accuracy:
+        acc_dyn.append(accuracy_run("two_sphere", args.acc_steps_c0))
+        acc_dyn.append(accuracy_run("cubes125", args.acc_steps_c1, steps=args.acc_steps_c1))
+
+    # ---- serving stream (continuous batching), rank 0 at N=1 only
+    serving = None
+    if r == 0 and world == 1 and args.serve > 0:
+        serving = serving_run(args)
+
     launches_per_step = 13  # predict, decide, 7 broad-phase (early exit unless due), extra32, bond32, 2 end
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -349,6 +444,7 @@ def ours(args):
                      "autotune_ms_per_variant": [round(float(x), 4) for x in variant_ms],
                      "phase_ms": {"predict": ph[0], "broadphase": ph[1], "step": ph[2], "end": ph[3]}},
         "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64, "accuracy_vs_fp64": acc,
+        "accuracy_dynamic": acc_dyn, "serving": serving,
         "gpu_launches": launches_per_step * K, "clocks": clocks,
     }
     sim.close()
@@ -371,6 +467,14 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--acc-steps-c0", type=int, default=2000)
+    ap.add_argument("--acc-steps-c1", type=int, default=4000)
+    ap.add_argument("--serve", type=int, default=256, help="requests of the serving stream (0: skip)")
+    ap.add_argument("--serve-chunk", type=int, default=500)
+    ap.add_argument("--serve-max-batch", type=int, default=32)
+    ap.add_argument("--serve-fp64-sample", type=int, default=6)
+    ap.add_argument("--serve-fp64-steps", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -162,7 +162,8 @@ int pd_run(pd_sim *sim);
 /* Enqueues `nsteps` explicit steps (timeloop.h:395-797) on the handle's stream. */
 int pd_step(pd_sim *sim, uint32_t nsteps);
 /* Bounded wait for the handle's stream; PD_ETIMEOUT when timeout_ms passes first,
- * PD_EDEVICE when the device error word is set. timeout_ms < 0 waits without limit. */
+ * PD_EDEVICE when the device error word is set. timeout_ms < 0 waits without limit;
+ * timeout_ms == 0 only polls (PD_ETIMEOUT while work is still queued). */
 int pd_sync(pd_sim *sim, int timeout_ms);
 /* Uses an external CUDA stream (cudaStream_t passed as void*; NULL = handle's own). */
 int pd_set_stream(pd_sim *sim, void *cuda_stream);
@@ -243,6 +244,38 @@ int pd_count_live_bonds(pd_sim *sim, uint64_t *live);
  * before any stream capture, with the simulation's device current. This entry point has no
  * counterpart in the reference. */
 int pd_count_live_bonds_noalloc(pd_sim *sim, uint64_t *live);
+
+/* ---- batches of independent simulations (serving) -------------------------------------
+ * The reference runs one simulation per process (run/simulate3d.cpp:37-176); these entry
+ * points have no counterpart there. A batch handle holds n_sims simulations, each with its
+ * own setup and main.conf values, concatenated in one device layout: every phase of a step
+ * is one launch over all of them and nothing couples two of them, so each computes exactly
+ * what it computes in a handle of its own. pd_step advances every simulation that is not
+ * finished. Simulation i's nodes are [node0, node0+n_nodes) of the handle's node order and
+ * its particles [particle0, particle0+n_particles) (pd_get_connectivity takes handle
+ * particle indices). Errors of these calls are reported by pd_global_error(). */
+int pd_create_batch(const pd_setup_arrays *setups, const pd_config *cfgs, uint32_t n_sims,
+                    int precision, pd_sim **out);
+/* Device bytes pd_create_batch would allocate for these setups (no device work). */
+int pd_estimate_bytes(const pd_setup_arrays *setups, uint32_t n_sims, int precision,
+                      uint64_t *bytes);
+/* Device bytes a handle holds; free and total memory of the current device. */
+int pd_device_bytes(const pd_sim *sim, uint64_t *bytes);
+int pd_device_memory(uint64_t *free_bytes, uint64_t *total_bytes);
+int pd_num_sims(const pd_sim *sim, uint32_t *n_sims);
+int pd_sim_range(const pd_sim *sim, uint32_t i, uint64_t *node0, uint64_t *n_nodes,
+                 uint32_t *particle0, uint32_t *n_particles);
+/* Steps simulation i has taken. */
+int pd_sim_steps(const pd_sim *sim, uint32_t i, uint64_t *steps);
+/* Ends simulation i at the current step boundary: waits for the handle's stream, reads its
+ * state and walls back into host memory (kept by the handle) and stops stepping it. Later
+ * reads of simulation i return that state. */
+int pd_finish_sim(pd_sim *sim, uint32_t i);
+/* State of simulation i alone (N_i*3 arrays in its own node order; pointers may be NULL). */
+int pd_get_sim_state(pd_sim *sim, uint32_t i, double *curpos, double *vel, double *acc,
+                     double *force);
+int pd_get_sim_disp(pd_sim *sim, uint32_t i, double *disp);
+int pd_get_sim_wall(pd_sim *sim, uint32_t i, double *wall_info, double *reaction);
 
 #ifdef __cplusplus
 }

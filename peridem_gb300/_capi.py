@@ -129,6 +129,17 @@ SIGNATURES = [
     ("pd_h5_info", C.c_int, [_P, C.c_char_p, C.POINTER(C.c_int), C.POINTER(_u64)]),
     ("pd_h5_read", C.c_int, [_P, C.c_char_p, C.c_int, _P, _u64]),
     ("pd_h5_close", None, [_P]),
+    ("pd_create_batch", C.c_int, [C.POINTER(PdSetupArrays), C.POINTER(PdConfig), _u32, C.c_int, C.POINTER(_P)]),
+    ("pd_estimate_bytes", C.c_int, [C.POINTER(PdSetupArrays), _u32, C.c_int, C.POINTER(_u64)]),
+    ("pd_device_bytes", C.c_int, [_P, C.POINTER(_u64)]),
+    ("pd_device_memory", C.c_int, [C.POINTER(_u64), C.POINTER(_u64)]),
+    ("pd_num_sims", C.c_int, [_P, C.POINTER(_u32)]),
+    ("pd_sim_range", C.c_int, [_P, _u32, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u32), C.POINTER(_u32)]),
+    ("pd_sim_steps", C.c_int, [_P, _u32, C.POINTER(_u64)]),
+    ("pd_finish_sim", C.c_int, [_P, _u32]),
+    ("pd_get_sim_state", C.c_int, [_P, _u32, _P, _P, _P, _P]),
+    ("pd_get_sim_disp", C.c_int, [_P, _u32, _P]),
+    ("pd_get_sim_wall", C.c_int, [_P, _u32, _P, _P]),
 ]
 
 _lib = None

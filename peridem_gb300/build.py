@@ -30,6 +30,7 @@ UNITS = [
     ("pd_noalloc.cu", []),
     ("pd_engine.cu", ["-fmad=false"]),
     ("pd_capi.cpp", []),
+    ("pd_batch.cpp", []),
     ("pd_config.cpp", []),
     ("pd_files.cpp", []),
     ("h5lite.cpp", []),

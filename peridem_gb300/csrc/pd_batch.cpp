@@ -1,0 +1,276 @@
+// pd_batch.cpp -- batches of independent simulations in one engine, and the extern "C"
+// entry points a serving loop uses on them.
+//
+// A batch concatenates the nodes, particles and bonds of S simulations in the layout of
+// pd_engine.h; every phase of a step is one launch over all of them, and the per-node work
+// looks up its simulation's constants (DevSimParams) and state (DevSimState). Nothing in a
+// step couples two simulations: bonds stay inside a particle, contact candidates come from
+// cells hashed with the simulation index, walls are per simulation. A simulation of a batch
+// therefore computes exactly what it computes alone.
+//
+// Simulations of a batch may need different step counts. The host stops one with
+// finish_sim() at a step boundary: its state is read back and kept on the host, and its
+// `active` flag is cleared so the kernels skip its nodes from then on. The reference runs one
+// simulation per process (run/simulate3d.cpp); none of this has a counterpart there.
+#include <algorithm>
+#include <cstddef>
+#include <cstring>
+
+#include "pd_engine.h"
+#include "pd_sim.h"
+
+#define PD_TRY(expr)              \
+  do {                            \
+    int _rc = (expr);             \
+    if (_rc != PD_OK) return _rc; \
+  } while (0)
+
+namespace pdg {
+
+namespace {
+inline uint64_t up32(uint64_t x) { return (x + 31) / 32 * 32; }
+inline uint64_t atleast1(uint64_t x) { return x ? x : 1; }
+}  // namespace
+
+// Mirrors every allocation of Engine::init (alloc_and_upload, build_bonds,
+// alloc_candidates) for the same setups, without touching the device.
+uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap) {
+  uint64_t N = 0, P = 0, S = sims.size(), ncl = 0;
+  for (auto &s : sims) {
+    N += s.node_offset[s.np];
+    P += s.np;
+    ncl += s.clamped.size();
+  }
+  const uint64_t C = up32(N), nsl = C / 32;
+  std::vector<uint32_t> deg(C, 0);
+  uint64_t g = 0;
+  for (auto &s : sims) {
+    for (uint32_t p = 0; p < s.np; ++p) {
+      const uint64_t g0 = g + s.node_offset[p];
+      const uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
+      for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
+        const uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
+        if (i < nloc && j < nloc) {
+          deg[g0 + i]++;
+          deg[g0 + j]++;
+        }
+      }
+    }
+    g += s.node_offset[s.np];
+  }
+  uint64_t E = 0;
+  for (uint64_t sl = 0; sl < nsl; ++sl) {
+    uint32_t w = 0;
+    for (int l = 0; l < 32; ++l) w = std::max(w, deg[sl * 32 + l]);
+    E += 32ull * w;
+  }
+  uint64_t b = 0;
+  // bonds
+  b += (nsl + 1) * 8 + C * 2 + atleast1(E) * 4 + atleast1(E / 32) * 4;
+  // node state, particles, simulations
+  b += 7 * 3 * C * 8 + C * 8 + C * 4 + C;
+  b += P * sizeof(DevPart) + 6 * P * 8 * 2 + 3 * P * 8;
+  b += S * sizeof(DevSimParams) + S * sizeof(DevSimState) + sizeof(DevCounters);
+  if (ncl) b += (P + 1 + ncl) * 4 + 3 * ncl * 8;
+  if (precision == PD_FP64) {
+    b += 3 * atleast1(E) * 8 + 2 * atleast1(E) * 8;
+  } else {
+    b += 3 * C * 16 + 3 * C * 8 + 2 * 3 * P * 8 + C + 3 * C * 8 + C + 2 * 6 * P * 4;
+  }
+  // broad phase
+  uint32_t bits = 10;
+  while ((1ull << bits) < 2 * N) ++bits;
+  const uint64_t T = 1ull << bits;
+  b += 2 * T * 4 + 3 * C * 4 + ((T + 4095) / 4096 + 1) * 4;
+  b += C * (cand_cap ? cand_cap : 32) * 4 + C * 2;
+  return b;
+}
+
+int Engine::sim_range(uint32_t sim, uint64_t *node0, uint64_t *n_nodes, uint32_t *particle0,
+                      uint32_t *n_particles) const {
+  if (sim >= S_) return PD_EINVAL;
+  if (node0) *node0 = sim_node0_[sim];
+  if (n_nodes) *n_nodes = sim_node0_[sim + 1] - sim_node0_[sim];
+  if (particle0) *particle0 = sim_p0_[sim];
+  if (n_particles) *n_particles = sim_p0_[sim + 1] - sim_p0_[sim];
+  return PD_OK;
+}
+
+// [3][Ncap] device array, nodes [node0, node0+nn) -> nn*3 row vectors.
+int Engine::read_nodes(const double *d, uint64_t node0, uint64_t nn, double *dst) {
+  std::vector<double> buf(3 * nn);
+  for (int c = 0; c < 3; ++c)
+    PD_TRY(check(cudaMemcpyAsync(buf.data() + c * nn, d + c * Ncap_ + node0, nn * 8, cudaMemcpyDeviceToHost, stream_),
+                 "read state"));
+  PD_TRY(check(cudaStreamSynchronize(stream_), "read state"));
+  for (uint64_t k = 0; k < nn; ++k)
+    for (int c = 0; c < 3; ++c) dst[3 * k + c] = buf[c * nn + k];
+  return PD_OK;
+}
+
+int Engine::get_sim_state(uint32_t sim, double *curpos, double *vel, double *acc, double *force, double *disp) {
+  if (sim >= S_) {
+    err = "simulation index out of range";
+    return PD_EINVAL;
+  }
+  const uint64_t n0 = sim_node0_[sim], nn = sim_node0_[sim + 1] - n0;
+  double *outs[5] = {curpos, vel, acc, force, disp};
+  if (finished_[sim]) {
+    for (int k = 0; k < 5; ++k)
+      if (outs[k]) std::memcpy(outs[k], final_[sim].data() + k * 3 * nn, 3 * nn * 8);
+    return PD_OK;
+  }
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const bool fused = precision_ == PD_FP32C;
+  // clamped nodes of this simulation (h_clamped_ lists them particle by particle)
+  std::vector<uint64_t> cl;
+  for (uint64_t i = 0; i < h_clamped_.size(); ++i)
+    if (h_clamped_[i] >= n0 && h_clamped_[i] < n0 + nn) cl.push_back(i);
+  if (curpos || disp) {
+    std::vector<double> dsp(3 * nn);
+    PD_TRY(read_nodes(fused ? d_dispb_[cur_ ^ 1] : d_disp_, n0, nn, dsp.data()));
+    if (disp) {
+      std::memcpy(disp, dsp.data(), 3 * nn * 8);
+      if (fused && sim_steps_[sim] > 0)  // clamped nodes end each step at zero (timeloop.h:767-774)
+        for (uint64_t i : cl)
+          for (int c = 0; c < 3; ++c) disp[3 * (h_clamped_[i] - n0) + c] = 0.0;
+    }
+    if (curpos) {
+      if (!cl.empty() && sim_steps_[sim] > 0 && !fused) {
+        // CurrPos of clamped nodes keeps the predicted displacement (zeroed afterwards)
+        std::vector<double> cd(3 * n_clamped_);
+        PD_TRY(cpy(cd.data(), d_clamped_disp_, cd.size() * 8, "read clamped"));
+        for (uint64_t i : cl)
+          for (int c = 0; c < 3; ++c) dsp[3 * (h_clamped_[i] - n0) + c] = cd[3 * i + c];
+      }
+      const HostSim &s = sims_[sim];
+      for (uint64_t k = 0; k < 3 * nn; ++k) curpos[k] = s.pos[k] + dsp[k];
+    }
+  }
+  if (vel) PD_TRY(read_nodes(d_vel_[cur_], n0, nn, vel));
+  if (acc) PD_TRY(read_nodes(d_acc_, n0, nn, acc));
+  if (force) PD_TRY(read_nodes(d_force_, n0, nn, force));
+  return PD_OK;
+}
+
+int Engine::finish_sim(uint32_t sim) {
+  if (sim >= S_) {
+    err = "simulation index out of range";
+    return PD_EINVAL;
+  }
+  if (finished_[sim]) return PD_OK;
+  const uint64_t nn = sim_node0_[sim + 1] - sim_node0_[sim];
+  std::vector<double> keep(15 * nn + 24);
+  PD_TRY(get_sim_state(sim, keep.data(), keep.data() + 3 * nn, keep.data() + 6 * nn, keep.data() + 9 * nn,
+                       keep.data() + 12 * nn));
+  PD_TRY(get_wall(sim, keep.data() + 15 * nn, keep.data() + 15 * nn + 6));
+  const int32_t off = 0;
+  PD_TRY(cpy((char *)(d_ss_ + sim) + offsetof(DevSimState, active), &off, sizeof(off), "deactivate"));
+  final_[sim].swap(keep);
+  finished_[sim] = 1;
+  return PD_OK;
+}
+
+}  // namespace pdg
+
+namespace {
+int fail(int rc, const std::string &m) { return pdg::set_global_error(rc, m); }
+}  // namespace
+
+extern "C" {
+
+int pd_create_batch(const pd_setup_arrays *setups, const pd_config *cfgs, uint32_t n_sims, int precision,
+                    pd_sim **out) {
+  if (!out) return fail(PD_EINVAL, "null output handle");
+  *out = nullptr;
+  if (!setups || !cfgs || n_sims == 0) return fail(PD_EINVAL, "empty batch");
+  if (precision != PD_FP64 && precision != PD_FP32C) return fail(PD_EINVAL, "unknown precision form");
+  std::vector<pdg::HostSim> sims(n_sims);
+  for (uint32_t i = 0; i < n_sims; ++i) {
+    std::string err;
+    int rc = pdg::host_sim_from_arrays(&setups[i], &cfgs[i], sims[i], err);
+    if (rc != PD_OK) return fail(rc, "simulation " + std::to_string(i) + ": " + err);
+  }
+  pd_sim *s = new pd_sim();
+  s->cfg = cfgs[0];
+  int rc = s->eng.init(sims, precision);
+  if (rc != PD_OK) {
+    std::string e = s->eng.err;
+    delete s;
+    return fail(rc, e);
+  }
+  *out = s;
+  return PD_OK;
+}
+
+int pd_estimate_bytes(const pd_setup_arrays *setups, uint32_t n_sims, int precision, uint64_t *bytes) {
+  if (!setups || !bytes || n_sims == 0) return fail(PD_EINVAL, "null argument");
+  std::vector<pdg::HostSim> sims(n_sims);
+  pd_config cfg;
+  pd_config_default(&cfg);
+  for (uint32_t i = 0; i < n_sims; ++i) {
+    std::string err;
+    int rc = pdg::host_sim_from_arrays(&setups[i], &cfg, sims[i], err);
+    if (rc != PD_OK) return fail(rc, "simulation " + std::to_string(i) + ": " + err);
+  }
+  *bytes = pdg::Engine::estimate_bytes(sims, precision, 0);
+  return PD_OK;
+}
+
+int pd_device_bytes(const pd_sim *s, uint64_t *bytes) {
+  if (!s || !bytes) return fail(PD_EINVAL, "null argument");
+  *bytes = s->eng.device_bytes();
+  return PD_OK;
+}
+
+int pd_device_memory(uint64_t *free_bytes, uint64_t *total_bytes) {
+  size_t f = 0, t = 0;
+  cudaError_t e = cudaMemGetInfo(&f, &t);
+  if (e != cudaSuccess) return fail(PD_ECUDA, std::string("cudaMemGetInfo: ") + cudaGetErrorString(e));
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return PD_OK;
+}
+
+int pd_num_sims(const pd_sim *s, uint32_t *n) {
+  if (!s || !n) return fail(PD_EINVAL, "null argument");
+  *n = s->eng.num_sims();
+  return PD_OK;
+}
+
+int pd_sim_range(const pd_sim *s, uint32_t sim, uint64_t *node0, uint64_t *n_nodes, uint32_t *particle0,
+                 uint32_t *n_particles) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  int rc = s->eng.sim_range(sim, node0, n_nodes, particle0, n_particles);
+  return rc == PD_OK ? rc : fail(rc, "simulation index out of range");
+}
+
+int pd_sim_steps(const pd_sim *s, uint32_t sim, uint64_t *steps) {
+  if (!s || !steps) return fail(PD_EINVAL, "null argument");
+  if (sim >= s->eng.num_sims()) return fail(PD_EINVAL, "simulation index out of range");
+  *steps = s->eng.sim_steps(sim);
+  return PD_OK;
+}
+
+int pd_finish_sim(pd_sim *s, uint32_t sim) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  return s->eng.finish_sim(sim);
+}
+
+int pd_get_sim_state(pd_sim *s, uint32_t sim, double *curpos, double *vel, double *acc, double *force) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  return s->eng.get_sim_state(sim, curpos, vel, acc, force, nullptr);
+}
+
+int pd_get_sim_disp(pd_sim *s, uint32_t sim, double *disp) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  return s->eng.get_sim_state(sim, nullptr, nullptr, nullptr, nullptr, disp);
+}
+
+int pd_get_sim_wall(pd_sim *s, uint32_t sim, double *wall_info, double *reaction) {
+  if (!s) return fail(PD_EINVAL, "null handle");
+  if (sim >= s->eng.num_sims()) return fail(PD_EINVAL, "simulation index out of range");
+  return s->eng.get_wall(sim, wall_info, reaction);
+}
+
+}  // extern "C"

@@ -23,6 +23,7 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
 constexpr int kScanBlock = kScanThreads * kScanPer;
 constexpr int kMaxCand = 64;
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;  // node not in the cell list
 
 __device__ __forceinline__ uint32_t cell_hash(long long cx, long long cy, long long cz, uint32_t sim,
                                               uint32_t mask) {
@@ -72,6 +73,10 @@ __global__ void k_bp_count(DevView v, uint32_t *count, uint32_t *key, uint32_t *
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.N) return;
   const uint32_t sim = v.parts[v.pid[n]].sim;
+  if (!v.ss[sim].active) {  // finished simulations leave the cell list
+    key[n] = kNoKey;
+    return;
+  }
   long long cx, cy, cz;
   double x, y, z;
   node_cell(v, n, v.sp[sim].cell, cx, cy, cz, x, y, z);
@@ -147,7 +152,7 @@ __global__ void k_bp_scatter(DevView v, const uint32_t *start, const uint32_t *k
                              uint32_t *sorted) {
   if (!v.cnt->rebuild) return;
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N) return;
+  if (n >= v.N || key[n] == kNoKey) return;
   sorted[start[key[n]] + slot[n]] = (uint32_t)n;
 }
 
@@ -157,6 +162,10 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.N) return;
   const uint32_t sim = v.parts[v.pid[n]].sim;
+  if (!v.ss[sim].active) {
+    cand_n[n] = 0;
+    return;
+  }
   const DevSimParams &sp = v.sp[sim];
   long long cx, cy, cz;
   double x, y, z;

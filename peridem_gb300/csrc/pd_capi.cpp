@@ -16,6 +16,8 @@ int fail_global(int rc, const std::string &msg) {
 
 namespace pdg {
 
+int set_global_error(int rc, const std::string &msg) { return fail_global(rc, msg); }
+
 // Copies caller arrays into a HostSim (the particle vector the reference loads in
 // load_particles<3>, load_hdf5.h:41-113).
 int host_sim_from_arrays(const pd_setup_arrays *su, const pd_config *cfg, HostSim &hs, std::string &err) {

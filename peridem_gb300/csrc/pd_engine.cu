@@ -12,14 +12,24 @@
 
 namespace pdg {
 
+#define PD_TRY(expr)             \
+  do {                           \
+    int _rc = (expr);            \
+    if (_rc != PD_OK) return _rc; \
+  } while (0)
+
 namespace {
 inline uint64_t round_up(uint64_t x, uint64_t m) { return (x + m - 1) / m * m; }
 }  // namespace
 
+// Device memory comes from the stream-ordered allocator and goes back to it in stream order:
+// neither creating nor closing a handle waits for other handles' queued work, so a server
+// can admit and retire simulations while others keep the GPU busy.
 Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
   for (int i = 0; i < 2; ++i)
     if (graph_[i]) cudaGraphExecDestroy(graph_[i]);
-  for (void *p : allocs_) cudaFree(p);
+  for (void *p : allocs_) cudaFreeAsync(p, capture_stream_);
   if (own_stream_ && capture_stream_) cudaStreamDestroy(capture_stream_);
 }
 
@@ -29,23 +39,36 @@ int Engine::check(cudaError_t e, const char *what) {
   return e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA;
 }
 
-#define PD_TRY(expr)             \
-  do {                           \
-    int _rc = (expr);            \
-    if (_rc != PD_OK) return _rc; \
-  } while (0)
+int Engine::raw_alloc(void **p, size_t bytes) {
+  cudaError_t e = cudaMallocAsync(p, bytes, capture_stream_);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    err = std::string("device allocation of ") + std::to_string(bytes) + " B: " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA;
+  }
+  device_bytes_ += bytes;
+  return PD_OK;
+}
+
+int Engine::cpy(void *dst, const void *src, size_t bytes, const char *what) {
+  PD_TRY(check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream_), what));
+  return check(cudaStreamSynchronize(stream_), what);
+}
+
+int Engine::mset(void *dst, int value, size_t bytes, const char *what) {
+  return check(cudaMemsetAsync(dst, value, bytes, stream_), what);
+}
 
 template <typename T>
 static int dalloc(Engine *E, std::vector<void *> &allocs, T **p, uint64_t count, std::string &err) {
+  (void)err;
   *p = nullptr;
   if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    err = std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " B): " + cudaGetErrorString(e);
-    (void)E;
-    return e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA;
-  }
-  allocs.push_back((void *)*p);
+  void *q = nullptr;
+  PD_TRY(E->raw_alloc(&q, count * sizeof(T)));
+  *p = (T *)q;
+  allocs.push_back(q);
   return PD_OK;
 }
 
@@ -140,6 +163,15 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   }
   Ncap_ = round_up(N_, 32);
   nslices_ = Ncap_ / 32;
+  sim_node0_.assign(S_ + 1, 0);
+  sim_p0_.assign(S_ + 1, 0);
+  for (uint32_t i = 0; i < S_; ++i) {
+    sim_node0_[i + 1] = sim_node0_[i] + sims_[i].node_offset[sims_[i].np];
+    sim_p0_[i + 1] = sim_p0_[i] + sims_[i].np;
+  }
+  sim_steps_.assign(S_, 0);
+  finished_.assign(S_, 0);
+  final_.assign(S_, std::vector<double>());
   PD_TRY(check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate"));
   own_stream_ = true;
   capture_stream_ = stream_;
@@ -209,10 +241,10 @@ int Engine::build_bonds() {
   PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));
   PD_TRY(dalloc(this, allocs_, &d_col_, col.size(), err));
   PD_TRY(dalloc(this, allocs_, &d_mask_, mask.size(), err));
-  PD_TRY(check(cudaMemcpy(d_slice_ptr_, h_slice_ptr_.data(), (nslices_ + 1) * 8, cudaMemcpyHostToDevice), "upload slice_ptr"));
-  PD_TRY(check(cudaMemcpy(d_deg_, h_deg_.data(), Ncap_ * 2, cudaMemcpyHostToDevice), "upload deg"));
-  PD_TRY(check(cudaMemcpy(d_col_, col.data(), col.size() * 4, cudaMemcpyHostToDevice), "upload col"));
-  PD_TRY(check(cudaMemcpy(d_mask_, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice), "upload mask"));
+  PD_TRY(cpy(d_slice_ptr_, h_slice_ptr_.data(), (nslices_ + 1) * 8, "upload slice_ptr"));
+  PD_TRY(cpy(d_deg_, h_deg_.data(), Ncap_ * 2, "upload deg"));
+  PD_TRY(cpy(d_col_, col.data(), col.size() * 4, "upload col"));
+  PD_TRY(cpy(d_mask_, mask.data(), mask.size() * 4, "upload mask"));
   return PD_OK;
 }
 
@@ -382,13 +414,13 @@ int Engine::alloc_and_upload() {
   PD_TRY(dalloc(this, allocs_, &d_sp_, S_, err));
   PD_TRY(dalloc(this, allocs_, &d_ss_, S_, err));
   PD_TRY(dalloc(this, allocs_, &d_cnt_, 1, err));
-  auto up = [&](void *d, const void *h, size_t b, const char *w) { return check(cudaMemcpy(d, h, b, cudaMemcpyHostToDevice), w); };
+  auto up = [&](void *d, const void *h, size_t b, const char *w) { return cpy(d, h, b, w); };
   PD_TRY(up(d_pos_, pos.data(), 3 * C * 8, "upload pos"));
   PD_TRY(up(d_disp_, disp.data(), 3 * C * 8, "upload disp"));
   PD_TRY(up(d_vel_[0], vel.data(), 3 * C * 8, "upload vel"));
   PD_TRY(up(d_vel_[1], vel.data(), 3 * C * 8, "upload vel"));
   PD_TRY(up(d_acc_, acc.data(), 3 * C * 8, "upload acc"));
-  PD_TRY(check(cudaMemset(d_force_, 0, 3 * C * 8), "memset force"));
+  PD_TRY(mset(d_force_, 0, 3 * C * 8, "memset force"));
   PD_TRY(up(d_ext_, ext.data(), 3 * C * 8, "upload extforce"));
   PD_TRY(up(d_vol_, vol.data(), C * 8, "upload vol"));
   PD_TRY(up(d_pid_, h_pid_.data(), C * 4, "upload pid"));
@@ -396,7 +428,7 @@ int Engine::alloc_and_upload() {
   PD_TRY(up(d_parts_, parts.data(), P_ * sizeof(DevPart), "upload particles"));
   PD_TRY(up(d_sp_, sps.data(), S_ * sizeof(DevSimParams), "upload sim params"));
   PD_TRY(up(d_ss_, sss.data(), S_ * sizeof(DevSimState), "upload sim state"));
-  PD_TRY(check(cudaMemset(d_centroid_, 0, 3ull * P_ * 8), "memset centroid"));
+  PD_TRY(mset(d_centroid_, 0, 3ull * P_ * 8, "memset centroid"));
   DevCounters cnt;
   std::memset(&cnt, 0, sizeof(cnt));
   cnt.moved = 1e300;  // forces the first broad-phase build
@@ -432,7 +464,7 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_disp32_, C, err));
     d_disp32b_[0] = d_disp32_;
     PD_TRY(dalloc(this, allocs_, &d_disp32b_[1], C, err));
-    PD_TRY(check(cudaMemset(d_disp32b_[1], 0, C * sizeof(float4)), "memset disp32"));
+    PD_TRY(mset(d_disp32b_[1], 0, C * sizeof(float4), "memset disp32"));
     d_dispb_[0] = d_disp_;
     PD_TRY(dalloc(this, allocs_, &d_dispb_[1], 3 * C, err));
     PD_TRY(dalloc(this, allocs_, &d_anchor_, 3ull * P_, err));
@@ -447,14 +479,18 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_extra_flag_, C, err));
     PD_TRY(dalloc(this, allocs_, &d_wall_local_, 6ull * P_, err));
     PD_TRY(dalloc(this, allocs_, &d_lrtb_local_, 6ull * P_, err));
-    PD_TRY(check(cudaMemset(d_extra_flag_, 0, C), "memset extra flag"));
+    PD_TRY(mset(d_extra_flag_, 0, C, "memset extra flag"));
     PD_TRY(up(d_pos32_, p32.data(), C * sizeof(float4), "upload pos32"));
-    PD_TRY(check(cudaMemset(d_disp32_, 0, C * sizeof(float4)), "memset disp32"));
+    PD_TRY(mset(d_disp32_, 0, C * sizeof(float4), "memset disp32"));
   }
 
   // broad phase
   uint32_t bits = 10;
   while ((1ull << bits) < 2 * N_) ++bits;
+  if (bits > 31) {
+    err = "too many nodes for the broad-phase cell table";
+    return PD_EINVAL;
+  }
   bp_.table_bits = bits;
   const uint64_t T = 1ull << bits;
   if (bp_.cand_cap == 0) bp_.cand_cap = 32;
@@ -496,8 +532,9 @@ int Engine::prepare_fused(int cur) {
 
 int Engine::alloc_candidates() {
   if (bp_.cand) {
-    cudaFree(bp_.cand);
-    cudaFree(bp_.cand_n);
+    cudaFreeAsync(bp_.cand, stream_);
+    cudaFreeAsync(bp_.cand_n, stream_);
+    device_bytes_ -= cand_bytes_;
     allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)bp_.cand), allocs_.end());
     allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)bp_.cand_n), allocs_.end());
     bp_.cand = nullptr;
@@ -505,7 +542,8 @@ int Engine::alloc_candidates() {
   }
   PD_TRY(dalloc(this, allocs_, &bp_.cand, Ncap_ * bp_.cand_cap, err));
   PD_TRY(dalloc(this, allocs_, &bp_.cand_n, Ncap_, err));
-  PD_TRY(check(cudaMemset(bp_.cand_n, 0, Ncap_ * 2), "memset cand_n"));
+  cand_bytes_ = Ncap_ * bp_.cand_cap * 4 + Ncap_ * 2;
+  PD_TRY(mset(bp_.cand_n, 0, Ncap_ * 2, "memset cand_n"));
   return PD_OK;
 }
 
@@ -554,6 +592,8 @@ int Engine::step(uint32_t nsteps) {
     cur_ ^= 1;
     ++steps_done_;
   }
+  for (uint32_t i = 0; i < S_; ++i)
+    if (!finished_[i]) sim_steps_[i] += nsteps;
   return PD_OK;
 }
 
@@ -563,7 +603,11 @@ int Engine::sync(int timeout_ms) {
     cudaError_t e = cudaStreamQuery(stream_);
     if (e == cudaSuccess) break;
     if (e != cudaErrorNotReady) return check(e, "stream");
-    if (timeout_ms >= 0) {
+    if (timeout_ms == 0) {
+      err = "pd_sync: work still queued";
+      return PD_ETIMEOUT;
+    }
+    if (timeout_ms > 0) {
       auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
       if (ms > timeout_ms) {
         err = "pd_sync: timed out after " + std::to_string(timeout_ms) + " ms";
@@ -573,7 +617,7 @@ int Engine::sync(int timeout_ms) {
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
   DevCounters c;
-  PD_TRY(check(cudaMemcpy(&c, d_cnt_, sizeof(c), cudaMemcpyDeviceToHost), "read counters"));
+  PD_TRY(cpy(&c, d_cnt_, sizeof(c), "read counters"));
   if (c.err) {
     err = "device error word 0x" + std::to_string(c.err);
     if (c.err & PD_DERR_NONFINITE) err += " (non-finite force density)";
@@ -603,7 +647,7 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
       for (int c = 0; c < 3; ++c) dst[3 * n + c] = buf[c * C + n];
   };
   auto fetch = [&](const double *d, double *dst) -> int {
-    PD_TRY(check(cudaMemcpy(buf.data(), d, 3 * C * 8, cudaMemcpyDeviceToHost), "read state"));
+    PD_TRY(cpy(buf.data(), d, 3 * C * 8, "read state"));
     scatter(dst);
     return PD_OK;
   };
@@ -621,7 +665,7 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
       if (n_clamped_ && steps_done_ > 0 && !fused) {
         // CurrPos of clamped nodes keeps the predicted displacement (zeroed afterwards)
         std::vector<double> cd(3 * n_clamped_);
-        PD_TRY(check(cudaMemcpy(cd.data(), d_clamped_disp_, 3 * n_clamped_ * 8, cudaMemcpyDeviceToHost), "read clamped"));
+        PD_TRY(cpy(cd.data(), d_clamped_disp_, 3 * n_clamped_ * 8, "read clamped"));
         for (uint64_t i = 0; i < n_clamped_; ++i)
           for (int c = 0; c < 3; ++c) dsp[3 * (uint64_t)h_clamped_[i] + c] = cd[3 * i + c];
       }
@@ -647,7 +691,7 @@ int Engine::set_state(const double *disp, const double *vel, const double *acc) 
   auto put = [&](double *d, const double *src) -> int {
     for (uint64_t n = 0; n < N_; ++n)
       for (int c = 0; c < 3; ++c) buf[c * C + n] = src[3 * n + c];
-    return check(cudaMemcpy(d, buf.data(), 3 * C * 8, cudaMemcpyHostToDevice), "write state");
+    return cpy(d, buf.data(), 3 * C * 8, "write state");
   };
   const bool fused = precision_ == PD_FP32C;
   if (disp) PD_TRY(put(fused ? d_dispb_[cur_ ^ 1] : d_disp_, disp));
@@ -660,7 +704,7 @@ int Engine::set_state(const double *disp, const double *vel, const double *acc) 
     launch_init_lrtb(view(cur_), stream_);
   }
   double big = 1e300;
-  PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
+  PD_TRY(cpy(&d_cnt_->moved, &big, 8, "force rebuild"));
   return check(cudaStreamSynchronize(stream_), "set_state");
 }
 
@@ -689,8 +733,8 @@ int Engine::get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, u
   const uint64_t e0 = h_slice_ptr_[s0], e1 = h_slice_ptr_[std::min<uint64_t>(s1, nslices_)];
   std::vector<uint32_t> col(e1 - e0), mask((e1 - e0) / 32);
   if (e1 > e0) {
-    PD_TRY(check(cudaMemcpy(col.data(), d_col_ + e0, (e1 - e0) * 4, cudaMemcpyDeviceToHost), "read col"));
-    PD_TRY(check(cudaMemcpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, cudaMemcpyDeviceToHost), "read mask"));
+    PD_TRY(cpy(col.data(), d_col_ + e0, (e1 - e0) * 4, "read col"));
+    PD_TRY(cpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, "read mask"));
   }
   uint64_t c = 0;
   for (uint64_t i = 0; i < nloc; ++i) {
@@ -719,9 +763,15 @@ int Engine::get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, u
 
 int Engine::get_wall(uint32_t sim, double *wall_info, double *reaction) {
   if (sim >= S_) return PD_EINVAL;
+  if (finished_[sim]) {  // kept by finish_sim
+    const double *w = final_[sim].data() + 15 * (sim_node0_[sim + 1] - sim_node0_[sim]);
+    if (wall_info) std::memcpy(wall_info, w, 6 * 8);
+    if (reaction) std::memcpy(reaction, w + 6, 18 * 8);
+    return PD_OK;
+  }
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
   DevSimState st;
-  PD_TRY(check(cudaMemcpy(&st, d_ss_ + sim, sizeof(st), cudaMemcpyDeviceToHost), "read wall"));
+  PD_TRY(cpy(&st, d_ss_ + sim, sizeof(st), "read wall"));
   if (wall_info) std::memcpy(wall_info, st.wall, 6 * 8);
   if (reaction) std::memcpy(reaction, st.react, 18 * 8);
   return PD_OK;
@@ -729,15 +779,15 @@ int Engine::get_wall(uint32_t sim, double *wall_info, double *reaction) {
 
 int Engine::get_aabb(double *lrtb) {
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
-  return check(cudaMemcpy(lrtb, d_lrtb_, 6ull * P_ * 8, cudaMemcpyDeviceToHost), "read aabb");
+  return cpy(lrtb, d_lrtb_, 6ull * P_ * 8, "read aabb");
 }
 
 int Engine::get_stats(pd_stats *st) {
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
   DevCounters c;
-  PD_TRY(check(cudaMemcpy(&c, d_cnt_, sizeof(c), cudaMemcpyDeviceToHost), "read counters"));
+  PD_TRY(cpy(&c, d_cnt_, sizeof(c), "read counters"));
   DevSimState s0;
-  PD_TRY(check(cudaMemcpy(&s0, d_ss_, sizeof(s0), cudaMemcpyDeviceToHost), "read sim"));
+  PD_TRY(cpy(&s0, d_ss_, sizeof(s0), "read sim"));
   st->step = s0.t - 1;
   st->live_bonds = stats_ ? c.live_bonds : initial_bonds_;
   st->pairwise_computations = c.pairwise;
@@ -745,7 +795,7 @@ int Engine::get_stats(pd_stats *st) {
   st->rebuilds = c.rebuilds;
   st->device_errors = c.err;
   unsigned long long z = 0;
-  PD_TRY(check(cudaMemcpy(&d_cnt_->pairwise, &z, 8, cudaMemcpyHostToDevice), "reset pairwise"));
+  PD_TRY(cpy(&d_cnt_->pairwise, &z, 8, "reset pairwise"));
   return PD_OK;
 }
 
@@ -755,7 +805,7 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
   if (skin_frac > 0 && skin_frac != bp_.skin_frac) {
     bp_.skin_frac = skin_frac;
     std::vector<DevSimParams> sps(S_);
-    PD_TRY(check(cudaMemcpy(sps.data(), d_sp_, S_ * sizeof(DevSimParams), cudaMemcpyDeviceToHost), "read params"));
+    PD_TRY(cpy(sps.data(), d_sp_, S_ * sizeof(DevSimParams), "read params"));
     double mh = 1e300;
     for (auto &sp : sps) {
       const double skin = skin_frac * sp.Rc;
@@ -765,9 +815,9 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
       mh = std::min(mh, 0.5 * skin);
     }
     half_skin_ = mh;
-    PD_TRY(check(cudaMemcpy(d_sp_, sps.data(), S_ * sizeof(DevSimParams), cudaMemcpyHostToDevice), "write params"));
+    PD_TRY(cpy(d_sp_, sps.data(), S_ * sizeof(DevSimParams), "write params"));
     double big = 1e300;
-    PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
+    PD_TRY(cpy(&d_cnt_->moved, &big, 8, "force rebuild"));
     relaunch = true;
   }
   if (cand_cap > 0 && cand_cap != bp_.cand_cap) {
@@ -778,7 +828,7 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
     bp_.cand_cap = cand_cap;
     PD_TRY(alloc_candidates());
     double big = 1e300;
-    PD_TRY(check(cudaMemcpy(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice), "force rebuild"));
+    PD_TRY(cpy(&d_cnt_->moved, &big, 8, "force rebuild"));
     relaunch = true;
   }
   if (tpb > 0 && tpb != tpb_) {
@@ -796,7 +846,7 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
 
 int Engine::clear_device_errors() {
   uint32_t z = 0;
-  return check(cudaMemcpy(&d_cnt_->err, &z, 4, cudaMemcpyHostToDevice), "clear errors");
+  return cpy(&d_cnt_->err, &z, 4, "clear errors");
 }
 
 double Engine::step_bytes(uint64_t live) const {
@@ -836,6 +886,8 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
     }
     cur_ ^= 1;
     ++steps_done_;
+    for (uint32_t i = 0; i < S_; ++i)
+      if (!finished_[i]) sim_steps_[i] += 1;
   }
   for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
   return rc;
@@ -843,13 +895,13 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
 
 int Engine::count_live_bonds(uint64_t *live) {
   unsigned long long *d = nullptr;
-  PD_TRY(check(cudaMalloc(&d, 8), "alloc"));
+  PD_TRY(check(cudaMallocAsync((void **)&d, 8, stream_), "alloc"));
   cudaMemsetAsync(d, 0, 8, stream_);
   launch_count_live(view(cur_), d, stream_);
   unsigned long long h = 0;
   cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, stream_);
+  cudaFreeAsync(d, stream_);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
-  cudaFree(d);
   PD_TRY(check(e, "count live bonds"));
   *live = h;
   return PD_OK;
@@ -892,8 +944,8 @@ int Engine::set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t 
   const uint64_t e0 = h_slice_ptr_[s0], e1 = h_slice_ptr_[s1];
   if (e1 == e0) return PD_OK;
   std::vector<uint32_t> col(e1 - e0), mask((e1 - e0) / 32);
-  PD_TRY(check(cudaMemcpy(col.data(), d_col_ + e0, (e1 - e0) * 4, cudaMemcpyDeviceToHost), "read col"));
-  PD_TRY(check(cudaMemcpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, cudaMemcpyDeviceToHost), "read mask"));
+  PD_TRY(cpy(col.data(), d_col_ + e0, (e1 - e0) * 4, "read col"));
+  PD_TRY(cpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, "read mask"));
   for (uint64_t i = 0; i < nloc; ++i) {
     const uint64_t g = g0 + i;
     const uint64_t base = h_slice_ptr_[g >> 5] - e0 + (g & 31);
@@ -909,7 +961,7 @@ int Engine::set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t 
         mask[mbase + j] &= ~bit;
     }
   }
-  PD_TRY(check(cudaMemcpy(d_mask_ + e0 / 32, mask.data(), (e1 - e0) / 32 * 4, cudaMemcpyHostToDevice), "write mask"));
+  PD_TRY(cpy(d_mask_ + e0 / 32, mask.data(), (e1 - e0) / 32 * 4, "write mask"));
   return PD_OK;
 }
 
@@ -917,9 +969,9 @@ int Engine::set_wall(uint32_t sim, const double *wall_info) {
   if (sim >= S_) return PD_EINVAL;
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
   DevSimState st;
-  PD_TRY(check(cudaMemcpy(&st, d_ss_ + sim, sizeof(st), cudaMemcpyDeviceToHost), "read sim state"));
+  PD_TRY(cpy(&st, d_ss_ + sim, sizeof(st), "read sim state"));
   for (int k = 0; k < 6; ++k) st.wall[k] = wall_info[k];
-  PD_TRY(check(cudaMemcpy(d_ss_ + sim, &st, sizeof(st), cudaMemcpyHostToDevice), "write sim state"));
+  PD_TRY(cpy(d_ss_ + sim, &st, sizeof(st), "write sim state"));
   if (precision_ == PD_FP32C) PD_TRY(prepare_fused(cur_));  // walls in the local frames
   return check(cudaStreamSynchronize(stream_), "set_wall");
 }
@@ -965,7 +1017,8 @@ int Engine::snapshot() {
   for (auto &m : mutable_) total += (m.second + 255) & ~(size_t)255;
   if (total > backup_bytes_) {
     if (backup_) {
-      cudaFree(backup_);
+      cudaFreeAsync(backup_, stream_);
+      device_bytes_ -= backup_bytes_;
       allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), backup_), allocs_.end());
       backup_ = nullptr;
     }
@@ -982,6 +1035,8 @@ int Engine::snapshot() {
   }
   backup_cur_ = cur_;
   backup_steps_ = steps_done_;
+  backup_sim_steps_ = sim_steps_;
+  backup_finished_ = finished_;
   return check(cudaStreamSynchronize(stream_), "snapshot");
 }
 
@@ -999,6 +1054,13 @@ int Engine::restore() {
   }
   cur_ = backup_cur_;
   steps_done_ = backup_steps_;
+  sim_steps_ = backup_sim_steps_;
+  // a simulation finished after the snapshot is live again (its active flag came back)
+  for (uint32_t i = 0; i < S_; ++i)
+    if (finished_[i] && !backup_finished_[i]) {
+      finished_[i] = 0;
+      final_[i].clear();
+    }
   return check(cudaStreamSynchronize(stream_), "restore");
 }
 

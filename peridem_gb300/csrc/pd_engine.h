@@ -193,6 +193,21 @@ class Engine {
   int profile(uint32_t nsteps, double *phase_ms);
   // Live directed bonds of movable particles (popcount of the live masks).
   int count_live_bonds(uint64_t *live);
+  // ---- batches of independent simulations (one launch per phase covers all of them) ----
+  uint32_t num_sims() const { return S_; }
+  int sim_range(uint32_t sim, uint64_t *node0, uint64_t *n_nodes, uint32_t *particle0, uint32_t *n_particles) const;
+  uint64_t sim_steps(uint32_t sim) const { return sim < S_ ? sim_steps_[sim] : 0; }
+  // Reads the simulation's state back, keeps it on the host and stops stepping it: the
+  // kernels skip its nodes from the next launch on and its device state is not kept.
+  int finish_sim(uint32_t sim);
+  bool sim_finished(uint32_t sim) const { return sim < S_ && finished_[sim]; }
+  // N*3 arrays of one simulation (its own node order); any pointer may be NULL.
+  int get_sim_state(uint32_t sim, double *curpos, double *vel, double *acc, double *force, double *disp);
+  // Bytes of device memory this engine holds, and the same figure computed from a setup
+  // before anything is allocated.
+  uint64_t device_bytes() const { return device_bytes_; }
+  static uint64_t estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap);
+  int raw_alloc(void **p, size_t bytes);
   double step_bytes(uint64_t live_bonds) const;
   uint64_t initial_bonds() const { return initial_bonds_; }
   uint64_t num_nodes() const { return N_; }
@@ -213,6 +228,11 @@ class Engine {
   int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
   int check(cudaError_t e, const char *what);
+  // Copy / memset ordered on the engine's stream, then a wait for that stream only (never
+  // the legacy default stream, so other handles' work keeps running).
+  int cpy(void *dst, const void *src, size_t bytes, const char *what);
+  int mset(void *dst, int value, size_t bytes, const char *what);
+  int read_nodes(const double *d, uint64_t node0, uint64_t nn, double *dst);
   DevView view(int cur) const;
 
   std::vector<HostSim> sims_;
@@ -233,8 +253,16 @@ class Engine {
   size_t backup_bytes_ = 0;
   int backup_cur_ = 0;
   uint64_t backup_steps_ = 0;
+  std::vector<uint64_t> backup_sim_steps_;
+  std::vector<uint8_t> backup_finished_;
   uint64_t steps_done_ = 0;
   uint64_t initial_bonds_ = 0;
+  uint64_t device_bytes_ = 0;
+  uint64_t cand_bytes_ = 0;
+  std::vector<uint64_t> sim_node0_, sim_steps_;
+  std::vector<uint32_t> sim_p0_;
+  std::vector<uint8_t> finished_;
+  std::vector<std::vector<double>> final_;  // [sim]: curpos, vel, acc, force, disp (N*3 each)
   double half_skin_ = 0;
 
   // host mirrors used when reading results back

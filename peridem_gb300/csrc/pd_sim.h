@@ -13,6 +13,8 @@ struct pd_sim {
 
 namespace pdg {
 int host_sim_from_arrays(const pd_setup_arrays *su, const pd_config *cfg, HostSim &hs, std::string &err);
+// Records the text pd_global_error() returns (thread-local) and passes rc through.
+int set_global_error(int rc, const std::string &msg);
 }
 
 #endif

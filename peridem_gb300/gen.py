@@ -182,31 +182,38 @@ def cubes125(n=5, edge=1.0 * MM, h=0.125 * MM, seed=1, steps=20000, dt=2e-8, g=9
     return s, base_config(dt, steps)
 
 
+def _grid_pack(rng, m: int, count: int, pitch: float, hs, smin: float, smax: float) -> list:
+    """`count` particles of random shape/size/resolution on the first cells of an m^3 grid of
+    pitch `pitch` centred on the origin (cells in z, y, x order)."""
+    parts = []
+    box = m * pitch
+    for idx in range(count):
+        iz, rem = divmod(idx, m * m)
+        iy, ix = divmod(rem, m)
+        kind = ("sphere", "cube", "ellipsoid")[int(rng.integers(3))]
+        h = float(hs[int(rng.integers(len(hs)))])
+        # sizes are bounding diameters, so that randomly rotated particles on the
+        # 1.5 mm pitch never overlap: a cube of size d has edge d / sqrt(3)
+        if kind == "ellipsoid":
+            size = rng.uniform(smin, smax, size=3)
+        elif kind == "cube":
+            size = float(rng.uniform(smin, smax)) / math.sqrt(3.0)
+        else:
+            size = float(rng.uniform(smin, smax))
+        loc = lattice(kind, size, h)
+        c = np.array([(ix + 0.5) * pitch, (iy + 0.5) * pitch, (iz + 0.5) * pitch]) - box / 2
+        c = c + rng.uniform(-0.02, 0.02, size=3) * pitch
+        p = make_particle(loc, h, GLASS, 3.0, rng, 0.05, c, rotation=random_rotation(rng), Rc=None)
+        parts.append(p)
+    return parts
+
+
 def crush512(n=8, box=12.0 * MM, seed=2, steps=10000, dt=5e-9, hs=(0.05 * MM, 0.075 * MM, 0.1 * MM),
              smin=0.6 * MM, smax=1.4 * MM, wall_speed=-1.0):
     """Config 2: n^3 particles of random shape/size/resolution in a box; top wall moves down."""
     rng = np.random.default_rng(seed)
     Rc = 0.5 * min(hs)
-    pitch = box / n
-    parts = []
-    for iz in range(n):
-        for iy in range(n):
-            for ix in range(n):
-                kind = ("sphere", "cube", "ellipsoid")[int(rng.integers(3))]
-                h = float(hs[int(rng.integers(len(hs)))])
-                # sizes are bounding diameters, so that randomly rotated particles on the
-                # 1.5 mm pitch never overlap: a cube of size d has edge d / sqrt(3)
-                if kind == "ellipsoid":
-                    size = rng.uniform(smin, smax, size=3)
-                elif kind == "cube":
-                    size = float(rng.uniform(smin, smax)) / math.sqrt(3.0)
-                else:
-                    size = float(rng.uniform(smin, smax))
-                loc = lattice(kind, size, h)
-                c = np.array([(ix + 0.5) * pitch, (iy + 0.5) * pitch, (iz + 0.5) * pitch]) - box / 2
-                c = c + rng.uniform(-0.02, 0.02, size=3) * pitch
-                p = make_particle(loc, h, GLASS, 3.0, rng, 0.05, c, rotation=random_rotation(rng), Rc=None)
-                parts.append(p)
+    parts = _grid_pack(rng, n, n ** 3, box / n, hs, smin, smax)
     half = box / 2
     wall = dict(allow=1, geom=[-half, -half, -half, half, half, half])
     s = finish(parts, Rc, dt, wall=wall)
@@ -214,4 +221,45 @@ def crush512(n=8, box=12.0 * MM, seed=2, steps=10000, dt=5e-9, hs=(0.05 * MM, 0.
     return s, base_config(dt, steps, speed_wall_z_max=wall_speed)
 
 
+def aggregate(n_particles: int, seed: int, steps: int, wall_speed: float = -1.0, dt=5e-9, pitch=1.5 * MM,
+              hs=(0.05 * MM, 0.075 * MM, 0.1 * MM), smin=0.6 * MM, smax=1.4 * MM):
+    """One aggregate of the serving stream: n_particles drawn like config 2's particles, packed
+    on the smallest cubic grid of config 2's pitch that holds them, in a walled box whose top
+    wall moves down at |wall_speed|."""
+    rng = np.random.default_rng(seed)
+    Rc = 0.5 * min(hs)
+    m = 1
+    while m ** 3 < n_particles:
+        m += 1
+    parts = _grid_pack(rng, m, n_particles, pitch, hs, smin, smax)
+    half = m * pitch / 2
+    wall = dict(allow=1, geom=[-half, -half, -half, half, half, half])
+    s = finish(parts, Rc, dt, wall=wall)
+    s.meta["name"] = f"aggregate{n_particles}"
+    return s, base_config(dt, steps, speed_wall_z_max=-abs(wall_speed))
+
+
+def serving_stream(n: int = 256, rate: float = 4.0, seed: int = 3, pmin: int = 8, pmax: int = 64,
+                   steps=(2000, 10000), speed=(0.5, 2.0)) -> list[dict]:
+    """Config 4's request stream: Poisson arrivals at `rate` per second; each request is an
+    aggregate of pmin..pmax particles with a random compression speed and step count.
+    Returns light specs; aggregate(**spec["gen"]) builds the setup."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        npart = int(rng.integers(pmin, pmax + 1))
+        nst = int(rng.integers(steps[0], steps[1] + 1))
+        v = float(rng.uniform(speed[0], speed[1]))
+        out.append(dict(rid=i, arrival=t, gen=dict(n_particles=npart, seed=int(seed * 100003 + i), steps=nst,
+                                                   wall_speed=-v)))
+    return out
+
+
 WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512}
+
+
+def build_aggregate(kw: dict):
+    """aggregate(**kw): a top-level function, so that a process pool can build requests."""
+    return aggregate(**kw)

@@ -146,3 +146,99 @@ class Sim:
         n = C.c_uint64()
         self._ck(lib().pd_count_live_bonds(self.h, C.byref(n)))
         return int(n.value)
+
+
+def _setup_array(setups):
+    arr = (_capi.PdSetupArrays * len(setups))()
+    keep = []
+    for i, s in enumerate(setups):
+        st, k = setup_struct(s)
+        arr[i] = st
+        keep.append(k)
+    return arr, keep
+
+
+def estimate_bytes(setups: list[Setup], precision: str = "fp32c") -> int:
+    """Device bytes a batch of these setups would take (no device work)."""
+    arr, keep = _setup_array(setups)
+    b = C.c_uint64()
+    rc = lib().pd_estimate_bytes(arr, len(setups), PRECISIONS[precision], C.byref(b))
+    del keep
+    if rc != 0:
+        raise PdError(rc, lib().pd_global_error().decode())
+    return int(b.value)
+
+
+def device_memory() -> tuple[int, int]:
+    """(free, total) bytes of the current device."""
+    f, t = C.c_uint64(), C.c_uint64()
+    rc = lib().pd_device_memory(C.byref(f), C.byref(t))
+    if rc != 0:
+        raise PdError(rc, lib().pd_global_error().decode())
+    return int(f.value), int(t.value)
+
+
+class Batch(Sim):
+    """Independent simulations in one handle: every phase of a step is one launch over all of
+    them. Simulation i keeps its own node order; finish(i) ends it at the current step."""
+
+    def __init__(self, setups: list[Setup], configs: list, precision: str = "fp32c"):
+        cfgs = (_capi.PdConfig * len(setups))()
+        for i, c in enumerate(configs):
+            cfgs[i] = c if isinstance(c, _capi.PdConfig) else make_config(c)
+        arr, keep = _setup_array(setups)
+        h = C.c_void_p()
+        rc = lib().pd_create_batch(arr, cfgs, len(setups), PRECISIONS[precision], C.byref(h))
+        del keep
+        if rc != 0:
+            raise PdError(rc, lib().pd_global_error().decode())
+        self.setups = list(setups)
+        super().__init__(setups[0], cfgs[0], precision, handle=h)
+        self.n_sims = len(setups)
+
+    def _gk(self, rc: int):
+        if rc != 0:
+            raise PdError(rc, lib().pd_global_error().decode() or lib().pd_last_error(self.h).decode())
+
+    def poll(self) -> bool:
+        """True when the handle's queued work is done (never blocks)."""
+        rc = lib().pd_sync(self.h, 0)
+        if rc == _capi.PD_ETIMEOUT:
+            return False
+        self._ck(rc)
+        return True
+
+    def sim_range(self, i: int) -> tuple[int, int, int, int]:
+        n0, nn, p0, npp = C.c_uint64(), C.c_uint64(), C.c_uint32(), C.c_uint32()
+        self._gk(lib().pd_sim_range(self.h, i, C.byref(n0), C.byref(nn), C.byref(p0), C.byref(npp)))
+        return n0.value, nn.value, p0.value, npp.value
+
+    def sim_steps(self, i: int) -> int:
+        n = C.c_uint64()
+        self._gk(lib().pd_sim_steps(self.h, i, C.byref(n)))
+        return int(n.value)
+
+    def finish(self, i: int):
+        self._ck(lib().pd_finish_sim(self.h, i))
+
+    def sim_state(self, i: int) -> dict:
+        nn = self.sim_range(i)[1]
+        out = {k: np.empty((nn, 3)) for k in ("curpos", "vel", "acc", "force", "disp")}
+        self._ck(lib().pd_get_sim_state(self.h, i, ptr(out["curpos"]), ptr(out["vel"]), ptr(out["acc"]),
+                                        ptr(out["force"])))
+        self._ck(lib().pd_get_sim_disp(self.h, i, ptr(out["disp"])))
+        return out
+
+    def sim_wall(self, i: int) -> tuple[np.ndarray, np.ndarray]:
+        w = np.empty(6)
+        r = np.empty((6, 3))
+        self._ck(lib().pd_get_sim_wall(self.h, i, ptr(w), ptr(r)))
+        return w, r
+
+    def sim_connectivity(self, i: int, p: int) -> np.ndarray:
+        return self.connectivity(self.sim_range(i)[2] + p)
+
+    def device_bytes(self) -> int:
+        b = C.c_uint64()
+        self._gk(lib().pd_device_bytes(self.h, C.byref(b)))
+        return int(b.value)

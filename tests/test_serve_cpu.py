@@ -1,0 +1,108 @@
+"""Host logic of the serving loop (peridem_gb300/serve.py) on a fake batch backend: admission
+by device budget, chunking that stops every request at exactly its step count, cohort
+retirement, oversize requests, and the queueing arithmetic of the one-at-a-time baseline."""
+from types import SimpleNamespace
+
+import numpy as np
+
+from peridem_gb300 import serve
+
+BYTES_PER_NODE = 1000
+
+
+class FakeBatch:
+    instances = []
+
+    def __init__(self, setups, configs, precision):
+        self.n = len(setups)
+        self.steps = [0] * self.n
+        self.fin = [False] * self.n
+        self.cfg = configs
+        self.nb = sum(len(s.pos) * BYTES_PER_NODE for s in setups)
+        self.closed = False
+        FakeBatch.instances.append(self)
+
+    def step(self, k, sync=True):
+        for i in range(self.n):
+            if not self.fin[i]:
+                self.steps[i] += k
+
+    def poll(self):
+        return True
+
+    def finish(self, i):
+        self.fin[i] = True
+
+    def sim_state(self, i):
+        return {"steps": self.steps[i]}
+
+    def sim_wall(self, i):
+        return (np.zeros(6), np.zeros((6, 3)))
+
+    def device_bytes(self):
+        return self.nb
+
+    def close(self):
+        self.closed = True
+
+
+def fake_estimate(setups, precision):
+    return sum(len(s.pos) * BYTES_PER_NODE for s in setups)
+
+
+def _req(rid, nodes, steps, arrival=0.0):
+    s = SimpleNamespace(pos=np.zeros((nodes, 3)), conn=np.zeros((nodes * 4, 2)))
+    return serve.Request(rid, s, {"dt": 1e-8}, steps, arrival)
+
+
+def _server(capacity, **kw):
+    FakeBatch.instances.clear()
+    return serve.Server("fp32c", capacity_bytes=capacity, make_batch=FakeBatch, estimate=fake_estimate, **kw)
+
+
+def test_every_request_stops_at_its_step_count():
+    reqs = [_req(i, 100 + 10 * i, st) for i, st in enumerate([7, 130, 64, 1, 99, 500, 33])]
+    srv = _server(10 ** 9, chunk_steps=50, max_batch=4)
+    res = srv.run(reqs, realtime=False)
+    assert [r.rid for r in res] == list(range(len(reqs)))
+    for r, q in zip(res, reqs):
+        assert r.error is None
+        assert r.state["steps"] == q.steps
+        assert r.bonds == 2 * len(q.setup.conn)
+    assert srv.used == 0 and all(b.closed for b in FakeBatch.instances)
+    assert len(FakeBatch.instances) >= 2  # max_batch=4 splits 7 requests
+
+
+def test_admission_respects_the_budget():
+    reqs = [_req(i, 1000, 40) for i in range(6)]
+    srv = _server(2500 * BYTES_PER_NODE, chunk_steps=10)
+    res = srv.run(reqs, realtime=False)
+    assert all(r.error is None for r in res)
+    assert srv.peak_used <= 2500 * BYTES_PER_NODE
+    assert max(b.n for b in FakeBatch.instances) <= 2
+
+
+def test_oversize_request_is_rejected_not_blocking():
+    reqs = [_req(0, 10, 5), _req(1, 10 ** 6, 5), _req(2, 10, 5)]
+    srv = _server(10 ** 5 * BYTES_PER_NODE)
+    res = srv.run(reqs, realtime=False)
+    assert res[1].error and res[0].error is None and res[2].error is None
+
+
+def test_realtime_arrivals_are_respected():
+    reqs = [_req(i, 50, 20, arrival=0.02 * i) for i in range(4)]
+    srv = _server(10 ** 9, chunk_steps=5)
+    res = srv.run(reqs)
+    for r in res:
+        assert r.admitted >= r.arrival - 1e-3
+        assert r.done >= r.admitted
+    s = serve.summarize(res, max(r.done for r in res))
+    assert s["completed"] == 4 and s["ttc_p99_s"] >= s["ttc_p50_s"]
+
+
+def test_sequential_queue_arithmetic():
+    arr = np.array([0.0, 1.0, 1.5, 10.0])
+    svc = np.array([2.0, 2.0, 1.0, 0.5])
+    ttc = serve.sequential_ttc(arr, svc)
+    # done: 2, 4, 5, 10.5
+    np.testing.assert_allclose(ttc, [2.0, 3.0, 3.5, 0.5])
