@@ -166,7 +166,7 @@ __device__ __forceinline__ bool nonfinite(double x) {
 
 // End-of-step work of the FP32 form for one particle: AABB from the local-frame keys of this
 // step (widened by a few float ulps each way), anchors moved on by one step, walls expressed in
-// the frame of the next step's disp32.
+// the frame of the next step's records.
 __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const DevPart &P,
                                                    const DevSimState &st) {
   double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;

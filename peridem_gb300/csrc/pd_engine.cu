@@ -97,14 +97,12 @@ DevView Engine::view(int cur) const {
   v.bxin = d_bxin_;
   v.brxin = d_brxin_;
   v.E = E_;
-  v.pos32 = d_pos32_;
-  v.disp32 = d_disp32_;
   v.anchor = d_anchor_;
   if (precision_ == PD_FP32C) {
     v.disp = d_dispb_[cur];
     v.disp_next = d_dispb_[cur ^ 1];
-    v.disp32 = d_disp32b_[cur];
-    v.disp32_next = d_disp32b_[cur ^ 1];
+    v.rec = d_rec_[cur];
+    v.rec_next = d_rec_[cur ^ 1];
     v.anchor_next = d_anchor_next_;
     v.clamp_flag = d_clamp_flag_;
     v.fused = 1;
@@ -450,21 +448,26 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_bxin_, std::max<uint64_t>(E_, 1), err));
     PD_TRY(dalloc(this, allocs_, &d_brxin_, std::max<uint64_t>(E_, 1), err));
   } else {
-    std::vector<float4> p32(C);
+    std::vector<Rec32> r32(C);
     for (uint64_t g = 0; g < C; ++g) {
+      Rec32 &r = r32[g];
+      r.u = make_float4(0.f, 0.f, 0.f, 0.f);
       if (g < N_) {
         const DevPart &P = parts[h_pid_[g]];
-        p32[g] = make_float4((float)(pos[g] - P.anchor_pos[0]), (float)(pos[C + g] - P.anchor_pos[1]),
-                             (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)vol[g]);
+        r.p = make_float4((float)(pos[g] - P.anchor_pos[0]), (float)(pos[C + g] - P.anchor_pos[1]),
+                          (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)vol[g]);
       } else {
-        p32[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.p = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    PD_TRY(dalloc(this, allocs_, &d_pos32_, C, err));
-    PD_TRY(dalloc(this, allocs_, &d_disp32_, C, err));
-    d_disp32b_[0] = d_disp32_;
-    PD_TRY(dalloc(this, allocs_, &d_disp32b_[1], C, err));
-    PD_TRY(mset(d_disp32b_[1], 0, C * sizeof(float4), "memset disp32"));
+    for (int b = 0; b < 2; ++b) {
+      PD_TRY(dalloc(this, allocs_, &d_rec_[b], C, err));
+      if (reinterpret_cast<uintptr_t>(d_rec_[b]) % 32) {  // the bond kernel reads records with 256-bit loads
+        err = "node records not 32-byte aligned";
+        return PD_ECUDA;
+      }
+      PD_TRY(up(d_rec_[b], r32.data(), C * sizeof(Rec32), "upload rec32"));
+    }
     d_dispb_[0] = d_disp_;
     PD_TRY(dalloc(this, allocs_, &d_dispb_[1], 3 * C, err));
     PD_TRY(dalloc(this, allocs_, &d_anchor_, 3ull * P_, err));
@@ -480,8 +483,6 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_wall_local_, 6ull * P_, err));
     PD_TRY(dalloc(this, allocs_, &d_lrtb_local_, 6ull * P_, err));
     PD_TRY(mset(d_extra_flag_, 0, C, "memset extra flag"));
-    PD_TRY(up(d_pos32_, p32.data(), C * sizeof(float4), "upload pos32"));
-    PD_TRY(mset(d_disp32_, 0, C * sizeof(float4), "memset disp32"));
   }
 
   // broad phase
@@ -517,7 +518,7 @@ int Engine::alloc_and_upload() {
 
 // FP32 form: disp[cur^1] holds the displacement of the last completed step (or the initial
 // one); derive this step's AABBs, anchors and wall frames from it, then run the predictor
-// into disp[cur]/disp32[cur] and set the anchors of the next step's disp32.
+// into disp[cur]/rec[cur] and set the anchors of the next step's records.
 int Engine::prepare_fused(int cur) {
   // AABBs from pos + disp (timeloop.h:389-393), anchors := disp of each anchor node, walls in
   // the anchors' frame
@@ -1002,8 +1003,8 @@ int Engine::snapshot() {
   reg(d_centroid_, 3ull * P_ * 8);
   if (d_clamped_disp_) reg(d_clamped_disp_, 3 * n_clamped_ * 8);
   if (precision_ == PD_FP32C) {
-    reg(d_disp32b_[0], C * sizeof(float4));
-    reg(d_disp32b_[1], C * sizeof(float4));
+    reg(d_rec_[0], C * sizeof(Rec32));
+    reg(d_rec_[1], C * sizeof(Rec32));
     reg(d_anchor_, 3ull * P_ * 8);
     reg(d_anchor_next_, 3ull * P_ * 8);
     reg(d_wall_local_, 6ull * P_ * 4);

@@ -14,8 +14,9 @@
 //     mask[slice_ptr[s]/32 + j]. Breaking clears a bit; bonds are never re-added;
 //   * FP64 form only: per-entry constants xi = pos[q]-pos[i] (3 doubles), |xi| and the
 //     correctly rounded reciprocal of |xi| (gen_xi, particle2.h:241-257);
-//   * FP32-compensated form only: float4 (local position, volume) and float4 (local
-//     displacement) per node, local = relative to the particle's anchor node;
+//   * FP32-compensated form only: a 32-byte record per node, float4 (local position,
+//     volume) + float4 (local displacement), double-buffered; local = relative to the
+//     particle's anchor node;
 //   * contact broad phase: hashed cell list (counting sort) rebuilt only when the nodes may
 //     have moved more than half the skin since the last build; per-node candidate lists
 //     (fixed capacity, ascending global index) of nodes within contact radius + skin.
@@ -84,6 +85,12 @@ struct DevCounters {
   unsigned long long live_bonds;
 };
 
+// FP32 form: one 32-byte record per node, so that a bond gathers its partner with a single
+// 256-bit load: p = (anchor-relative position, volume), u = (anchor-relative displacement, 0).
+struct __align__(32) Rec32 {
+  float4 p, u;
+};
+
 // Everything a kernel needs, passed by value.
 struct DevView {
   uint64_t N;            // nodes
@@ -105,13 +112,13 @@ struct DevView {
   const double *bxi, *bxin, *brxin;  // FP64 form, [3][E], [E], [E]
   uint64_t E;
   // FP32-compensated form (the predictor of the next step runs in the bond kernel's tail:
-  // disp/disp32 are read for this step while disp_next/disp32_next receive the next one)
-  float4 *pos32, *disp32, *disp32_next;
+  // disp/rec are read for this step while disp_next/rec_next receive the next one)
+  Rec32 *rec, *rec_next;
   double *disp_next;
   const uint8_t *clamp_flag;  // 1 for nodes listed in clamped_nodes
   int fused;                  // 1: FP32 form with the fused predictor
-  const double *anchor;       // [P][3] anchor of disp32 (this step)
-  double *anchor_next;        // [P][3] anchor of disp32_next
+  const double *anchor;       // [P][3] anchor of rec[].u (this step)
+  double *anchor_next;        // [P][3] anchor of rec_next[].u
   double break_band;     // relative band around snot where the FP64 stretch decides
   double *f_extra;       // [3][Ncap] FP64 non-bond force density of flagged nodes
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
@@ -275,7 +282,7 @@ class Engine {
   // device buffers
   double *d_pos_ = nullptr, *d_disp_ = nullptr, *d_vel_[2] = {nullptr, nullptr}, *d_acc_ = nullptr;
   double *d_dispb_[2] = {nullptr, nullptr};  // FP32 form: double-buffered displacement
-  float4 *d_disp32b_[2] = {nullptr, nullptr};
+  Rec32 *d_rec_[2] = {nullptr, nullptr};
   double *d_anchor_next_ = nullptr;
   uint8_t *d_clamp_flag_ = nullptr;
   double *d_force_ = nullptr, *d_ext_ = nullptr, *d_vol_ = nullptr;
@@ -285,7 +292,6 @@ class Engine {
   uint16_t *d_deg_ = nullptr;
   uint32_t *d_col_ = nullptr, *d_mask_ = nullptr;
   double *d_bxi_ = nullptr, *d_bxin_ = nullptr, *d_brxin_ = nullptr;
-  float4 *d_pos32_ = nullptr, *d_disp32_ = nullptr;
   double *d_anchor_ = nullptr;
   double *d_f_extra_ = nullptr;
   uint8_t *d_extra_flag_ = nullptr;

@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(128) k_extra32(DevView v) {
   const bool mov = P.movable != 0;
   bool wall_near = false;
   if (mov && P.stoppable && sp.allow_wall) {
-    const float4 pl = v.pos32[n], ul = v.disp32[n];
+    const float4 pl = v.rec[n].p, ul = v.rec[n].u;
     const float cx = pl.x + ul.x, cy = pl.y + ul.y, cz = pl.z + ul.z;
     const float *wl = v.wall_local + 6 * (uint64_t)k;
     const float lim = (float)sp.Rc * 1.001f;
@@ -182,12 +182,16 @@ __device__ __forceinline__ float bond32(const float4 &pi, const float4 &ui, cons
   const float xx = pq.x - pi.x, xy = pq.y - pi.y, xz = pq.z - pi.z;
   const float ex = uq.x - ui.x, ey = uq.y - ui.y, ez = uq.z - ui.z;
   const float yx = xx + ex, yy = xy + ey, yz = xz + ez;
-  const float xin = sqrtf(fmaf(xx, xx, fmaf(xy, xy, xz * xz)));
-  const float yn = sqrtf(fmaf(yx, yx, fmaf(yy, yy, yz * yz)));
+  const float x2 = fmaf(xx, xx, fmaf(xy, xy, xz * xz));
+  const float y2 = fmaf(yx, yx, fmaf(yy, yy, yz * yz));
+  // |xi| and |xi+eta| from the hardware reciprocal square root (relative error ~1e-7; the
+  // breaking decision near snot is re-taken in FP64)
+  const float rx = rsqrtf(x2), ry = rsqrtf(y2);
+  const float xin = x2 * rx, yn = y2 * ry;
   const float xe = fmaf(xx, ex, fmaf(xy, ey, xz * ez));
   const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
   const float str = __fdividef(fmaf(2.f, xe, ee), (yn + xin) * xin);
-  const float g = __fdividef(cn * str * pq.w, yn);
+  const float g = cn * str * pq.w * ry;
   float t, y;
   y = fmaf(g, yx, -a.cx); t = a.sx + y; a.cx = (t - a.sx) - y; a.sx = t;
   y = fmaf(g, yy, -a.cy); t = a.sy + y; a.cy = (t - a.sy) - y; a.sy = t;
@@ -195,8 +199,22 @@ __device__ __forceinline__ float bond32(const float4 &pi, const float4 &ui, cons
   return str;
 }
 
-// U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register cap).
-template <int U, int MINB>
+// A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector.
+template <int W>
+__device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
+  if (W) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(u.x), "=f"(u.y), "=f"(u.z), "=f"(u.w)
+        : "l"(r));
+  } else {
+    p = __ldg(&r->p);
+    u = __ldg(&r->u);
+  }
+}
+
+// U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register
+// cap); W: 256-bit record loads.
+template <int U, int MINB, int W>
 __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
@@ -207,8 +225,8 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
   const DevSimState &st = v.ss[P.sim];
   const bool run = valid && st.active;
   const uint64_t C3 = v.Ncap;
-  const float4 pi4 = v.pos32[nn];
-  const float4 ui4 = v.disp32[nn];
+  float4 pi4, ui4;
+  ld_rec<W>(v.rec + nn, pi4, ui4);
   Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   uint32_t live = 0;
   if (run && movable) {
@@ -219,8 +237,7 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
     const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
-    const float4 *__restrict__ p32 = v.pos32;
-    const float4 *__restrict__ d32 = v.disp32;
+    const Rec32 *__restrict__ rec = v.rec;
     int j = 0;
     for (; j + U <= dg; j += U) {
       uint32_t q[U], m[U];
@@ -231,10 +248,7 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
       }
       float4 pq[U], uq[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        pq[u] = __ldg(p32 + q[u]);
-        uq[u] = __ldg(d32 + q[u]);
-      }
+      for (int u = 0; u < U; ++u) ld_rec<W>(rec + q[u], pq[u], uq[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if ((m[u] >> lane) & 1u) {
@@ -252,7 +266,9 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
       if (!((mw >> lane) & 1u)) continue;
       const uint32_t q = __ldg(colp + 32 * j);
       ++live;
-      const float str = bond32(pi4, ui4, __ldg(p32 + q), __ldg(d32 + q), cn, a);
+      float4 pq, uq;
+      ld_rec<W>(rec + q, pq, uq);
+      const float str = bond32(pi4, ui4, pq, uq, cn, a);
       if (brk && str > slo) {
         if (str > shi) cut_bond(&maskp[j], lane);
         else band_check(v, nn, q, &maskp[j], lane, P.snot);
@@ -295,7 +311,7 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
     const float ix = (float)(dn.x - d.x), iy = (float)(dn.y - d.y), iz = (float)(dn.z - d.z);
     i2 = ix * ix + iy * iy + iz * iz;
     const double *anx = v.anchor_next + 3 * (uint64_t)k;
-    v.disp32_next[nn] = make_float4((float)(dn.x - anx[0]), (float)(dn.y - anx[1]), (float)(dn.z - anx[2]), 0.f);
+    v.rec_next[nn].u = make_float4((float)(dn.x - anx[0]), (float)(dn.y - anx[1]), (float)(dn.z - anx[2]), 0.f);
   }
   // particle AABB of this step's positions in the particle's local frame
   {
@@ -345,9 +361,10 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
   if (v.P) k_anchor_next<<<(v.P + 127) / 128, 128, 0, s>>>(v);
 }
 
-// Bond-kernel variants the autotuner chooses from: {positions per load group, min blocks/SM}.
-const int kBondVariants[][2] = {{4, 1}, {2, 8}, {4, 6}, {8, 1}, {8, 4}, {1, 8}};
-const int kNumBondVariants = 6;
+// Bond-kernel variants the autotuner chooses from: {positions per load group, min blocks/SM,
+// 256-bit record loads}.
+const int kBondVariants[][3] = {{4, 6, 1}, {4, 6, 0}, {2, 8, 1}, {4, 4, 1}, {8, 4, 1}, {1, 8, 1}, {4, 1, 1}};
+const int kNumBondVariants = 7;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -357,12 +374,13 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   k_extra32<<<(unsigned)blocks, 128, 0, s>>>(v);
   const unsigned b = (unsigned)blocks;
   switch (variant) {
-    case 1: k_bond32<2, 8><<<b, 128, 0, s>>>(v); break;
-    case 2: k_bond32<4, 6><<<b, 128, 0, s>>>(v); break;
-    case 3: k_bond32<8, 1><<<b, 128, 0, s>>>(v); break;
-    case 4: k_bond32<8, 4><<<b, 128, 0, s>>>(v); break;
-    case 5: k_bond32<1, 8><<<b, 128, 0, s>>>(v); break;
-    default: k_bond32<4, 1><<<b, 128, 0, s>>>(v); break;
+    case 1: k_bond32<4, 6, 0><<<b, 128, 0, s>>>(v); break;
+    case 2: k_bond32<2, 8, 1><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<4, 4, 1><<<b, 128, 0, s>>>(v); break;
+    case 4: k_bond32<8, 4, 1><<<b, 128, 0, s>>>(v); break;
+    case 5: k_bond32<1, 8, 1><<<b, 128, 0, s>>>(v); break;
+    case 6: k_bond32<4, 1, 1><<<b, 128, 0, s>>>(v); break;
+    default: k_bond32<4, 6, 1><<<b, 128, 0, s>>>(v); break;
   }
 }
 

@@ -44,9 +44,9 @@ __global__ void k_predict(DevView v) {
       // squared increment in FP32 (only bounds the broad-phase rebuild test)
       const float ix = (float)in.x, iy = (float)in.y, iz = (float)in.z;
       inc2 = ix * ix + iy * iy + iz * iz;
-      if (v.disp32) {
+      if (v.rec) {
         const double *an = v.anchor + 3 * (uint64_t)k;
-        v.disp32[n] = make_float4((float)(d.x - an[0]), (float)(d.y - an[1]), (float)(d.z - an[2]), 0.f);
+        v.rec[n].u = make_float4((float)(d.x - an[0]), (float)(d.y - an[1]), (float)(d.z - an[2]), 0.f);
       }
     }
   }
@@ -301,7 +301,7 @@ __global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const ui
   const DevSimState &st = v.ss[P.sim];
   const DevSimParams &sp = v.sp[P.sim];
   if (!st.active) return;
-  if (v.disp32) {
+  if (v.rec) {
     end_particle_fp32c(v, k, P, st);
   } else {
     unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
@@ -465,7 +465,7 @@ __global__ void k_init_lrtb_fin(DevView v) {
     L[c] = ord_key(INFINITY);
     L[3 + c] = ord_key(-INFINITY);
   }
-  if (v.disp32) {
+  if (v.rec) {
     const DevPart &P = v.parts[k];
     const DevSimState &st = v.ss[P.sim];
     double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
