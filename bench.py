@@ -231,27 +231,40 @@ def compare_forms(a, b, setup, conn_a, conn_b):
             "kinetic_energy_rel_diff": abs(ke_a - ke_b) / max(abs(ke_b), 1e-300)}
 
 
-def accuracy_run(name: str, nsteps: int, **over):
-    """Both forms of the same workload for `steps` steps; the FP64 form is bit-exact with the
-    CPU oracle (tests/test_gpu_parity.py), so it stands for the oracle here."""
+def accuracy_run(name: str, nsteps: int, eps: float = 1e-7, **over):
+    """Both forms of the same workload for `nsteps` steps; the FP64 form is bit-exact with the
+    CPU oracle (tests/test_gpu_parity.py), so it stands for the oracle here. A third run, FP64
+    from an initial displacement perturbed by eps*h per component (FP32 rounding level), gives
+    the FP64 solution's own sensitivity: the floor no reduced-precision form can beat once
+    fracture makes the dynamics chaotic."""
     from peridem_gb300 import gen
     from peridem_gb300.sim import Sim
     s, cfg = gen.WORKLOADS[name](**over)
     a = Sim(s, cfg, "fp32c")
     b = Sim(s, cfg, "fp64")
+    c = Sim(s, cfg, "fp64")
+    h = float(np.cbrt(np.min(s.vol)))
+    rng = np.random.default_rng(12345)
+    c.set_state(disp=s.disp + eps * h * rng.uniform(-1.0, 1.0, size=s.disp.shape))
     t0 = time.perf_counter()
     a.step(nsteps)
     t1 = time.perf_counter()
     b.step(nsteps)
     t2 = time.perf_counter()
+    c.step(nsteps)
     n0 = s.n_bonds_directed // 2
-    ca = [a.connectivity(p) for p in range(s.n_particles)]
     cb = [b.connectivity(p) for p in range(s.n_particles)]
-    out = compare_forms(a.state(), b.state(), s, ca, cb)
+    sb = b.state()
+    out = compare_forms(a.state(), sb, s, [a.connectivity(p) for p in range(s.n_particles)], cb)
+    sens = compare_forms(c.state(), sb, s, [c.connectivity(p) for p in range(s.n_particles)], cb)
     out.update(workload=name, steps=nsteps, nodes=s.n_nodes, initial_pairs=n0,
-               broken_pairs_fp64=n0 - out["live_pairs_fp64"], wall_s_fp32c=t1 - t0, wall_s_fp64=t2 - t1)
-    a.close()
-    b.close()
+               broken_pairs_fp64=n0 - out["live_pairs_fp64"], wall_s_fp32c=t1 - t0, wall_s_fp64=t2 - t1,
+               fp64_perturbed={"eps_h": eps, "max_rel_disp_err": sens["max_rel_disp_err"],
+                               "broken_bond_mismatch": sens["broken_bond_mismatch"],
+                               "bond_mismatches": sens["bond_mismatches"],
+                               "kinetic_energy_rel_diff": sens["kinetic_energy_rel_diff"]})
+    for x in (a, b, c):
+        x.close()
     return out
 
 
@@ -349,7 +362,11 @@ def ours(args):
     # ---- FP32-compensated form (the headline); the autotuner picks the bond-kernel variant on
     # a snapshot of the state and restores it
     sim = Sim(s, cfg, "fp32c")
-    variant, variant_ms = sim.autotune(8)
+    if args.variant >= 0:
+        variant, variant_ms = args.variant, np.zeros(0)
+        sim.set_variant(variant)
+    else:
+        variant, variant_ms = sim.autotune(8)
     with Clocks(lr) as clk:
         ms, live0, live1 = time_device(sim, K, W, dist, torch)
     clocks = clk.summary()
@@ -468,6 +485,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1, help="bond-kernel variant (default: autotune)")
     ap.add_argument("--acc-steps-c0", type=int, default=2000)
     ap.add_argument("--acc-steps-c1", type=int, default=4000)
     ap.add_argument("--serve", type=int, default=256, help="requests of the serving stream (0: skip)")

@@ -41,6 +41,7 @@ def oracle_lib() -> C.CDLL:
         L.or_step.argtypes = [_P, _u32]
         L.or_get_state.argtypes = [_P, _P, _P, _P, _P]
         L.or_get_disp.argtypes = [_P, _P]
+        L.or_get_afd.argtypes = [_P, _P]
         L.or_get_connectivity.argtypes = [_P, _u32, _P, _u64, C.POINTER(_u64)]
         L.or_get_wall.argtypes = [_P, _P, _P]
         L.or_get_aabb.argtypes = [_P, _P]
@@ -95,6 +96,11 @@ class Oracle:
         L = oracle_lib()
         L.or_get_state(self.h, _ptr(out["curpos"]), _ptr(out["vel"]), _ptr(out["acc"]), _ptr(out["force"]))
         L.or_get_disp(self.h, _ptr(out["disp"]))
+        return out
+
+    def afd(self) -> np.ndarray:
+        out = np.empty((self.N, 3))
+        oracle_lib().or_get_afd(self.h, _ptr(out))
         return out
 
     def connectivity(self, p: int) -> np.ndarray:
@@ -268,6 +274,9 @@ def run_reference(s, cfg: dict, outdir: str = "mem_out", setup_key: str = "mem_s
             for p in range(s.n_particles):
                 g = "P_%05d/" % p
                 d = {k: _get(name, g + k) for k in ("CurrPos", "vel", "acc", "force")}
+                afd = _get(name, g + "applied_force_density")
+                if afd is not None:
+                    d["applied_force_density"] = afd
                 d["Connectivity"] = _get(name, g + "Connectivity", np.int64)
                 parts.append(d)
             frames.setdefault(cnt, {})["particles"] = parts

@@ -723,6 +723,12 @@ int or_get_disp(or_sim *S, double *disp) {
   return PD_OK;
 }
 
+int or_get_afd(or_sim *S, double *afd) {
+  for (const Part &p : S->P)
+    for (uint32_t k = 0; k < p.n; ++k) put3(afd, p.g0 + k, p.afd[k]);
+  return PD_OK;
+}
+
 // NbdArr2conn (timeloop.h:20-44)
 int or_get_connectivity(or_sim *S, uint32_t particle, uint32_t *pairs, uint64_t cap, uint64_t *n) {
   if (particle >= S->P.size()) return PD_EINVAL;

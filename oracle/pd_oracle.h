@@ -26,6 +26,9 @@ void or_set_threads(or_sim *s, int threads);
 int or_step(or_sim *s, uint32_t nsteps);
 int or_get_state(or_sim *s, double *curpos, double *vel, double *acc, double *force);
 int or_get_disp(or_sim *s, double *disp);
+/* applied_force_density of every node (N*3; zero outside the prescribed-velocity particle and
+ * before the constraint is first applied), timeloop.h:760-764. */
+int or_get_afd(or_sim *s, double *afd);
 int or_get_connectivity(or_sim *s, uint32_t particle, uint32_t *pairs, uint64_t cap,
                         uint64_t *n);
 int or_get_wall(or_sim *s, double *wall_info, double *reaction);

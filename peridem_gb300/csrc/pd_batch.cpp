@@ -143,8 +143,14 @@ int Engine::get_sim_state(uint32_t sim, double *curpos, double *vel, double *acc
         for (uint64_t i : cl)
           for (int c = 0; c < 3; ++c) dsp[3 * (h_clamped_[i] - n0) + c] = cd[3 * i + c];
       }
-      const HostSim &s = sims_[sim];
-      for (uint64_t k = 0; k < 3 * nn; ++k) curpos[k] = s.pos[k] + dsp[k];
+      if (reset_possible_) {  // reset_partzero_y moves reference positions on the device
+        std::vector<double> p(3 * nn);
+        PD_TRY(read_nodes(d_pos_, n0, nn, p.data()));
+        for (uint64_t k = 0; k < 3 * nn; ++k) curpos[k] = p[k] + dsp[k];
+      } else {
+        const HostSim &s = sims_[sim];
+        for (uint64_t k = 0; k < 3 * nn; ++k) curpos[k] = s.pos[k] + dsp[k];
+      }
     }
   }
   if (vel) PD_TRY(read_nodes(d_vel_[cur_], n0, nn, vel));

@@ -172,6 +172,11 @@ int pd_get_state(pd_sim *s, double *curpos, double *vel, double *acc, double *fo
   return s->eng.get_state(curpos, vel, acc, force, nullptr);
 }
 
+int pd_get_applied_force_density(pd_sim *s, double *afd) {
+  if (!s || !afd) return fail_global(PD_EINVAL, "null argument");
+  return s->eng.get_afd(afd);
+}
+
 int pd_get_disp(pd_sim *s, double *disp) {
   if (!s) return fail_global(PD_EINVAL, "null handle");
   return s->eng.get_state(nullptr, nullptr, nullptr, nullptr, disp);

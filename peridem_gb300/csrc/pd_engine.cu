@@ -121,6 +121,12 @@ DevView Engine::view(int cur) const {
   v.cand_n = bp_.cand_n;
   v.cand_cap = bp_.cand_cap;
   v.centroid = d_centroid_;
+  v.afd = d_afd_;
+  if (n_clamped_) {
+    v.clamped_ptr = d_clamped_;
+    v.clamped_list = d_clamped_ + (P_ + 1);
+    v.clamped_disp = d_clamped_disp_;
+  }
   v.cnt = d_cnt_;
   v.stats = stats_ ? 1 : 0;
   return v;
@@ -134,6 +140,7 @@ static void host_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t
   if (sp.set_damping_ts != -1 && t == (uint32_t)sp.set_damping_ts) st.damping = 1;
   if (sp.set_zero_wall_speed_ts != -1 && t == (uint32_t)sp.set_zero_wall_speed_ts)
     for (int c = 0; c < 6; ++c) st.spd[c] = 0;
+  if (sp.set_fix_velocity_ts != -1 && t == (uint32_t)sp.set_fix_velocity_ts) st.vconstraint = 1;
   if (sp.gradient_extforce) {
     double sc = (double)t / (double)sp.extforce_maxstep;
     if (sc > 1) sc = 1;
@@ -354,6 +361,20 @@ int Engine::alloc_and_upload() {
     sp.np = s.np;
     sp.node0 = gnode;
     sp.nnodes = ns;
+    // prescribed velocity and reset_partzero_y (timeloop.h:412-420, 500-535, 684-764)
+    sp.pv_particle = (cf.particle_w_fixed_velocity >= 0 && (uint32_t)cf.particle_w_fixed_velocity < s.np)
+                         ? cf.particle_w_fixed_velocity
+                         : -1;
+    sp.set_fix_velocity_ts = cf.set_fix_velocity_timestep;
+    sp.fix_mean_x = cf.fix_velocity_mean_x;
+    sp.fix_angular = cf.fix_velocity_angular;
+    sp.pv_mean_x = cf.prescribed_velocity_mean_x;
+    sp.pv_angular = cf.prescribed_angular_vel;
+    sp.reset_y = (cf.reset_partzero_y && s.np >= 2) ? 1 : 0;
+    sp.reset_y_ts = cf.reset_partzero_y_timestep;
+    sp.wheel_rad = cf.wheel_rad;
+    if (sp.pv_particle >= 0) pv_possible_ = true;
+    if (sp.reset_y) reset_possible_ = true;
     // Wall: load_wall<3> then RectWall::apply_config (contact.h:325-372)
     DevSimState &st = sss[si];
     std::memset(&st, 0, sizeof(st));
@@ -439,6 +460,11 @@ int Engine::alloc_and_upload() {
     PD_TRY(up(d_clamped_, cl.data(), cl.size() * 4, "upload clamped"));
     PD_TRY(dalloc(this, allocs_, &d_clamped_disp_, 3 * n_clamped_, err));
     h_clamped_ = clamped_list;
+  }
+
+  if (pv_possible_) {
+    PD_TRY(dalloc(this, allocs_, &d_afd_, 3 * C, err));
+    PD_TRY(mset(d_afd_, 0, 3 * C * 8, "memset applied force density"));
   }
 
   PD_TRY(build_bonds());
@@ -550,11 +576,13 @@ int Engine::alloc_candidates() {
 
 int Engine::launch_step_seq(int cur, cudaStream_t s) {
   DevView v = view(cur);
+  if (reset_possible_) launch_reset_y(v, s);
   if (precision_ == PD_FP64) launch_predict(v, tpb_, s);
   if (torque_possible_) launch_centroids(v, s);
   launch_bp_decide(v, half_skin_, s);
   launch_broadphase(v, bp_, s);
   launch_step_kernel(v, precision_, variant_, s);
+  if (pv_possible_) launch_prescribed(v, s);
   if (stats_) launch_pairwise_count(v, s);
   launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, s);
   return check(cudaGetLastError(), "step launch");
@@ -670,12 +698,18 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
         for (uint64_t i = 0; i < n_clamped_; ++i)
           for (int c = 0; c < 3; ++c) dsp[3 * (uint64_t)h_clamped_[i] + c] = cd[3 * i + c];
       }
-      uint64_t off = 0;
-      for (auto &s : sims_) {
-        uint64_t ns = s.node_offset[s.np];
-        for (uint64_t k = 0; k < ns; ++k)
-          for (int c = 0; c < 3; ++c) curpos[3 * (off + k) + c] = s.pos[3 * k + c] + dsp[3 * (off + k) + c];
-        off += ns;
+      if (reset_possible_) {  // reset_partzero_y moves reference positions on the device
+        std::vector<double> p(3 * N_);
+        PD_TRY(fetch(d_pos_, p.data()));
+        for (uint64_t k = 0; k < 3 * N_; ++k) curpos[k] = p[k] + dsp[k];
+      } else {
+        uint64_t off = 0;
+        for (auto &s : sims_) {
+          uint64_t ns = s.node_offset[s.np];
+          for (uint64_t k = 0; k < ns; ++k)
+            for (int c = 0; c < 3; ++c) curpos[3 * (off + k) + c] = s.pos[3 * k + c] + dsp[3 * (off + k) + c];
+          off += ns;
+        }
       }
     }
   }
@@ -867,6 +901,7 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
     DevView v = view(cur_);
     cudaStream_t s = stream_;
     cudaEventRecord(ev[0], s);
+    if (reset_possible_) launch_reset_y(v, s);
     if (precision_ == PD_FP64) launch_predict(v, tpb_, s);
     if (torque_possible_) launch_centroids(v, s);
     cudaEventRecord(ev[1], s);
@@ -874,6 +909,7 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
     launch_broadphase(v, bp_, s);
     cudaEventRecord(ev[2], s);
     launch_step_kernel(v, precision_, variant_, s);
+    if (pv_possible_) launch_prescribed(v, s);
     cudaEventRecord(ev[3], s);
     if (stats_) launch_pairwise_count(v, s);
     launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, s);
@@ -892,6 +928,18 @@ int Engine::profile(uint32_t nsteps, double *phase_ms) {
   }
   for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
   return rc;
+}
+
+int Engine::get_afd(double *afd) {
+  if (!d_afd_) {
+    std::memset(afd, 0, 3 * N_ * 8);
+    return PD_OK;
+  }
+  std::vector<double> buf(3 * Ncap_);
+  PD_TRY(cpy(buf.data(), d_afd_, 3 * Ncap_ * 8, "read applied force density"));
+  for (uint64_t n = 0; n < N_; ++n)
+    for (int c = 0; c < 3; ++c) afd[3 * n + c] = buf[c * Ncap_ + n];
+  return PD_OK;
 }
 
 int Engine::count_live_bonds(uint64_t *live) {
@@ -1001,6 +1049,8 @@ int Engine::snapshot() {
   reg(d_ss_, (size_t)S_ * sizeof(DevSimState));
   reg(d_cnt_, sizeof(DevCounters));
   reg(d_centroid_, 3ull * P_ * 8);
+  if (reset_possible_) reg(d_pos_, 3 * C * 8);
+  if (d_afd_) reg(d_afd_, 3 * C * 8);
   if (d_clamped_disp_) reg(d_clamped_disp_, 3 * n_clamped_ * 8);
   if (precision_ == PD_FP32C) {
     reg(d_rec_[0], C * sizeof(Rec32));

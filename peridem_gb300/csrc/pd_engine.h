@@ -60,6 +60,13 @@ struct DevSimParams {
   int32_t set_stoppable_index, set_stoppable_ts;
   uint32_t p0, np;            // particle range of this simulation
   uint64_t node0, nnodes;     // node range of this simulation
+  // prescribed velocity of one particle (timeloop.h:684-764); pv_particle -1 = none
+  int32_t pv_particle, set_fix_velocity_ts, fix_mean_x, fix_angular;
+  double pv_mean_x, pv_angular;
+  // reset_partzero_y (timeloop.h:500-535)
+  int32_t reset_y;
+  uint32_t reset_y_ts;
+  double wheel_rad;
 };
 
 // Per-simulation state that changes from step to step.
@@ -70,7 +77,7 @@ struct DevSimState {
   double extf_scale;
   uint32_t t;       // index of the step about to run (1-based, like timeloop.h:395)
   int32_t fracture, self_contact, damping, friction, torque, active;
-  uint32_t pad;
+  int32_t vconstraint;  // enable_velocity_constraint
 };
 
 // Global counters (one block of device memory, read back by pd_get_stats).
@@ -115,7 +122,7 @@ struct DevView {
   // disp/rec are read for this step while disp_next/rec_next receive the next one)
   Rec32 *rec, *rec_next;
   double *disp_next;
-  const uint8_t *clamp_flag;  // 1 for nodes listed in clamped_nodes
+  const uint8_t *clamp_flag;  // FP32 form: 1 for nodes listed in clamped_nodes
   int fused;                  // 1: FP32 form with the fused predictor
   const double *anchor;       // [P][3] anchor of rec[].u (this step)
   double *anchor_next;        // [P][3] anchor of rec_next[].u
@@ -137,6 +144,12 @@ struct DevView {
   const double *centroid;
   DevCounters *cnt;
   int stats;
+  // prescribed velocity: the corrector stores the old acceleration of the particle's nodes
+  // here, k_prescribed turns it into applied_force_density ([3][Ncap], or null)
+  double *afd;
+  // clamped nodes ([P+1] offsets, global node ids) and their predicted displacement (FP64 form)
+  const uint32_t *clamped_ptr, *clamped_list;
+  const double *clamped_disp;
 };
 
 // Broad-phase scratch (hashed cell list).
@@ -200,6 +213,8 @@ class Engine {
   int profile(uint32_t nsteps, double *phase_ms);
   // Live directed bonds of movable particles (popcount of the live masks).
   int count_live_bonds(uint64_t *live);
+  // applied_force_density (N*3, file order); zeros when no particle has a prescribed velocity.
+  int get_afd(double *afd);
   // ---- batches of independent simulations (one launch per phase covers all of them) ----
   uint32_t num_sims() const { return S_; }
   int sim_range(uint32_t sim, uint64_t *node0, uint64_t *n_nodes, uint32_t *particle0, uint32_t *n_particles) const;
@@ -305,6 +320,8 @@ class Engine {
   uint32_t *d_clamped_ = nullptr;  // [P+1] offsets followed by global node ids
   double *d_clamped_disp_ = nullptr;
   uint64_t n_clamped_ = 0;
+  double *d_afd_ = nullptr;
+  bool pv_possible_ = false, reset_possible_ = false;
   BroadPhase bp_;
   std::vector<void *> allocs_;
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
@@ -326,6 +343,8 @@ void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
+void launch_prescribed(const DevView &v, cudaStream_t s);
+void launch_reset_y(const DevView &v, cudaStream_t s);
 
 }  // namespace pdg
 #endif

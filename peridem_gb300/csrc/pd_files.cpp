@@ -211,6 +211,14 @@ int pd_write_frame(pd_sim *s, uint32_t counter) {
   int rc = s->eng.get_state(cur.data(), vel.data(), acc.data(), force.data(), nullptr);
   if (rc != PD_OK) return rc;
   const auto &hs = s->eng.sims()[0];
+  // applied_force_density of the prescribed-velocity particle (timeloop.h:844-848)
+  const int32_t pvp = s->cfg.particle_w_fixed_velocity;
+  std::vector<double> afd;
+  if (pvp >= 0 && (uint32_t)pvp < P) {
+    afd.resize(3 * N);
+    rc = s->eng.get_afd(afd.data());
+    if (rc != PD_OK) return rc;
+  }
   h5lite::Writer w;
   for (uint32_t p = 0; p < P; ++p) {
     const uint64_t a = hs.node_offset[p], n = hs.node_offset[p + 1] - a;
@@ -219,6 +227,7 @@ int pd_write_frame(pd_sim *s, uint32_t counter) {
     w.add(g + "vel", h5lite::F64, {n, 3}, vel.data() + 3 * a);
     w.add(g + "acc", h5lite::F64, {n, 3}, acc.data() + 3 * a);
     w.add(g + "force", h5lite::F64, {n, 3}, force.data() + 3 * a);
+    if (!afd.empty() && p == (uint32_t)pvp) w.add(g + "applied_force_density", h5lite::F64, {n, 3}, afd.data() + 3 * a);
     uint64_t m = 0;
     rc = s->eng.get_connectivity(p, nullptr, 0, &m);
     if (rc != PD_OK) return rc;

@@ -213,8 +213,10 @@ __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
 }
 
 // U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register
-// cap); W: 256-bit record loads.
-template <int U, int MINB, int W>
+// cap); W: 256-bit record loads; PF: the next group's column indices and live masks are
+// loaded before this group's partner records, so that the column stream's latency overlaps
+// the gathers and arithmetic of the current group.
+template <int U, int MINB, int W, int PF>
 __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
@@ -239,12 +241,35 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
     const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
     const Rec32 *__restrict__ rec = v.rec;
     int j = 0;
-    for (; j + U <= dg; j += U) {
-      uint32_t q[U], m[U];
+    uint32_t qn[U], mn[U];
+    if (PF && U <= dg) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        q[u] = __ldg(colp + 32 * (j + u));
-        m[u] = maskp[j + u];
+        qn[u] = __ldg(colp + 32 * u);
+        mn[u] = maskp[u];
+      }
+    }
+    for (; j + U <= dg; j += U) {
+      uint32_t q[U], m[U];
+      if (PF) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          q[u] = qn[u];
+          m[u] = mn[u];
+        }
+        if (j + 2 * U <= dg) {
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            qn[u] = __ldg(colp + 32 * (j + U + u));
+            mn[u] = maskp[j + U + u];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          q[u] = __ldg(colp + 32 * (j + u));
+          m[u] = maskp[j + u];
+        }
       }
       float4 pq[U], uq[U];
 #pragma unroll
@@ -289,6 +314,7 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
     if (movable) {
       // velocity-Verlet corrector (timeloop.h:670-682)
       const D3 ao = an;
+      if (v.afd && st.vconstraint && (int32_t)(k - sp.p0) == sp.pv_particle) st3(v.afd, nn, C3, ao);
       an = P.irho * f;
       vo = vi + sp.hdt * (ao + an);
       if (clamped) {  // timeloop.h:767-774
@@ -361,10 +387,9 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
   if (v.P) k_anchor_next<<<(v.P + 127) / 128, 128, 0, s>>>(v);
 }
 
-// Bond-kernel variants the autotuner chooses from: {positions per load group, min blocks/SM,
-// 256-bit record loads}.
-const int kBondVariants[][3] = {{4, 6, 1}, {4, 6, 0}, {2, 8, 1}, {4, 4, 1}, {8, 4, 1}, {1, 8, 1}, {4, 1, 1}};
-const int kNumBondVariants = 7;
+// Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
+// 256-bit record loads, column prefetch>.
+const int kNumBondVariants = 9;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -374,13 +399,15 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   k_extra32<<<(unsigned)blocks, 128, 0, s>>>(v);
   const unsigned b = (unsigned)blocks;
   switch (variant) {
-    case 1: k_bond32<4, 6, 0><<<b, 128, 0, s>>>(v); break;
-    case 2: k_bond32<2, 8, 1><<<b, 128, 0, s>>>(v); break;
-    case 3: k_bond32<4, 4, 1><<<b, 128, 0, s>>>(v); break;
-    case 4: k_bond32<8, 4, 1><<<b, 128, 0, s>>>(v); break;
-    case 5: k_bond32<1, 8, 1><<<b, 128, 0, s>>>(v); break;
-    case 6: k_bond32<4, 1, 1><<<b, 128, 0, s>>>(v); break;
-    default: k_bond32<4, 6, 1><<<b, 128, 0, s>>>(v); break;
+    case 1: k_bond32<4, 6, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 2: k_bond32<2, 8, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<4, 4, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 4: k_bond32<8, 4, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 5: k_bond32<1, 8, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 6: k_bond32<4, 6, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 7: k_bond32<8, 4, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 8: k_bond32<4, 4, 1, 1><<<b, 128, 0, s>>>(v); break;
+    default: k_bond32<4, 6, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
 

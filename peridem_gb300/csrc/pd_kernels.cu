@@ -234,6 +234,7 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
     D3 vo = vi;
     if (P.movable) {
       const D3 ao = ld3(v.acc, nn, C3);
+      if (v.afd && st.vconstraint && (int32_t)(k - sp.p0) == sp.pv_particle) st3(v.afd, nn, C3, ao);
       const D3 an = P.irho * f;
       D3 tmp = ao + an;
       tmp = sp.hdt * tmp;
@@ -352,6 +353,7 @@ __device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint3
   if (sp.set_damping_ts != -1 && t == (uint32_t)sp.set_damping_ts) st.damping = 1;
   if (sp.set_zero_wall_speed_ts != -1 && t == (uint32_t)sp.set_zero_wall_speed_ts)
     for (int c = 0; c < 6; ++c) st.spd[c] = 0;
+  if (sp.set_fix_velocity_ts != -1 && t == (uint32_t)sp.set_fix_velocity_ts) st.vconstraint = 1;
   if (sp.gradient_extforce) {
     double sc = (double)t / (double)sp.extforce_maxstep;
     if (sc > 1) sc = 1;
@@ -413,6 +415,169 @@ __global__ void k_centroids(DevView v) {
 
 void launch_centroids(const DevView &v, cudaStream_t s) {
   if (v.P) k_centroids<<<v.P, 32, 0, s>>>(v);
+}
+
+// Prescribed velocity of one particle per simulation, after the corrector (timeloop.h:684-764):
+// the particle's velocity is split into its mean and the rest; the mean's x component
+// (fix_velocity_mean_x) and the rest (fix_velocity_angular: rotation about z at the
+// prescribed rate, about mean_CurrPos) are replaced. applied_force_density =
+// rho*((2/dt)*(pv - vel) - acc_old) - force, with vel already equal to pv (as in the
+// reference). The means are sequential sums in node order, like Eigen's += loop.
+__global__ void k_prescribed(DevView v) {
+  const uint32_t s = blockIdx.x;
+  if (s >= v.S) return;
+  const DevSimParams &sp = v.sp[s];
+  const DevSimState &st = v.ss[s];
+  if (!st.active || !st.vconstraint || sp.pv_particle < 0) return;
+  const uint32_t k = sp.p0 + (uint32_t)sp.pv_particle;
+  const DevPart &P = v.parts[k];
+  if (!P.movable) return;
+  const uint64_t C3 = v.Ncap;
+  __shared__ double sh[6];
+  if (threadIdx.x == 0) {
+    D3 mv = d3(0.0, 0.0, 0.0), mp = d3(0.0, 0.0, 0.0);
+    for (uint32_t i = 0; i < P.n; ++i) mv = mv + ld3(v.vel_out, P.g0 + i, C3);
+    const double nn = (double)P.n;
+    mv = d3(mv.x / nn, mv.y / nn, mv.z / nn);
+    if (sp.fix_angular) {  // mean_CurrPos (particle2.h:94-103)
+      for (uint32_t i = 0; i < P.n; ++i) mp = mp + (ld3(v.pos, P.g0 + i, C3) + ld3(v.disp, P.g0 + i, C3));
+      mp = d3(mp.x / nn, mp.y / nn, mp.z / nn);
+    }
+    sh[0] = mv.x;
+    sh[1] = mv.y;
+    sh[2] = mv.z;
+    sh[3] = mp.x;
+    sh[4] = mp.y;
+    sh[5] = mp.z;
+  }
+  __syncthreads();
+  const double two_dt = 2 / sp.dt;
+  float i2 = 0.f;
+  for (uint32_t i = threadIdx.x; i < P.n; i += blockDim.x) {
+    const uint64_t g = P.g0 + i;
+    const D3 vel = ld3(v.vel_out, g, C3);
+    D3 mean = d3(sh[0], sh[1], sh[2]);
+    D3 vrot = vel - mean;
+    if (sp.fix_mean_x) mean.x = sp.pv_mean_x;
+    if (sp.fix_angular) {
+      const D3 rv = (ld3(v.pos, g, C3) + ld3(v.disp, g, C3)) - d3(sh[3], sh[4], sh[5]);
+      const double r = norm3(rv);
+      D3 ru = d3(0.0, 0.0, 0.0);
+      if (r > 0) ru = d3(rv.x / r, rv.y / r, rv.z / r);
+      const double rw = r * sp.pv_angular;
+      vrot = d3(-rw * ru.y, rw * ru.x, 0.0);
+    }
+    const D3 pv = vrot + mean;
+    const bool clamped32 = v.fused && v.clamp_flag[g];  // FP32 form: clamped nodes already at rest
+    if (!clamped32) st3(v.vel_out, g, C3, pv);
+    const D3 dd = pv - pv;
+    const D3 a = (two_dt * dd) - ld3(v.afd, g, C3);
+    st3(v.afd, g, C3, (P.rho * a) - ld3(v.force, g, C3));
+    if (v.fused && !clamped32) {
+      // the fused predictor of the FP32 form ran with the velocity before the overwrite
+      const D3 d = ld3(v.disp, g, C3);
+      const D3 an = ld3(v.acc, g, C3);
+      const D3 inc = sp.dt * pv + sp.hdt2 * an;
+      const D3 dn = d + inc;
+      st3(v.disp_next, g, C3, dn);
+      const double *anx = v.anchor_next + 3 * (uint64_t)k;
+      v.rec_next[g].u = make_float4((float)(dn.x - anx[0]), (float)(dn.y - anx[1]), (float)(dn.z - anx[2]), 0.f);
+      const float ix = (float)(dn.x - d.x), iy = (float)(dn.y - d.y), iz = (float)(dn.z - d.z);
+      i2 = fmaxf(i2, ix * ix + iy * iy + iz * iz);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) i2 = fmaxf(i2, __shfl_xor_sync(0xffffffffu, i2, o));
+  if ((threadIdx.x & 31) == 0 && i2 > 0.f) {
+    const double inc = sqrt((double)i2) * (1.0 + 1e-5);
+    atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(inc));
+  }
+}
+
+void launch_prescribed(const DevView &v, cudaStream_t s) {
+  if (v.S && v.afd) k_prescribed<<<v.S, 256, 0, s>>>(v);
+}
+
+// reset_partzero_y at the top of step t (timeloop.h:500-535): particle 0 is lifted so that its
+// mean y sits wheel_rad + contact radius above the highest node of the other particles within
+// wheel_rad (in x) of its mean x. The displacement read here is the one after the previous
+// corrector (clamped nodes at zero).
+__device__ __forceinline__ D3 disp_after_corrector(const DevView &v, uint64_t g, uint32_t t) {
+  if (v.fused) {  // FP32 form: the previous step's buffer keeps clamped nodes' prediction
+    if (t > 1 && v.clamp_flag[g]) return d3(0.0, 0.0, 0.0);
+    return ld3(v.disp_next, g, v.Ncap);
+  }
+  return ld3(v.disp, g, v.Ncap);
+}
+
+__global__ void k_reset_y(DevView v) {
+  const uint32_t s = blockIdx.x;
+  if (s >= v.S) return;
+  const DevSimParams &sp = v.sp[s];
+  const DevSimState &st = v.ss[s];
+  if (!st.active || !sp.reset_y || st.t != sp.reset_y_ts) return;
+  const uint64_t C3 = v.Ncap;
+  const DevPart &P0 = v.parts[sp.p0];
+  const DevPart &P1 = v.parts[sp.p0 + 1];
+  __shared__ double m0[3];
+  __shared__ unsigned long long best;
+  __shared__ int found;
+  __shared__ double move;
+  if (threadIdx.x == 0) {
+    D3 m = d3(0.0, 0.0, 0.0);
+    for (uint32_t i = 0; i < P0.n; ++i)
+      m = m + (ld3(v.pos, P0.g0 + i, C3) + disp_after_corrector(v, P0.g0 + i, st.t));
+    const double nn = (double)P0.n;
+    m0[0] = m.x / nn;
+    m0[1] = m.y / nn;
+    m0[2] = m.z / nn;
+    best = ord_key(-INFINITY);
+    found = 0;
+  }
+  __syncthreads();
+  // highest y among the other particles' nodes near particle 0's mean x (an exact max)
+  const uint64_t a = P1.g0, b = sp.node0 + sp.nnodes;
+  double my = -INFINITY;
+  int any = 0;
+  for (uint64_t g = a + threadIdx.x; g < b; g += blockDim.x) {
+    const D3 now = ld3(v.pos, g, C3) + disp_after_corrector(v, g, st.t);
+    if (fabs(m0[0] - now.x) <= sp.wheel_rad) {
+      any = 1;
+      my = fmax(my, now.y);
+    }
+  }
+  if (any) {
+    atomicMax(&best, ord_key(my));
+    found = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double max_bulk_y;
+    if (found) {
+      max_bulk_y = ord_val(best);
+    } else {  // the reference's initial value: pos[0] of particle 1 plus disp[1]
+      const uint64_t j = P1.n > 1 ? 1 : 0;
+      max_bulk_y = v.pos[P1.g0 + C3] + disp_after_corrector(v, P1.g0 + j, st.t).y;
+    }
+    const double dest = (max_bulk_y + sp.wheel_rad) + sp.Rc;
+    move = dest - m0[1];
+    if (v.fused) {  // the FP32 form keeps positions relative to the particle's anchor
+      DevPart &Pw = v.parts[sp.p0];
+      Pw.anchor_pos[1] = Pw.anchor_pos[1] + move;
+      float *wl = v.wall_local + 6 * (uint64_t)sp.p0;
+      const double *an = v.anchor + 3 * (uint64_t)sp.p0;
+      for (int f = 0; f < 6; ++f) {
+        const int c = f % 3;
+        wl[f] = (float)(st.wall[f] - (Pw.anchor_pos[c] + an[c]));
+      }
+    }
+  }
+  __syncthreads();
+  double *py = const_cast<double *>(v.pos) + C3;
+  for (uint32_t i = threadIdx.x; i < P0.n; i += blockDim.x) py[P0.g0 + i] = py[P0.g0 + i] + move;
+}
+
+void launch_reset_y(const DevView &v, cudaStream_t s) {
+  if (v.S) k_reset_y<<<v.S, 256, 0, s>>>(v);
 }
 
 // gen_xi (particle2.h:241-257): xi = pos[q] - pos[i], |xi| and RN(1/|xi|) per SELL entry.

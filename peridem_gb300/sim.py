@@ -87,6 +87,11 @@ class Sim:
         self._ck(lib().pd_get_disp(self.h, ptr(out["disp"])))
         return out
 
+    def applied_force_density(self) -> np.ndarray:
+        out = np.empty((self.N, 3))
+        self._ck(lib().pd_get_applied_force_density(self.h, ptr(out)))
+        return out
+
     def set_state(self, disp=None, vel=None, acc=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (disp, vel, acc)]
         self._ck(lib().pd_set_state(self.h, *(ptr(a) for a in arrs)))

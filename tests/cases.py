@@ -56,10 +56,21 @@ def bdry_only(steps=30):
     return s, cfg
 
 
+def prescribed(steps=30):
+    """Prescribed velocity of particle 0 (mean x velocity and angular velocity about z, from
+    step 4 on), and reset_partzero_y moving particle 0 above the other particle at step 9."""
+    s, cfg = gen.two_sphere(R=0.3 * MM, h=0.1 * MM, v=15.0, steps=steps, walls=True)
+    cfg.update(particle_w_fixed_velocity=0, set_fix_velocity_timestep=4, fix_velocity_mean_x=1,
+               prescribed_velocity_mean_x=-2.5, fix_velocity_angular=1, prescribed_angular_vel=2.0e4,
+               reset_partzero_y=1, reset_partzero_y_timestep=9, wheel_rad=0.35 * MM, compute_wall_reaction=1)
+    return s, cfg
+
+
 CASES = {
     "impact_walls": impact_walls,
     "impact_free": impact_free,
     "cubes_gravity": cubes_gravity,
     "toggles": toggles,
     "bdry_only": bdry_only,
+    "prescribed": prescribed,
 }

@@ -3,7 +3,8 @@
 Runs the reference's run/simulate3d.cpp main() (built from the reference sources against
 stand-in Eigen/MPI/HDF5 headers, oracle/_ref) on each case of tests/cases.py with
 save_file = 1 and stores, per saved frame, what the reference writes to tc_%05u.h5 and
-wall_%05u.h5 (CurrPos, vel, acc, force, Connectivity per particle; wall_info, reaction), next
+wall_%05u.h5 (CurrPos, vel, acc, force, Connectivity per particle, applied_force_density of a
+prescribed-velocity particle; wall_info, reaction), next
 to the setup arrays and the main.conf values used, so that tests on machines without the
 reference sources can check against the reference's own results.
 
@@ -44,6 +45,9 @@ def make(name: str) -> Path:
         parts = frames[c]["particles"]
         for key in ("CurrPos", "vel", "acc", "force"):
             out[f"f{c}_{key}"] = np.concatenate([p[key] for p in parts], axis=0)
+        for pi, p in enumerate(parts):  # written for the prescribed-velocity particle only
+            if "applied_force_density" in p:
+                out[f"f{c}_afd_p{pi}"] = p["applied_force_density"]
         conns = [np.asarray(p["Connectivity"], dtype=np.int64).reshape(-1, 2) for p in parts]
         out[f"f{c}_conn_offset"] = np.concatenate([[0], np.cumsum([len(x) for x in conns])]).astype(np.int64)
         out[f"f{c}_conn"] = np.concatenate(conns, axis=0) if conns else np.zeros((0, 2), np.int64)
@@ -71,6 +75,7 @@ def load(name: str) -> dict:
         f = {k: z[f"f{c}_{k}"] for k in ("CurrPos", "vel", "acc", "force", "conn_offset", "conn", "wall_info")}
         if f"f{c}_reaction" in z:
             f["reaction"] = z[f"f{c}_reaction"]
+        f["afd"] = {int(k.rsplit("_p", 1)[1]): z[k] for k in z.files if k.startswith(f"f{c}_afd_p")}
         frames[c] = f
     return {"setup": s, "config": cfg, "frames": frames}
 

@@ -10,8 +10,11 @@ from tests import cases
 NAMES = sorted(cases.CASES)
 
 
-def _check(name, g, t, counter, curpos, vel, acc, force, conn_fn, wall, reaction):
+def _check(name, g, t, counter, curpos, vel, acc, force, conn_fn, wall, reaction, afd=None):
     f = g["frames"][counter]
+    for p, ref in f.get("afd", {}).items():
+        sl = g["setup"].particle_slice(p)
+        np.testing.assert_array_equal(afd[sl], ref, err_msg=f"{name} frame {counter} applied_force_density")
     np.testing.assert_array_equal(curpos, f["CurrPos"], err_msg=f"{name} frame {counter} CurrPos")
     np.testing.assert_array_equal(vel, f["vel"], err_msg=f"{name} frame {counter} vel")
     np.testing.assert_array_equal(acc, f["acc"], err_msg=f"{name} frame {counter} acc")
@@ -38,7 +41,8 @@ def test_oracle_matches_reference_golden(name):
         t += cfg["modulo"]
         st = orc.state()
         w, r = orc.wall()
-        _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], orc.connectivity, w, r)
+        _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], orc.connectivity, w, r,
+               orc.afd())
 
 
 @pytest.mark.gpu
@@ -54,5 +58,6 @@ def test_gpu_fp64_matches_reference_golden(name):
         t += cfg["modulo"]
         st = sim.state()
         w, r = sim.wall()
-        _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], sim.connectivity, w, r)
+        _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], sim.connectivity, w, r,
+               sim.applied_force_density())
     sim.close()

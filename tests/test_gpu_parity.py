@@ -29,6 +29,7 @@ def _compare_exact(name, s, sim, orc, t):
     scale = max(1e-300, np.abs(ro).max())
     assert np.abs(rg - ro).max() <= 1e-12 * scale, f"{name} reaction"
     np.testing.assert_array_equal(sim.aabb(), orc.aabb())
+    np.testing.assert_array_equal(sim.applied_force_density(), orc.afd(), err_msg=f"{name} t={t} afd")
 
 
 @pytest.mark.parametrize("name", sorted(cases.CASES))
@@ -90,7 +91,7 @@ def test_two_sphere_full_size_bitexact():
         np.testing.assert_array_equal(a[k], b[k])
 
 
-@pytest.mark.parametrize("name", ["impact_free", "cubes_gravity", "impact_walls"])
+@pytest.mark.parametrize("name", ["impact_free", "cubes_gravity", "impact_walls", "prescribed"])
 def test_fp32c_within_tolerance(name):
     s, cfg = cases.CASES[name]()
     steps = cfg["timesteps"]

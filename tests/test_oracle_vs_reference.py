@@ -32,6 +32,9 @@ def test_oracle_matches_reference(name):
             for kr, ko in (("CurrPos", "curpos"), ("vel", "vel"), ("acc", "acc"), ("force", "force")):
                 np.testing.assert_array_equal(ref[p][kr], st[ko][sl], err_msg=f"{name} t={t} p={p} {kr}")
             np.testing.assert_array_equal(ref[p]["Connectivity"], orc.connectivity(p).astype(np.int64))
+            if "applied_force_density" in ref[p]:
+                np.testing.assert_array_equal(ref[p]["applied_force_density"], orc.afd()[sl],
+                                              err_msg=f"{name} t={t} p={p} applied_force_density")
         w, r = orc.wall()
         np.testing.assert_array_equal(frames[cnt]["wall"]["wall_info"].ravel(), w)
         if frames[cnt]["wall"]["reaction"] is not None:
