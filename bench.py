@@ -439,6 +439,8 @@ def ours(args):
     if not args.no_accuracy:
         acc_dyn.append(accuracy_run("two_sphere", args.acc_steps_c0))
         acc_dyn.append(accuracy_run("cubes125", args.acc_steps_c1, steps=args.acc_steps_c1))
+        if args.acc_steps_c2 > 0:
+            acc_dyn.append(accuracy_run(args.workload, args.acc_steps_c2))
 
     # ---- serving stream (continuous batching), rank 0 at N=1 only
     serving = None
@@ -488,6 +490,7 @@ def main():
     ap.add_argument("--variant", type=int, default=-1, help="bond-kernel variant (default: autotune)")
     ap.add_argument("--acc-steps-c0", type=int, default=2000)
     ap.add_argument("--acc-steps-c1", type=int, default=4000)
+    ap.add_argument("--acc-steps-c2", type=int, default=0, help="also compare both forms on the bench workload")
     ap.add_argument("--serve", type=int, default=256, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-chunk", type=int, default=500)
     ap.add_argument("--serve-max-batch", type=int, default=32)

@@ -23,17 +23,33 @@
 
 namespace pdg {
 
-__global__ void __launch_bounds__(128) k_extra32(DevView v) {
-  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N) return;
+// Whether node n has any FP64 non-bond work this step: contact candidates, a wall within the
+// contact radius (FP32 test in the particle's frame, slightly widened), external force or
+// torque.
+__device__ __forceinline__ bool extra_needed(const DevView &v, uint64_t n, uint32_t k, const DevPart &P,
+                                             const DevSimParams &sp, const DevSimState &st, const float4 &pl,
+                                             const float4 &ul) {
+  const bool mov = P.movable != 0;
+  if (v.cand_n[n] != 0 || st.torque || (mov && P.has_ext)) return true;
+  if (mov && P.stoppable && sp.allow_wall) {
+    const float cx = pl.x + ul.x, cy = pl.y + ul.y, cz = pl.z + ul.z;
+    const float *wl = v.wall_local + 6 * (uint64_t)k;
+    const float lim = (float)sp.Rc * 1.001f;
+    return fabsf(cx - wl[0]) <= lim || fabsf(cx - wl[3]) <= lim || fabsf(cy - wl[1]) <= lim ||
+           fabsf(cy - wl[4]) <= lim || fabsf(cz - wl[2]) <= lim || fabsf(cz - wl[5]) <= lim;
+  }
+  return false;
+}
+
+// FP64 non-bond force density of node n in the reference's order: self-contact
+// (timeloop.h:554-557), walls (contact.h:1060-1124), external force and torque
+// (timeloop.h:582-633), then contact with the other particles in ascending partner order
+// (timeloop.h:637-651). Kept out of line: the bond kernel calls it only for nodes that need it.
+__device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
   const uint32_t k = v.pid[n];
   const DevPart &P = v.parts[k];
   const DevSimParams &sp = v.sp[P.sim];
   DevSimState &st = v.ss[P.sim];
-  if (!st.active) {
-    v.extra_flag[n] = 0;
-    return;
-  }
   const int nc = v.cand_n[n];
   const bool mov = P.movable != 0;
   bool wall_near = false;
@@ -46,10 +62,6 @@ __global__ void __launch_bounds__(128) k_extra32(DevView v) {
                 fabsf(cy - wl[4]) <= lim || fabsf(cz - wl[2]) <= lim || fabsf(cz - wl[5]) <= lim;
   }
   const bool ext = mov && P.has_ext;
-  if (nc == 0 && !wall_near && !ext && !st.torque) {
-    v.extra_flag[n] = 0;
-    return;
-  }
   const uint64_t C3 = v.Ncap;
   const D3 di = ld3(v.disp, n, C3), pi = ld3(v.pos, n, C3), vi = ld3(v.vel_in, n, C3);
   const double voli = v.vol[n];
@@ -153,7 +165,22 @@ __global__ void __launch_bounds__(128) k_extra32(DevView v) {
       }
     }
   }
-  st3(v.f_extra, n, C3, f);
+  return f;
+}
+
+// Separate-kernel form: the FP64 non-bond force of every node that has some, for the bond
+// kernel to add (f_extra, extra_flag).
+__global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t k = v.pid[n];
+  const DevPart &P = v.parts[k];
+  const DevSimState &st = v.ss[P.sim];
+  if (!st.active || !extra_needed(v, n, k, P, v.sp[P.sim], st, v.rec[n].p, v.rec[n].u)) {
+    v.extra_flag[n] = 0;
+    return;
+  }
+  st3(v.f_extra, n, v.Ncap, extra_force(v, n));
   v.extra_flag[n] = 1;
 }
 
@@ -213,11 +240,12 @@ __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
 }
 
 // U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register
-// cap); W: 256-bit record loads; PF: the next group's column indices and live masks are
-// loaded before this group's partner records, so that the column stream's latency overlaps
-// the gathers and arithmetic of the current group.
-template <int U, int MINB, int W, int PF>
-__global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
+// cap); W: 256-bit record loads; PF: the column indices and live masks of the next PF groups
+// are loaded ahead of this group's partner records, so that the column stream's latency
+// overlaps the gathers and arithmetic of the current group; FX: the FP64 non-bond work is
+// done here (extra_force) instead of in a separate k_extra32 launch.
+template <int U, int MINB, int W, int PF, int FX>
+__global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
   const uint64_t nn = valid ? n : 0;
@@ -241,27 +269,40 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
     const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
     const Rec32 *__restrict__ rec = v.rec;
     int j = 0;
-    uint32_t qn[U], mn[U];
-    if (PF && U <= dg) {
+    // column indices and live masks of the next PF groups, loaded ahead (static indices only,
+    // so that the ring stays in registers)
+    uint32_t qb[PF > 0 ? PF : 1][U], mb[PF > 0 ? PF : 1][U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        qn[u] = __ldg(colp + 32 * u);
-        mn[u] = maskp[u];
+    for (int d = 0; d < PF; ++d) {
+      if ((d + 1) * U <= dg) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          qb[d][u] = __ldg(colp + 32 * (d * U + u));
+          mb[d][u] = maskp[d * U + u];
+        }
       }
     }
     for (; j + U <= dg; j += U) {
       uint32_t q[U], m[U];
-      if (PF) {
+      if (PF > 0) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          q[u] = qn[u];
-          m[u] = mn[u];
+          q[u] = qb[0][u];
+          m[u] = mb[0][u];
         }
-        if (j + 2 * U <= dg) {
+#pragma unroll
+        for (int d = 0; d + 1 < PF; ++d) {
 #pragma unroll
           for (int u = 0; u < U; ++u) {
-            qn[u] = __ldg(colp + 32 * (j + U + u));
-            mn[u] = maskp[j + U + u];
+            qb[d][u] = qb[d + 1][u];
+            mb[d][u] = mb[d + 1][u];
+          }
+        }
+        if (j + (PF + 1) * U <= dg) {
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
+            mb[PF - 1][u] = maskp[j + PF * U + u];
           }
         }
       } else {
@@ -303,7 +344,11 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(DevView v) {
   float i2 = 0.f;  // squared displacement increment of the next step (broad-phase bound)
   if (run) {
     D3 f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
-    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, C3);
+    if (FX) {  // the non-bond work of k_extra32, fused (same arithmetic, same order)
+      if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
+    } else if (v.extra_flag[nn]) {
+      f = f + ld3(v.f_extra, nn, C3);
+    }
     st3(v.force, nn, C3, f);
     if (nonfinite(f.x) || nonfinite(f.y) || nonfinite(f.z)) atomicOr(&v.cnt->err, PD_DERR_NONFINITE);
     const D3 vi = ld3(v.vel_in, nn, C3);
@@ -389,25 +434,27 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
 // 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 9;
+const int kNumBondVariants = 10;
 
 int num_bond_variants() { return kNumBondVariants; }
 
 void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
-  k_extra32<<<(unsigned)blocks, 128, 0, s>>>(v);
   const unsigned b = (unsigned)blocks;
+  const bool fused_extra = variant >= 6;
+  if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
   switch (variant) {
-    case 1: k_bond32<4, 6, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 2: k_bond32<2, 8, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 3: k_bond32<4, 4, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 4: k_bond32<8, 4, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 5: k_bond32<1, 8, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 6: k_bond32<4, 6, 1, 1><<<b, 128, 0, s>>>(v); break;
-    case 7: k_bond32<8, 4, 1, 1><<<b, 128, 0, s>>>(v); break;
-    case 8: k_bond32<4, 4, 1, 1><<<b, 128, 0, s>>>(v); break;
-    default: k_bond32<4, 6, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 1: k_bond32<4, 6, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 2: k_bond32<4, 4, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<2, 6, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
+    case 4: k_bond32<8, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 5: k_bond32<4, 4, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 6: k_bond32<4, 4, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 7: k_bond32<4, 4, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
+    case 8: k_bond32<4, 6, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 9: k_bond32<2, 6, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
+    default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
 
