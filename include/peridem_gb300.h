@@ -280,6 +280,19 @@ int pd_get_sim_state(pd_sim *sim, uint32_t i, double *curpos, double *vel, doubl
 int pd_get_sim_disp(pd_sim *sim, uint32_t i, double *disp);
 int pd_get_sim_wall(pd_sim *sim, uint32_t i, double *wall_info, double *reaction);
 
+/* ---- bond lists on the GPU (setup generation) -----------------------------------------
+ * For each particle p (nodes [node_offset[p], node_offset[p+1]) of pos, N*3), every node pair
+ * (i, j), i < j, particle-local indices, with ((dx*dx + dy*dy) + dz*dz) <= r*r, r = radius[p],
+ * sorted by (i, j): the Connectivity the reference's setup scripts build with
+ * sorted(cKDTree(pos).query_pairs(delta)) (exp_dict.py:542-567), pair for pair where scipy
+ * evaluates that expression without fused multiply-adds (its x86 builds).
+ * pair_offset (n_particles+1) receives the pair count prefix; with pairs == NULL only the
+ * counts are computed, otherwise cap must hold pair_offset[n_particles] pairs (PD_EINVAL if
+ * not). Runs on the current device. Errors: pd_pairs_error(). */
+int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double *radius,
+                   uint32_t n_particles, uint32_t *pairs, uint64_t cap, uint64_t *pair_offset);
+const char *pd_pairs_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@ UNITS = [
     ("pd_broadphase.cu", []),
     ("pd_fp32c.cu", []),
     ("pd_noalloc.cu", []),
+    ("pd_pairs.cu", ["-fmad=false"]),
     ("pd_engine.cu", ["-fmad=false"]),
     ("pd_capi.cpp", []),
     ("pd_batch.cpp", []),

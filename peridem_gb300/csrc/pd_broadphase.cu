@@ -48,13 +48,15 @@ __device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double c
 }
 
 // Decide whether this step rebuilds; also zero the wall reactions of every simulation
-// (Wall.setzero_reaction at the top of each step, timeloop.h:397).
-__global__ void k_bp_decide(DevView v, double half_skin) {
+// (Wall.setzero_reaction at the top of each step, timeloop.h:397). Inside the step graph the
+// decision also sets the conditional node that runs the rebuild kernels.
+__global__ void k_bp_decide(DevView v, double half_skin, cudaGraphConditionalHandle cond) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t == 0) {
     DevCounters &c = *v.cnt;
     double stepmax = __longlong_as_double((long long)c.stepmax_bits);
     c.rebuild = (c.moved + stepmax > half_skin) ? 1u : 0u;
+    if (cond) cudaGraphSetConditional(cond, c.rebuild);
     c.contacts = 0;    // per-step counters
     c.live_bonds = 0;
   }
@@ -226,8 +228,8 @@ void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s) {
   }
 }
 
-void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s) {
-  k_bp_decide<<<1, 128, 0, s>>>(v, half_skin);
+void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s, cudaGraphConditionalHandle cond) {
+  k_bp_decide<<<1, 128, 0, s>>>(v, half_skin, cond);
 }
 
 }  // namespace pdg

@@ -588,6 +588,68 @@ int Engine::launch_step_seq(int cur, cudaStream_t s) {
   return check(cudaGetLastError(), "step launch");
 }
 
+int Engine::capture_conditional(int cur, cudaGraphExec_t *out) {
+  cudaStream_t cs = capture_stream_;
+  DevView v = view(cur);
+  // the rebuild kernels as a graph of their own
+  cudaGraph_t gb = nullptr, g = nullptr;
+  PD_TRY(check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture"));
+  launch_broadphase(v, bp_, cs);
+  PD_TRY(check(cudaStreamEndCapture(cs, &gb), "end capture"));
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  cudaGraphConditionalHandle h = 0;
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  bool capturing = e == cudaSuccess;
+  if (capturing) {
+    if (reset_possible_) launch_reset_y(v, cs);
+    if (precision_ == PD_FP64) launch_predict(v, tpb_, cs);
+    if (torque_possible_) launch_centroids(v, cs);
+    launch_bp_decide(v, half_skin_, cs, h);
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *ed = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, &ed, &nd);
+    std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+    cudaGraphNode_t cond = nullptr;
+    if (e == cudaSuccess) {
+      // zeroed storage: the struct's union makes its default constructor unavailable
+      alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+      std::memset(raw, 0, sizeof(raw));
+      cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(raw);
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      e = cudaGraphAddNode(&cond, g, dv.data(), nullptr, dv.size(), &cp);
+      if (e == cudaSuccess) {
+        cudaGraphNode_t child;
+        e = cudaGraphAddChildGraphNode(&child, cp.conditional.phGraph_out[0], nullptr, 0, gb);
+      }
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) {
+      launch_step_kernel(v, precision_, variant_, cs);
+      if (pv_possible_) launch_prescribed(v, cs);
+      if (stats_) launch_pairwise_count(v, cs);
+      launch_end_step(v, d_clamped_, n_clamped_, d_clamped_disp_, cs);
+    }
+    cudaGraph_t done = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cs, &done);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  cudaGraphDestroy(gb);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return PD_ECUDA;
+  }
+  return PD_OK;
+}
+
 int Engine::capture_graphs() {
   for (int i = 0; i < 2; ++i) {
     if (graph_[i]) {
@@ -595,6 +657,20 @@ int Engine::capture_graphs() {
       graph_[i] = nullptr;
     }
   }
+  bool cond_ok = use_conditional_;
+  for (int i = 0; i < 2 && cond_ok; ++i)
+    if (capture_conditional(i, &graph_[i]) != PD_OK) cond_ok = false;
+  if (cond_ok) {
+    graphs_ok_ = true;
+    return PD_OK;
+  }
+  for (int i = 0; i < 2; ++i) {
+    if (graph_[i]) {
+      cudaGraphExecDestroy(graph_[i]);
+      graph_[i] = nullptr;
+    }
+  }
+  use_conditional_ = false;
   for (int i = 0; i < 2; ++i) {
     cudaGraph_t g;
     PD_TRY(check(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "begin capture"));

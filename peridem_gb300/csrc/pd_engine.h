@@ -249,6 +249,9 @@ class Engine {
   int launch_step_seq(int cur, cudaStream_t s);
   int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
+  // One step graph whose broad-phase rebuild kernels sit in a conditional node set by
+  // k_bp_decide (0 on success; falls back to the plain graph when unsupported).
+  int capture_conditional(int cur, cudaGraphExec_t *out);
   int check(cudaError_t e, const char *what);
   // Copy / memset ordered on the engine's stream, then a wait for that stream only (never
   // the legacy default stream, so other handles' work keeps running).
@@ -269,6 +272,7 @@ class Engine {
   bool torque_possible_ = false;
   bool stats_ = false;
   bool use_graphs_ = true;
+  bool use_conditional_ = true;  // broad phase in a conditional graph node
   int variant_ = 0;
   std::vector<std::pair<void *, size_t>> mutable_;  // device buffers that change while stepping
   void *backup_ = nullptr;
@@ -338,7 +342,7 @@ void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamp
 void launch_centroids(const DevView &v, cudaStream_t s);
 void launch_bond_constants(const DevView &v, double *bxi, double *bxin, double *brxin, cudaStream_t s);
 void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s);
-void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s);
+void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s, cudaGraphConditionalHandle cond = 0);
 void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);

@@ -72,8 +72,46 @@ def lattice(kind: str, size, h: float) -> np.ndarray:
     return P[keep]
 
 
+_BOND_BUILDER = "cpu"
+
+
+def set_bond_builder(kind: str):
+    """'cpu': scipy cKDTree (the reference's own call); 'gpu': pd_query_pairs on the current
+    CUDA device (the same pairs, tested equal)."""
+    global _BOND_BUILDER
+    if kind not in ("cpu", "gpu"):
+        raise ValueError(kind)
+    _BOND_BUILDER = kind
+
+
+def bonds_gpu(positions: list, radii: list) -> list:
+    """Pair lists of several point sets in one GPU call (pd_query_pairs): for each set, the
+    sorted (i, j), i < j, with |x_i - x_j| <= r."""
+    import ctypes as C
+    from ._capi import lib, ptr
+    L = lib()
+    P = len(positions)
+    off = np.zeros(P + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(x) for x in positions])
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=np.float64).reshape(-1, 3) for x in positions])
+                               if P else np.zeros((0, 3)))
+    rad = np.ascontiguousarray(radii, dtype=np.float64)
+    po = np.zeros(P + 1, dtype=np.uint64)
+    rc = L.pd_query_pairs(ptr(pos), ptr(off), ptr(rad), P, None, 0, ptr(po))
+    if rc != 0:
+        raise RuntimeError(f"pd_query_pairs: [{rc}] {L.pd_pairs_error().decode()}")
+    M = int(po[-1])
+    out = np.zeros((max(M, 1), 2), dtype=np.uint32)
+    rc = L.pd_query_pairs(ptr(pos), ptr(off), ptr(rad), P, ptr(out), M, ptr(po))
+    if rc != 0:
+        raise RuntimeError(f"pd_query_pairs: [{rc}] {L.pd_pairs_error().decode()}")
+    return [out[int(po[p]):int(po[p + 1])].copy() for p in range(P)]
+
+
 def bonds(pos: np.ndarray, delta: float) -> np.ndarray:
     """sorted(cKDTree(pos).query_pairs(delta)) as an (M,2) array (exp_dict.py:544-567)."""
+    if _BOND_BUILDER == "gpu":
+        return bonds_gpu([pos], [delta])[0]
     from scipy.spatial import cKDTree
     pr = cKDTree(pos).query_pairs(delta, output_type="ndarray")
     if len(pr) == 0:
