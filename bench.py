@@ -178,6 +178,7 @@ def time_device(sim, K: int, W: int, dist, torch):
     if W:
         sim.step(W)
     live0 = sim.live_bonds()
+    sim.rebuilds_before = sim.stats()["rebuilds"]
     barrier(dist)
     torch.cuda.synchronize()
     a = torch.cuda.Event(enable_timing=True)
@@ -190,6 +191,7 @@ def time_device(sim, K: int, W: int, dist, torch):
     sim.sync()
     ms = a.elapsed_time(b)
     live1 = sim.live_bonds()
+    sim.rebuilds_timed = sim.stats()["rebuilds"] - sim.rebuilds_before
     return ms, live0, live1
 
 
@@ -370,6 +372,7 @@ def ours(args):
     with Clocks(lr) as clk:
         ms, live0, live1 = time_device(sim, K, W, dist, torch)
     clocks = clk.summary()
+    graph_mode = sim.graph_mode()
     ms = max_over_ranks(dist, ms)
     bu = K * 0.5 * (live0 + live1)
     value = sum_over_ranks(dist, bu) / (ms * 1e-3)
@@ -447,7 +450,12 @@ def ours(args):
     if r == 0 and world == 1 and args.serve > 0:
         serving = serving_run(args)
 
-    launches_per_step = 13  # predict, decide, 7 broad-phase (early exit unless due), extra32, bond32, 2 end
+    # our kernels per step: bp_decide, k_extra32 (unless fused), k_bond32, k_end_sims,
+    # k_end_particles; the 7 broad-phase kernels run only in rebuild steps when the step graph
+    # holds them in a conditional node, else every step (exiting at once unless due)
+    per_step = 5 if variant_ms is None or variant < 6 else 4
+    bp = 7 * (sim.rebuilds_timed if graph_mode == 2 else K)
+    gpu_launches = per_step * K + bp
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -464,7 +472,8 @@ def ours(args):
                      "phase_ms": {"predict": ph[0], "broadphase": ph[1], "step": ph[2], "end": ph[3]}},
         "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64, "accuracy_vs_fp64": acc,
         "accuracy_dynamic": acc_dyn, "serving": serving,
-        "gpu_launches": launches_per_step * K, "clocks": clocks,
+        "gpu_launches": gpu_launches, "broadphase_rebuilds_timed": sim.rebuilds_timed, "clocks": clocks,
+        "graph_mode": {0: "separate launches", 1: "step graph", 2: "step graph, conditional broad phase"}.get(graph_mode),
     }
     sim.close()
     if r == 0:

@@ -233,6 +233,9 @@ int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);
+/* How steps are launched: 0 separate launches, 1 one CUDA graph per step, 2 a step graph whose
+ * broad-phase rebuild kernels sit in a conditional node (after the first pd_step). */
+int pd_graph_mode(const pd_sim *sim);
 /* Copy of all device state that stepping changes, and its restore (checkpoint in HBM). */
 int pd_snapshot(pd_sim *sim);
 int pd_restore(pd_sim *sim);

@@ -117,6 +117,7 @@ SIGNATURES = [
     ("pd_autotune", C.c_int, [_P, _u32, C.POINTER(C.c_int), _P]),
     ("pd_set_variant", C.c_int, [_P, C.c_int]),
     ("pd_num_variants", C.c_int, []),
+    ("pd_graph_mode", C.c_int, [_P]),
     ("pd_snapshot", C.c_int, [_P]),
     ("pd_restore", C.c_int, [_P]),
     ("pd_resume", C.c_int, [_P, _u32, C.c_int]),

@@ -32,6 +32,7 @@ UNITS = [
     ("pd_engine.cu", ["-fmad=false"]),
     ("pd_capi.cpp", []),
     ("pd_batch.cpp", []),
+    ("pd_frames.cpp", []),
     ("pd_config.cpp", []),
     ("pd_files.cpp", []),
     ("h5lite.cpp", []),

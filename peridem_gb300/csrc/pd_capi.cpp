@@ -265,6 +265,8 @@ int pd_set_variant(pd_sim *s, int variant) {
 
 int pd_num_variants(void) { return pdg::num_bond_variants(); }
 
+int pd_graph_mode(const pd_sim *s) { return s ? s->eng.graph_mode() : -1; }
+
 int pd_snapshot(pd_sim *s) {
   if (!s) return fail_global(PD_EINVAL, "null handle");
   return s->eng.snapshot();

@@ -128,6 +128,7 @@ struct DevView {
   double *anchor_next;        // [P][3] anchor of rec_next[].u
   double break_band;     // relative band around snot where the FP64 stretch decides
   double *f_extra;       // [3][Ncap] FP64 non-bond force density of flagged nodes
+  double *f_bond;        // [3][Ncap] bond-force sums of the split bond kernel
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
   float *wall_local;     // [P][6] wall planes in each particle's local frame
   unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
@@ -161,6 +162,21 @@ struct BroadPhase {
   uint16_t *cand_n = nullptr;
   uint32_t cand_cap = 0;
   double skin_frac = 0.5;
+};
+
+// A frame's worth of device state in pinned host memory, copied in stream order: the copies
+// run after the step that produced the state and before later steps overwrite it, so the
+// step pipeline does not stop for output (timeloop.h:801-953 writes synchronously).
+struct HostFrame {
+  double *disp = nullptr, *vel = nullptr, *acc = nullptr, *force = nullptr;  // [3][Ncap]
+  double *pos = nullptr;    // [3][Ncap], only when reference positions can move
+  double *cdisp = nullptr;  // [n_clamped][3] predicted displacement of clamped nodes
+  double *afd = nullptr;    // [3][Ncap], only with a prescribed-velocity particle
+  uint32_t *mask = nullptr; // live masks
+  struct DevSimState *ss = nullptr;
+  struct DevCounters *cnt = nullptr;
+  uint64_t steps = 0;       // steps done when staged
+  cudaEvent_t done = nullptr;
 };
 
 // Host-side description of one simulation (setup + resolved config).
@@ -215,6 +231,17 @@ class Engine {
   int count_live_bonds(uint64_t *live);
   // applied_force_density (N*3, file order); zeros when no particle has a prescribed velocity.
   int get_afd(double *afd);
+  // ---- output frames off the critical path (pd_frames.cpp) ----
+  int frame_alloc(HostFrame &f);
+  void frame_free(HostFrame &f);
+  // Enqueues the copies of the current state into f and an event after them; also restarts
+  // the pairwise counter (as get_stats does). Returns at once.
+  int frame_stage(HostFrame &f);
+  // After f.done: the arrays get_state / get_connectivity / get_wall / get_afd would return.
+  void frame_state(const HostFrame &f, double *curpos, double *vel, double *acc, double *force,
+                   double *afd) const;
+  void frame_connectivity(const HostFrame &f, uint32_t particle, std::vector<uint32_t> &pairs) const;
+  void frame_wall(const HostFrame &f, uint32_t sim, double *wall_info, double *reaction) const;
   // ---- batches of independent simulations (one launch per phase covers all of them) ----
   uint32_t num_sims() const { return S_; }
   int sim_range(uint32_t sim, uint64_t *node0, uint64_t *n_nodes, uint32_t *particle0, uint32_t *n_particles) const;
@@ -235,6 +262,8 @@ class Engine {
   uint64_t num_nodes() const { return N_; }
   uint32_t num_particles() const { return P_; }
   uint64_t steps_done() const { return steps_done_; }
+  // 0: separate launches, 1: step graph, 2: step graph with the conditional broad phase
+  int graph_mode() const { return !use_graphs_ ? 0 : (graphs_ok_ && use_conditional_ ? 2 : 1); }
   cudaStream_t stream() const { return stream_; }
   int precision() const { return precision_; }
   // Device view of the state between steps (what the next step reads).
@@ -297,6 +326,7 @@ class Engine {
   std::vector<uint16_t> h_deg_;
   std::vector<uint32_t> h_g0_;
   std::vector<uint32_t> h_clamped_;
+  std::vector<uint32_t> h_col_;  // SELL column indices, read back once for staged frames
 
   // device buffers
   double *d_pos_ = nullptr, *d_disp_ = nullptr, *d_vel_[2] = {nullptr, nullptr}, *d_acc_ = nullptr;
@@ -312,7 +342,7 @@ class Engine {
   uint32_t *d_col_ = nullptr, *d_mask_ = nullptr;
   double *d_bxi_ = nullptr, *d_bxin_ = nullptr, *d_brxin_ = nullptr;
   double *d_anchor_ = nullptr;
-  double *d_f_extra_ = nullptr;
+  double *d_f_extra_ = nullptr, *d_f_bond_ = nullptr;
   uint8_t *d_extra_flag_ = nullptr;
   float *d_wall_local_ = nullptr;
   unsigned int *d_lrtb_local_ = nullptr;

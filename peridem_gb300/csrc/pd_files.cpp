@@ -5,16 +5,21 @@
 // small C API over h5lite so that scripts can write setup files and read frames.
 #include <sys/stat.h>
 
-#include <chrono>
-#include <cstdio>
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <ctime>
+#include <deque>
 #include <fstream>
+#include <functional>
 #include <iomanip>
 #include <iostream>
+#include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 
 #include "h5lite.h"
 #include "pd_sim.h"
@@ -203,6 +208,162 @@ int pd_open(const char *conf, const char *setup_h5, const char *outdir, int prec
   return PD_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// tc_%05u.h5 and wall_%05u.h5 of one frame from host arrays (timeloop.h:801-953).
+int write_frame_files(pd_sim *s, uint32_t counter, const double *cur, const double *vel, const double *acc,
+                      const double *force, const double *afd,
+                      const std::function<int(uint32_t, std::vector<uint32_t> &)> &conn, const double *wall,
+                      const double *react) {
+  const uint32_t P = s->eng.num_particles();
+  const auto &hs = s->eng.sims()[0];
+  const int32_t pvp = s->cfg.particle_w_fixed_velocity;
+  h5lite::Writer w;
+  std::vector<uint32_t> pairs;
+  for (uint32_t p = 0; p < P; ++p) {
+    const uint64_t a = hs.node_offset[p], n = hs.node_offset[p + 1] - a;
+    const std::string g = pnum(p) + "/";
+    w.add(g + "CurrPos", h5lite::F64, {n, 3}, cur + 3 * a);
+    w.add(g + "vel", h5lite::F64, {n, 3}, vel + 3 * a);
+    w.add(g + "acc", h5lite::F64, {n, 3}, acc + 3 * a);
+    w.add(g + "force", h5lite::F64, {n, 3}, force + 3 * a);
+    // applied_force_density of the prescribed-velocity particle (timeloop.h:844-848)
+    if (afd && pvp >= 0 && p == (uint32_t)pvp) w.add(g + "applied_force_density", h5lite::F64, {n, 3}, afd + 3 * a);
+    int rc = conn(p, pairs);
+    if (rc != PD_OK) return rc;
+    w.add(g + "Connectivity", h5lite::U32, {pairs.size() / 2, 2}, pairs.data());
+  }
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "/tc_%05u.h5", counter);
+  std::string err;
+  if (!w.write(s->outdir + buf, err)) return fail(PD_EIO, err);
+  h5lite::Writer ww;
+  ww.add("wall_info", h5lite::F64, {6, 1}, wall);
+  if (s->cfg.compute_wall_reaction) ww.add("reaction", h5lite::F64, {6, 3}, react);
+  std::snprintf(buf, sizeof(buf), "/wall_%05u.h5", counter);
+  if (!ww.write(s->outdir + buf, err)) return fail(PD_EIO, err);
+  return PD_OK;
+}
+
+// Frames of pd_run off the critical path: the main thread stages a frame (copies enqueued on
+// the engine's stream, pinned destination) and goes on stepping; this thread waits for the
+// copies, builds the arrays of the frame on the host and writes the files. Two staging slots.
+class FrameWriter {
+ public:
+  using Done = std::function<void(uint32_t counter, uint32_t t, const pdg::HostFrame &)>;
+  FrameWriter(pd_sim *s, Done done) : s_(s), done_(std::move(done)) {}
+  ~FrameWriter() { finish(); }
+
+  int start(int nslots) {
+    slots_.resize(nslots);
+    for (auto &f : slots_) {
+      int rc = s_->eng.frame_alloc(f);
+      if (rc != PD_OK) return fail(rc, s_->eng.err);
+      free_.push_back(&f);
+    }
+    th_ = std::thread([this] { run(); });
+    return PD_OK;
+  }
+
+  // Main thread: stage the engine's current state as frame `counter` (after step t).
+  int submit(uint32_t counter, uint32_t t) {
+    pdg::HostFrame *f = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(m_);
+      cv_.wait(lk, [&] { return !free_.empty() || rc_ != PD_OK; });
+      if (rc_ != PD_OK) return rc_;
+      f = free_.front();
+      free_.pop_front();
+    }
+    int rc = s_->eng.frame_stage(*f);
+    if (rc != PD_OK) return fail(rc, s_->eng.err);
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      jobs_.push_back({f, counter, t});
+    }
+    cv_.notify_all();
+    return PD_OK;
+  }
+
+  // Waits for every staged frame to be written; returns the first error.
+  int finish() {
+    if (th_.joinable()) {
+      {
+        std::lock_guard<std::mutex> lk(m_);
+        stop_ = true;
+      }
+      cv_.notify_all();
+      th_.join();
+    }
+    for (auto &f : slots_) s_->eng.frame_free(f);
+    slots_.clear();
+    return rc_;
+  }
+
+ private:
+  struct Job {
+    pdg::HostFrame *f;
+    uint32_t counter, t;
+  };
+
+  void run() {
+    const uint64_t N = s_->eng.num_nodes();
+    std::vector<double> cur(3 * N), vel(3 * N), acc(3 * N), force(3 * N), afd;
+    for (;;) {
+      Job j;
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return !jobs_.empty() || stop_; });
+        if (jobs_.empty()) return;
+        j = jobs_.front();
+        jobs_.pop_front();
+      }
+      int rc = PD_OK;
+      if (cudaEventSynchronize(j.f->done) != cudaSuccess) rc = fail(PD_ECUDA, "staged frame copy failed");
+      if (rc == PD_OK && j.f->cnt->err)  // the device error word (non-finite force, list overflow)
+        rc = fail(PD_EDEVICE, "device error word " + std::to_string(j.f->cnt->err) + " at step " + std::to_string(j.t));
+      if (rc == PD_OK) {
+        const pdg::HostFrame &f = *j.f;
+        if (f.afd) afd.resize(3 * N);
+        s_->eng.frame_state(f, cur.data(), vel.data(), acc.data(), force.data(), f.afd ? afd.data() : nullptr);
+        double wall[6], react[18];
+        s_->eng.frame_wall(f, 0, wall, react);
+        rc = write_frame_files(
+            s_, j.counter, cur.data(), vel.data(), acc.data(), force.data(), f.afd ? afd.data() : nullptr,
+            [&](uint32_t p, std::vector<uint32_t> &pairs) {
+              s_->eng.frame_connectivity(f, p, pairs);
+              return PD_OK;
+            },
+            wall, react);
+        if (rc == PD_OK) done_(j.counter, j.t, f);
+      }
+      {
+        std::lock_guard<std::mutex> lk(m_);
+        if (rc != PD_OK && rc_ == PD_OK) rc_ = rc;
+        free_.push_back(j.f);
+      }
+      cv_.notify_all();
+    }
+  }
+
+  pd_sim *s_;
+  Done done_;
+  std::vector<pdg::HostFrame> slots_;
+  std::deque<pdg::HostFrame *> free_;
+  std::deque<Job> jobs_;
+  std::mutex m_;
+  std::condition_variable cv_;
+  std::thread th_;
+  bool stop_ = false;
+  int rc_ = PD_OK;
+};
+
+}  // namespace
+
+extern "C" {
+
 int pd_write_frame(pd_sim *s, uint32_t counter) {
   if (!s) return fail(PD_EINVAL, "null handle");
   const uint64_t N = s->eng.num_nodes();
@@ -210,8 +371,6 @@ int pd_write_frame(pd_sim *s, uint32_t counter) {
   std::vector<double> cur(3 * N), vel(3 * N), acc(3 * N), force(3 * N);
   int rc = s->eng.get_state(cur.data(), vel.data(), acc.data(), force.data(), nullptr);
   if (rc != PD_OK) return rc;
-  const auto &hs = s->eng.sims()[0];
-  // applied_force_density of the prescribed-velocity particle (timeloop.h:844-848)
   const int32_t pvp = s->cfg.particle_w_fixed_velocity;
   std::vector<double> afd;
   if (pvp >= 0 && (uint32_t)pvp < P) {
@@ -219,36 +378,19 @@ int pd_write_frame(pd_sim *s, uint32_t counter) {
     rc = s->eng.get_afd(afd.data());
     if (rc != PD_OK) return rc;
   }
-  h5lite::Writer w;
-  for (uint32_t p = 0; p < P; ++p) {
-    const uint64_t a = hs.node_offset[p], n = hs.node_offset[p + 1] - a;
-    const std::string g = pnum(p) + "/";
-    w.add(g + "CurrPos", h5lite::F64, {n, 3}, cur.data() + 3 * a);
-    w.add(g + "vel", h5lite::F64, {n, 3}, vel.data() + 3 * a);
-    w.add(g + "acc", h5lite::F64, {n, 3}, acc.data() + 3 * a);
-    w.add(g + "force", h5lite::F64, {n, 3}, force.data() + 3 * a);
-    if (!afd.empty() && p == (uint32_t)pvp) w.add(g + "applied_force_density", h5lite::F64, {n, 3}, afd.data() + 3 * a);
-    uint64_t m = 0;
-    rc = s->eng.get_connectivity(p, nullptr, 0, &m);
-    if (rc != PD_OK) return rc;
-    std::vector<uint32_t> conn(2 * m);
-    rc = s->eng.get_connectivity(p, conn.data(), m, &m);
-    if (rc != PD_OK) return rc;
-    w.add(g + "Connectivity", h5lite::U32, {m, 2}, conn.data());
-  }
-  char buf[64];
-  std::snprintf(buf, sizeof(buf), "/tc_%05u.h5", counter);
-  std::string err;
-  if (!w.write(s->outdir + buf, err)) return fail(PD_EIO, err);
   double wall[6], react[18];
   rc = s->eng.get_wall(0, wall, react);
   if (rc != PD_OK) return rc;
-  h5lite::Writer ww;
-  ww.add("wall_info", h5lite::F64, {6, 1}, wall);
-  if (s->cfg.compute_wall_reaction) ww.add("reaction", h5lite::F64, {6, 3}, react);
-  std::snprintf(buf, sizeof(buf), "/wall_%05u.h5", counter);
-  if (!ww.write(s->outdir + buf, err)) return fail(PD_EIO, err);
-  return PD_OK;
+  return write_frame_files(
+      s, counter, cur.data(), vel.data(), acc.data(), force.data(), afd.empty() ? nullptr : afd.data(),
+      [&](uint32_t p, std::vector<uint32_t> &pairs) {
+        uint64_t m = 0;
+        int r = s->eng.get_connectivity(p, nullptr, 0, &m);
+        if (r != PD_OK) return r;
+        pairs.resize(2 * m);
+        return s->eng.get_connectivity(p, pairs.data(), m, &m);
+      },
+      wall, react);
 }
 
 // Sets the kinematic state (and, with enable_fracture, the surviving bonds) from a saved
@@ -353,40 +495,54 @@ int pd_run(pd_sim *s) {
   auto t0 = std::chrono::system_clock::now();
   std::vector<double> run_time, t_ind;
   std::vector<uint32_t> pw_vec;
+  // progress row of each written frame (timeloop.h:909-947), printed by the writer thread
+  FrameWriter fw(s, [&](uint32_t ctr, uint32_t t, const pdg::HostFrame &f) {
+    auto t1 = std::chrono::system_clock::now();
+    const int ms = (int)std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count();
+    t0 = t1;
+    double avg = 0;
+    const int start = (int)run_time.size() - 10;
+    if (start > 0)
+      for (int c = start; c < (int)run_time.size(); ++c) avg += run_time[c];
+    avg /= 10;
+    const int rem = (int)((int)(last_counter - ctr) * avg);
+    char ts[80];
+    time_t nt = time(nullptr);
+    strftime(ts, sizeof(ts), "%F-%T", localtime(&nt));
+    std::cout << std::left << std::setw(cw) << t << std::setw(cw) << ctr << std::setw(cw + 5) << (double)ms / 1000
+              << std::setw(cw) << format_ms(rem) << std::setw(cw) << f.cnt->pairwise << std::setw(cw) << ts
+              << std::endl;
+    run_time.push_back(ms);
+    t_ind.push_back(t);
+    pw_vec.push_back((uint32_t)f.cnt->pairwise);
+  });
+  if (cf.save_file && cf.modulo) {
+    int rc = fw.start(2);
+    if (rc != PD_OK) return rc;
+  }
   uint32_t t = 0;
   while (t < cf.timesteps) {
     uint32_t n = cf.timesteps - t;
     if (cf.save_file && cf.modulo) n = std::min<uint32_t>(n, cf.modulo - (t % cf.modulo));
     int rc = s->eng.step(n);
-    if (rc == PD_OK) rc = s->eng.sync(-1);
-    if (rc != PD_OK) return rc;
+    if (rc != PD_OK) {
+      fw.finish();
+      return rc;
+    }
     t += n;
     if (cf.save_file && cf.modulo && t % cf.modulo == 0) {
-      rc = pd_write_frame(s, counter);
-      if (rc != PD_OK) return rc;
-      pd_stats st;
-      s->eng.get_stats(&st);
-      auto t1 = std::chrono::system_clock::now();
-      const int ms = (int)std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count();
-      t0 = t1;
-      double avg = 0;
-      const int start = (int)run_time.size() - 10;
-      if (start > 0)
-        for (int c = start; c < (int)run_time.size(); ++c) avg += run_time[c];
-      avg /= 10;
-      const int rem = (int)((int)(last_counter - counter) * avg);
-      char ts[80];
-      time_t nt = time(nullptr);
-      strftime(ts, sizeof(ts), "%F-%T", localtime(&nt));
-      std::cout << std::left << std::setw(cw) << t << std::setw(cw) << counter << std::setw(cw + 5)
-                << (double)ms / 1000 << std::setw(cw) << format_ms(rem) << std::setw(cw) << st.pairwise_computations
-                << std::setw(cw) << ts << std::endl;
-      run_time.push_back(ms);
-      t_ind.push_back(t);
-      pw_vec.push_back((uint32_t)st.pairwise_computations);
+      rc = fw.submit(counter, t);
+      if (rc != PD_OK) {
+        fw.finish();
+        return rc;
+      }
       ++counter;
     }
   }
+  int rc = s->eng.sync(-1);
+  const int wrc = fw.finish();
+  if (rc != PD_OK) return rc;
+  if (wrc != PD_OK) return wrc;
   if (is_dir("output/hdf5")) {  // run_time.h5 at the reference's fixed path (timeloop.h:957-964)
     h5lite::Writer w;
     w.add("run_time", h5lite::F64, {run_time.size(), 1}, run_time.data());

@@ -226,6 +226,84 @@ __device__ __forceinline__ float bond32(const float4 &pi, const float4 &ui, cons
   return str;
 }
 
+// Per-node end of the FP32-form step, given the total force density f: force store,
+// velocity-Verlet corrector in FP64 (timeloop.h:670-682), clamped nodes (timeloop.h:767-774),
+// the next step's predictor (timeloop.h:537-540) into disp_next / rec_next, the particle's
+// local-frame AABB of this step and the broad-phase movement bound. Warp-collective.
+__device__ __forceinline__ void verlet_tail(const DevView &v, uint64_t nn, uint32_t k, const DevPart &P,
+                                            const DevSimState &st, bool run, D3 f, const float4 &pi4,
+                                            const float4 &ui4) {
+  const uint64_t C3 = v.Ncap;
+  const int32_t movable = P.movable;
+  float i2 = 0.f;  // squared displacement increment of the next step (broad-phase bound)
+  if (run) {
+    st3(v.force, nn, C3, f);
+    if (nonfinite(f.x) || nonfinite(f.y) || nonfinite(f.z)) atomicOr(&v.cnt->err, PD_DERR_NONFINITE);
+    const D3 vi = ld3(v.vel_in, nn, C3);
+    D3 vo = vi;
+    D3 an = ld3(v.acc, nn, C3);
+    const DevSimParams &sp = v.sp[P.sim];
+    const bool clamped = movable && v.clamp_flag[nn];
+    if (movable) {
+      // velocity-Verlet corrector (timeloop.h:670-682)
+      const D3 ao = an;
+      if (v.afd && st.vconstraint && (int32_t)(k - sp.p0) == sp.pv_particle) st3(v.afd, nn, C3, ao);
+      an = P.irho * f;
+      vo = vi + sp.hdt * (ao + an);
+      if (clamped) {  // timeloop.h:767-774
+        vo = d3(0.0, 0.0, 0.0);
+        an = d3(0.0, 0.0, 0.0);
+      }
+      st3(v.acc, nn, C3, an);
+    }
+    st3(v.vel_out, nn, C3, vo);
+    // predictor of the next step (timeloop.h:537-540)
+    const D3 d = ld3(v.disp, nn, C3);
+    D3 dn;
+    if (clamped) {
+      dn = d3(0.0, 0.0, 0.0);
+    } else {
+      const D3 inc = sp.dt * vo + sp.hdt2 * an;
+      dn = d + inc;
+    }
+    st3(v.disp_next, nn, C3, dn);
+    const float ix = (float)(dn.x - d.x), iy = (float)(dn.y - d.y), iz = (float)(dn.z - d.z);
+    i2 = ix * ix + iy * iy + iz * iz;
+    const double *anx = v.anchor_next + 3 * (uint64_t)k;
+    v.rec_next[nn].u = make_float4((float)(dn.x - anx[0]), (float)(dn.y - anx[1]), (float)(dn.z - anx[2]), 0.f);
+  }
+  // particle AABB of this step's positions in the particle's local frame
+  {
+    const bool contrib = run && movable;
+    const float px = pi4.x + ui4.x, py = pi4.y + ui4.y, pz = pi4.z + ui4.z;
+    float lo[3] = {contrib ? px : INFINITY, contrib ? py : INFINITY, contrib ? pz : INFINITY};
+    float hi[3] = {contrib ? px : -INFINITY, contrib ? py : -INFINITY, contrib ? pz : -INFINITY};
+    const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+    const bool uniform = __all_sync(0xffffffffu, k == k0);
+    if (uniform) {
+      for (int o = 16; o > 0; o >>= 1) {
+        for (int c = 0; c < 3; ++c) {
+          lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+          hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+      }
+    }
+    const bool writer = uniform ? ((threadIdx.x & 31) == 0) : contrib;
+    if (writer && lo[0] <= hi[0]) {
+      unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
+      for (int c = 0; c < 3; ++c) {
+        atomicMin(&L[c], fkey(lo[c]));
+        atomicMax(&L[3 + c], fkey(hi[c]));
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) i2 = fmaxf(i2, __shfl_xor_sync(0xffffffffu, i2, o));
+  if ((threadIdx.x & 31) == 0 && i2 > 0.f) {
+    const double inc = sqrt((double)i2) * (1.0 + 1e-5);
+    atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(inc));
+  }
+}
+
 // A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector.
 template <int W>
 __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
@@ -243,8 +321,9 @@ __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
 // cap); W: 256-bit record loads; PF: the column indices and live masks of the next PF groups
 // are loaded ahead of this group's partner records, so that the column stream's latency
 // overlaps the gathers and arithmetic of the current group; FX: the FP64 non-bond work is
-// done here (extra_force) instead of in a separate k_extra32 launch.
-template <int U, int MINB, int W, int PF, int FX>
+// done here (extra_force) instead of in a separate k_extra32 launch; SPLIT: only the bond sums
+// here (fewer live registers in the gather loop), the FP64 rest in k_verlet32.
+template <int U, int MINB, int W, int PF, int FX, int SPLIT>
 __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
@@ -341,83 +420,44 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ De
       }
     }
   }
-  float i2 = 0.f;  // squared displacement increment of the next step (broad-phase bound)
-  if (run) {
-    D3 f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
-    if (FX) {  // the non-bond work of k_extra32, fused (same arithmetic, same order)
-      if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
-    } else if (v.extra_flag[nn]) {
-      f = f + ld3(v.f_extra, nn, C3);
-    }
-    st3(v.force, nn, C3, f);
-    if (nonfinite(f.x) || nonfinite(f.y) || nonfinite(f.z)) atomicOr(&v.cnt->err, PD_DERR_NONFINITE);
-    const D3 vi = ld3(v.vel_in, nn, C3);
-    D3 vo = vi;
-    D3 an = ld3(v.acc, nn, C3);
-    const DevSimParams &sp = v.sp[P.sim];
-    const bool clamped = movable && v.clamp_flag[nn];
-    if (movable) {
-      // velocity-Verlet corrector (timeloop.h:670-682)
-      const D3 ao = an;
-      if (v.afd && st.vconstraint && (int32_t)(k - sp.p0) == sp.pv_particle) st3(v.afd, nn, C3, ao);
-      an = P.irho * f;
-      vo = vi + sp.hdt * (ao + an);
-      if (clamped) {  // timeloop.h:767-774
-        vo = d3(0.0, 0.0, 0.0);
-        an = d3(0.0, 0.0, 0.0);
-      }
-      st3(v.acc, nn, C3, an);
-    }
-    st3(v.vel_out, nn, C3, vo);
-    // predictor of the next step (timeloop.h:537-540)
-    const D3 d = ld3(v.disp, nn, C3);
-    D3 dn;
-    if (clamped) {
-      dn = d3(0.0, 0.0, 0.0);
-    } else {
-      const D3 inc = sp.dt * vo + sp.hdt2 * an;
-      dn = d + inc;
-    }
-    st3(v.disp_next, nn, C3, dn);
-    const float ix = (float)(dn.x - d.x), iy = (float)(dn.y - d.y), iz = (float)(dn.z - d.z);
-    i2 = ix * ix + iy * iy + iz * iz;
-    const double *anx = v.anchor_next + 3 * (uint64_t)k;
-    v.rec_next[nn].u = make_float4((float)(dn.x - anx[0]), (float)(dn.y - anx[1]), (float)(dn.z - anx[2]), 0.f);
-  }
-  // particle AABB of this step's positions in the particle's local frame
-  {
-    const bool contrib = run && movable;
-    const float px = pi4.x + ui4.x, py = pi4.y + ui4.y, pz = pi4.z + ui4.z;
-    float lo[3] = {contrib ? px : INFINITY, contrib ? py : INFINITY, contrib ? pz : INFINITY};
-    float hi[3] = {contrib ? px : -INFINITY, contrib ? py : -INFINITY, contrib ? pz : -INFINITY};
-    const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
-    const bool uniform = __all_sync(0xffffffffu, k == k0);
-    if (uniform) {
-      for (int o = 16; o > 0; o >>= 1) {
-        for (int c = 0; c < 3; ++c) {
-          lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
-          hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
-        }
+  if (SPLIT) {  // the bond sums go to memory; k_verlet32 finishes the node
+    if (run) st3(v.f_bond, nn, C3, d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy,
+                                      (double)a.sz - (double)a.cz));
+  } else {
+    D3 f = d3(0.0, 0.0, 0.0);
+    if (run) {
+      f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
+      if (FX) {  // the non-bond work of k_extra32, fused (same arithmetic, same order)
+        if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
+      } else if (v.extra_flag[nn]) {
+        f = f + ld3(v.f_extra, nn, C3);
       }
     }
-    const bool writer = uniform ? ((threadIdx.x & 31) == 0) : contrib;
-    if (writer && lo[0] <= hi[0]) {
-      unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
-      for (int c = 0; c < 3; ++c) {
-        atomicMin(&L[c], fkey(lo[c]));
-        atomicMax(&L[3 + c], fkey(hi[c]));
-      }
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) i2 = fmaxf(i2, __shfl_xor_sync(0xffffffffu, i2, o));
-  if ((threadIdx.x & 31) == 0 && i2 > 0.f) {
-    const double inc = sqrt((double)i2) * (1.0 + 1e-5);
-    atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(inc));
+    verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
   }
   if (v.stats) {
     for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
     if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
   }
+}
+
+// Second half of the split form: bond sums from k_bond32<..., SPLIT=1> plus the non-bond
+// force, then the same per-node tail as the fused form.
+__global__ void __launch_bounds__(128) k_verlet32(const __grid_constant__ DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  const uint32_t k = v.pid[nn];
+  const DevPart &P = v.parts[k];
+  const DevSimState &st = v.ss[P.sim];
+  const bool run = valid && st.active;
+  const Rec32 r = v.rec[nn];
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (run) {
+    f = ld3(v.f_bond, nn, v.Ncap);
+    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, v.Ncap);
+  }
+  verlet_tail(v, nn, k, P, st, run, f, r.p, r.u);
 }
 
 // A_next := this step's predicted displacement of each particle's anchor node.
@@ -434,7 +474,7 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
 // 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 10;
+const int kNumBondVariants = 12;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -442,20 +482,30 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
-  const bool fused_extra = variant >= 6;
+  const bool fused_extra = variant >= 6 && variant <= 9;
+  const bool split = variant >= 10 && v.f_bond;
   if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
   switch (variant) {
-    case 1: k_bond32<4, 6, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 2: k_bond32<4, 4, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
-    case 3: k_bond32<2, 6, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
-    case 4: k_bond32<8, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 5: k_bond32<4, 4, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 6: k_bond32<4, 4, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
-    case 7: k_bond32<4, 4, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
-    case 8: k_bond32<4, 6, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
-    case 9: k_bond32<2, 6, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
-    default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 1: k_bond32<4, 6, 1, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 2: k_bond32<4, 4, 1, 2, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<2, 6, 1, 2, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 4: k_bond32<8, 4, 1, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 5: k_bond32<4, 4, 1, 0, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 6: k_bond32<4, 4, 1, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 7: k_bond32<4, 4, 1, 2, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 8: k_bond32<4, 6, 1, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 9: k_bond32<2, 6, 1, 2, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 10:
+      if (split) k_bond32<2, 8, 1, 2, 0, 1><<<b, 128, 0, s>>>(v);
+      else k_bond32<2, 6, 1, 2, 0, 0><<<b, 128, 0, s>>>(v);
+      break;
+    case 11:
+      if (split) k_bond32<4, 6, 1, 2, 0, 1><<<b, 128, 0, s>>>(v);
+      else k_bond32<2, 6, 1, 2, 0, 0><<<b, 128, 0, s>>>(v);
+      break;
+    default: k_bond32<4, 4, 1, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
   }
+  if (split) k_verlet32<<<b, 128, 0, s>>>(v);
 }
 
 }  // namespace pdg

@@ -166,8 +166,11 @@ def read_frame(outdir, counter: int, n_particles: int) -> dict:
     parts = []
     for p in range(n_particles):
         g = "P_%05d/" % p
-        parts.append({k: r.read(g + k) for k in ("CurrPos", "vel", "acc", "force")} |
-                     {"Connectivity": r.read(g + "Connectivity", U32)})
+        d = {k: r.read(g + k) for k in ("CurrPos", "vel", "acc", "force")}
+        d["Connectivity"] = r.read(g + "Connectivity", U32)
+        if r.has(g + "applied_force_density"):
+            d["applied_force_density"] = r.read(g + "applied_force_density")
+        parts.append(d)
     w = Reader(f"{outdir}/wall_{counter:05d}.h5")
     wall = {"wall_info": w.read("wall_info").reshape(-1)}
     if w.has("reaction"):

@@ -141,6 +141,10 @@ class Sim:
     def set_variant(self, v: int):
         self._ck(lib().pd_set_variant(self.h, int(v)))
 
+    def graph_mode(self) -> int:
+        """0 separate launches, 1 step graph, 2 step graph with a conditional broad phase."""
+        return int(lib().pd_graph_mode(self.h))
+
     def snapshot(self):
         self._ck(lib().pd_snapshot(self.h))
 

@@ -1,5 +1,6 @@
 """The drop-in `simulate3d -c main.conf -i setup.h5 -o outdir` (run/simulate3d.cpp) end to end:
-setup file in the reference's schema, main.conf in its grammar, frames out in its layout.
+setup file in the reference's schema, main.conf in its grammar, frames out in its layout
+(staged in stream order and written by a host thread while the steps go on).
 Frames must equal the golden frames PeriDEM's own code wrote for the same case (bit for bit
 in the FP64 form), and a resumed run (do_resume, timeloop.h:262-312) must equal the oracle
 resumed from the same frame."""
@@ -30,7 +31,7 @@ def run_cli(tmp_path, setup, cfg, precision="fp64"):
     return out, r.stdout
 
 
-@pytest.mark.parametrize("name", ["impact_walls", "toggles", "cubes_gravity"])
+@pytest.mark.parametrize("name", ["impact_walls", "toggles", "cubes_gravity", "prescribed"])
 def test_cli_frames_equal_reference_golden(tmp_path, name):
     g = load(name)
     s, cfg = g["setup"], g["config"]
@@ -41,6 +42,8 @@ def test_cli_frames_equal_reference_golden(tmp_path, name):
         parts = fr["particles"]
         for key in ("CurrPos", "vel", "acc", "force"):
             np.testing.assert_array_equal(np.concatenate([p[key] for p in parts]), f[key], err_msg=f"{key} {counter}")
+        for p, ref in f.get("afd", {}).items():
+            np.testing.assert_array_equal(parts[p]["applied_force_density"], ref, err_msg=f"afd {counter}")
         co = f["conn_offset"]
         for p in range(s.n_particles):
             np.testing.assert_array_equal(parts[p]["Connectivity"].astype(np.int64), f["conn"][co[p]:co[p + 1]])
@@ -97,6 +100,31 @@ def test_cli_fp32c_close_to_reference(tmp_path):
     ref = g["frames"][last]["CurrPos"]
     disp_ref = ref - s.pos
     assert np.abs(cur - ref).max() <= 1e-5 * np.abs(disp_ref).max()
+
+
+def test_staged_frames_equal_synchronous_frames(tmp_path):
+    """pd_run's frames (staged copies, writer thread) equal pd_write_frame's (synchronous reads)."""
+    from peridem_gb300 import _capi
+    import ctypes as C
+    g = load("toggles")
+    s, cfg = g["setup"], dict(g["config"])
+    out, _ = run_cli(tmp_path, s, cfg)
+    L = _capi.lib()
+    sync_dir = tmp_path / "sync"
+    sync_dir.mkdir()
+    h = C.c_void_p()
+    assert L.pd_open(str(tmp_path / "main.conf").encode(), str(tmp_path / "setup.h5").encode(),
+                     str(sync_dir).encode(), 0, C.byref(h)) == 0
+    for counter in range(1, cfg["timesteps"] // cfg["modulo"] + 1):
+        assert L.pd_step(h, cfg["modulo"]) == 0
+        assert L.pd_write_frame(h, counter) == 0
+        a = h5.read_frame(out, counter, s.n_particles)
+        b = h5.read_frame(sync_dir, counter, s.n_particles)
+        for pa, pb in zip(a["particles"], b["particles"]):
+            for k in pa:
+                np.testing.assert_array_equal(pa[k], pb[k])
+        np.testing.assert_array_equal(a["wall"]["wall_info"], b["wall"]["wall_info"])
+    L.pd_close(h)
 
 
 def test_cli_missing_setup_fails_cleanly(tmp_path):
