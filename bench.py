@@ -296,6 +296,18 @@ def serving_run(args):
                 peak_device_gb=srv.peak_used / 1e9, setup_gen_s=t_gen, chunk_steps=args.serve_chunk,
                 nodes_mean=float(np.mean([len(r.setup.pos) for r in reqs])),
                 steps_mean=float(np.mean([r.steps for r in reqs])))
+    # capacity: the same requests all waiting at once (cohorts of up to max_batch share launches)
+    if args.serve_burst:
+        srv_b = serve.Server("fp32c", chunk_steps=args.serve_chunk, max_batch=args.serve_max_batch, keep_state=False)
+        t0 = time.perf_counter()
+        res_b = srv_b.run(reqs, realtime=False)
+        wall_b = time.perf_counter() - t0
+        sb = serve.summarize(res_b, wall_b)
+        cb = [e for e in srv_b.log if e[1] == "admit"]
+        summ["all_at_once"] = {k: sb[k] for k in ("completed", "wall_s", "sims_per_hour", "bond_updates_per_s",
+                                                  "ttc_p50_s", "ttc_p99_s")}
+        summ["all_at_once"].update(cohorts=len(cb), max_cohort=max((len(e[2]) for e in cb), default=0),
+                                   peak_device_gb=srv_b.peak_used / 1e9)
     # one at a time, plain FP64: measured per-step time and creation time on a sample spread
     # over the sizes, fitted as linear in directed bonds, then a FIFO queue over the arrivals
     order = np.argsort([2 * len(r.setup.conn) for r in reqs])
@@ -502,6 +514,7 @@ def main():
     ap.add_argument("--acc-steps-c2", type=int, default=0, help="also compare both forms on the bench workload")
     ap.add_argument("--serve", type=int, default=256, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-chunk", type=int, default=500)
+    ap.add_argument("--serve-burst", type=int, default=1, help="also serve the stream with every request waiting at t=0")
     ap.add_argument("--serve-max-batch", type=int, default=32)
     ap.add_argument("--serve-fp64-sample", type=int, default=6)
     ap.add_argument("--serve-fp64-steps", type=int, default=100)

@@ -109,7 +109,6 @@ DevView Engine::view(int cur) const {
   }
   v.break_band = 1e-4;
   v.f_extra = d_f_extra_;
-  v.f_bond = d_f_bond_;
   v.extra_flag = d_extra_flag_;
   v.wall_local = d_wall_local_;
   v.lrtb_local_next = d_lrtb_local_;
@@ -506,7 +505,6 @@ int Engine::alloc_and_upload() {
       PD_TRY(up(d_clamp_flag_, cf.data(), C, "upload clamp flags"));
     }
     PD_TRY(dalloc(this, allocs_, &d_f_extra_, 3 * C, err));
-    PD_TRY(dalloc(this, allocs_, &d_f_bond_, 3 * C, err));
     PD_TRY(dalloc(this, allocs_, &d_extra_flag_, C, err));
     PD_TRY(dalloc(this, allocs_, &d_wall_local_, 6ull * P_, err));
     PD_TRY(dalloc(this, allocs_, &d_lrtb_local_, 6ull * P_, err));

@@ -128,7 +128,6 @@ struct DevView {
   double *anchor_next;        // [P][3] anchor of rec_next[].u
   double break_band;     // relative band around snot where the FP64 stretch decides
   double *f_extra;       // [3][Ncap] FP64 non-bond force density of flagged nodes
-  double *f_bond;        // [3][Ncap] bond-force sums of the split bond kernel
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
   float *wall_local;     // [P][6] wall planes in each particle's local frame
   unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
@@ -342,7 +341,7 @@ class Engine {
   uint32_t *d_col_ = nullptr, *d_mask_ = nullptr;
   double *d_bxi_ = nullptr, *d_bxin_ = nullptr, *d_brxin_ = nullptr;
   double *d_anchor_ = nullptr;
-  double *d_f_extra_ = nullptr, *d_f_bond_ = nullptr;
+  double *d_f_extra_ = nullptr;
   uint8_t *d_extra_flag_ = nullptr;
   float *d_wall_local_ = nullptr;
   unsigned int *d_lrtb_local_ = nullptr;

@@ -321,9 +321,8 @@ __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
 // cap); W: 256-bit record loads; PF: the column indices and live masks of the next PF groups
 // are loaded ahead of this group's partner records, so that the column stream's latency
 // overlaps the gathers and arithmetic of the current group; FX: the FP64 non-bond work is
-// done here (extra_force) instead of in a separate k_extra32 launch; SPLIT: only the bond sums
-// here (fewer live registers in the gather loop), the FP64 rest in k_verlet32.
-template <int U, int MINB, int W, int PF, int FX, int SPLIT>
+// done here (extra_force) instead of in a separate k_extra32 launch.
+template <int U, int MINB, int W, int PF, int FX>
 __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = n < v.N;
@@ -420,44 +419,20 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ De
       }
     }
   }
-  if (SPLIT) {  // the bond sums go to memory; k_verlet32 finishes the node
-    if (run) st3(v.f_bond, nn, C3, d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy,
-                                      (double)a.sz - (double)a.cz));
-  } else {
-    D3 f = d3(0.0, 0.0, 0.0);
-    if (run) {
-      f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
-      if (FX) {  // the non-bond work of k_extra32, fused (same arithmetic, same order)
-        if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
-      } else if (v.extra_flag[nn]) {
-        f = f + ld3(v.f_extra, nn, C3);
-      }
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (run) {
+    f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
+    if (FX) {  // the non-bond work of k_extra32, fused (same arithmetic, same order)
+      if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
+    } else if (v.extra_flag[nn]) {
+      f = f + ld3(v.f_extra, nn, C3);
     }
-    verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
   }
+  verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
   if (v.stats) {
     for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
     if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
   }
-}
-
-// Second half of the split form: bond sums from k_bond32<..., SPLIT=1> plus the non-bond
-// force, then the same per-node tail as the fused form.
-__global__ void __launch_bounds__(128) k_verlet32(const __grid_constant__ DevView v) {
-  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = n < v.N;
-  const uint64_t nn = valid ? n : 0;
-  const uint32_t k = v.pid[nn];
-  const DevPart &P = v.parts[k];
-  const DevSimState &st = v.ss[P.sim];
-  const bool run = valid && st.active;
-  const Rec32 r = v.rec[nn];
-  D3 f = d3(0.0, 0.0, 0.0);
-  if (run) {
-    f = ld3(v.f_bond, nn, v.Ncap);
-    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, v.Ncap);
-  }
-  verlet_tail(v, nn, k, P, st, run, f, r.p, r.u);
 }
 
 // A_next := this step's predicted displacement of each particle's anchor node.
@@ -474,7 +449,7 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
 // 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 12;
+const int kNumBondVariants = 10;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -482,30 +457,20 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
-  const bool fused_extra = variant >= 6 && variant <= 9;
-  const bool split = variant >= 10 && v.f_bond;
+  const bool fused_extra = variant >= 6;
   if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
   switch (variant) {
-    case 1: k_bond32<4, 6, 1, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 2: k_bond32<4, 4, 1, 2, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 3: k_bond32<2, 6, 1, 2, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 4: k_bond32<8, 4, 1, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 5: k_bond32<4, 4, 1, 0, 0, 0><<<b, 128, 0, s>>>(v); break;
-    case 6: k_bond32<4, 4, 1, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 7: k_bond32<4, 4, 1, 2, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 8: k_bond32<4, 6, 1, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 9: k_bond32<2, 6, 1, 2, 1, 0><<<b, 128, 0, s>>>(v); break;
-    case 10:
-      if (split) k_bond32<2, 8, 1, 2, 0, 1><<<b, 128, 0, s>>>(v);
-      else k_bond32<2, 6, 1, 2, 0, 0><<<b, 128, 0, s>>>(v);
-      break;
-    case 11:
-      if (split) k_bond32<4, 6, 1, 2, 0, 1><<<b, 128, 0, s>>>(v);
-      else k_bond32<2, 6, 1, 2, 0, 0><<<b, 128, 0, s>>>(v);
-      break;
-    default: k_bond32<4, 4, 1, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 1: k_bond32<4, 6, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 2: k_bond32<4, 4, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<2, 6, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
+    case 4: k_bond32<8, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 5: k_bond32<4, 4, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
+    case 6: k_bond32<4, 4, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 7: k_bond32<4, 4, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
+    case 8: k_bond32<4, 6, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 9: k_bond32<2, 6, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
+    default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
-  if (split) k_verlet32<<<b, 128, 0, s>>>(v);
 }
 
 }  // namespace pdg
