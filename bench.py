@@ -428,7 +428,10 @@ def ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sim_e = Sim(s, cfg, "fp32c")
+        sim_e.set_variant(variant)
+        tc = time.perf_counter()
         sim_e.step(K)
+        ts = time.perf_counter()
         st = sim_e.state()
         t1 = time.perf_counter()
         e2e_s = max_over_ranks(dist, t1 - t0)
@@ -437,7 +440,8 @@ def ours(args):
         e2e = {"value": sum_over_ranks(dist, K * s.n_bonds_directed) / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                "what": "pd_create_from_arrays (host arrays -> HBM, bond lists built) + K steps + "
-                       "pd_get_state/pd_get_disp to host, wall clock"}
+                       "pd_get_state/pd_get_disp to host, wall clock",
+               "split_s": {"create": tc - t0, "steps": ts - tc, "readback": t1 - ts}}
         sim_e.close()
 
     # ---- CPU baseline (oracle port, bounded sample), rank 0 at N=1 only
@@ -465,7 +469,7 @@ def ours(args):
     # our kernels per step: bp_decide, k_extra32 (unless fused), k_bond32, k_end_sims,
     # k_end_particles; the 7 broad-phase kernels run only in rebuild steps when the step graph
     # holds them in a conditional node, else every step (exiting at once unless due)
-    per_step = 5 if variant_ms is None or variant < 6 else 4
+    per_step = 4 if 6 <= variant <= 9 else 5  # variants 6-9 fuse k_extra32 into the bond kernel
     bp = 7 * (sim.rebuilds_timed if graph_mode == 2 else K)
     gpu_launches = per_step * K + bp
     line = {

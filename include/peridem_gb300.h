@@ -45,6 +45,8 @@ extern "C" {
 #define PD_DERR_NONFINITE 1u      /* a NaN/Inf force density was produced             */
 #define PD_DERR_CAND_OVERFLOW 2u  /* per-node contact candidate list overflowed       */
 #define PD_DERR_CONTACT_OVERFLOW 4u /* more in-range contacts than the per-node cap   */
+#define PD_DERR_STAGE_TIMEOUT 8u    /* a shared-memory staging copy missed its wait limit
+                                       (the block used global loads; results unaffected) */
 
 /*
  * pd_config: the run parameters of `main.conf`. Field names, meanings, defaults and

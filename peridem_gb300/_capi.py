@@ -22,6 +22,7 @@ PD_ETIMEOUT = -5
 PD_EDEVICE = -6
 PD_ECONFIG = -7
 PD_ESTATE = -8
+PD_DERR_STAGE_TIMEOUT = 8
 PD_FP64 = 0
 PD_FP32C = 1
 PD_DERR_NONFINITE = 1

@@ -76,6 +76,7 @@ uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision,
     b += 3 * atleast1(E) * 8 + 2 * atleast1(E) * 8;
   } else {
     b += 2 * C * 32 + 3 * C * 8 + 2 * 3 * P * 8 + C + 3 * C * 8 + C + 2 * 6 * P * 4;
+    b += 2 * 4 * atleast1((N + kStageNodes - 1) / kStageNodes);  // staged-kernel record ranges
   }
   // broad phase
   uint32_t bits = 10;

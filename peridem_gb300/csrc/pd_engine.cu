@@ -109,6 +109,9 @@ DevView Engine::view(int cur) const {
   }
   v.break_band = 1e-4;
   v.f_extra = d_f_extra_;
+  v.win_lo = d_win_lo_;
+  v.win_cnt = d_win_cnt_;
+  v.win_max = win_max_;
   v.extra_flag = d_extra_flag_;
   v.wall_local = d_wall_local_;
   v.lrtb_local_next = d_lrtb_local_;
@@ -242,6 +245,33 @@ int Engine::build_bonds() {
   }
   initial_bonds_ = 0;
   for (uint64_t n = 0; n < N_; ++n) initial_bonds_ += deg[n];
+  if (precision_ == PD_FP32C) {
+    // record ranges of the staged bond kernel: per block of kStageNodes nodes, the smallest
+    // contiguous range holding its own nodes and every partner
+    const uint64_t nb = (N_ + kStageNodes - 1) / kStageNodes;
+    std::vector<uint32_t> wlo(nb), wcnt(nb);
+    win_max_ = 0;
+    for (uint64_t b = 0; b < nb; ++b) {
+      const uint64_t n0 = b * kStageNodes, n1 = std::min<uint64_t>(N_, n0 + kStageNodes);
+      uint64_t lo = n0, hi = n1 - 1;
+      for (uint64_t sl = n0 / 32; sl < (n1 + 31) / 32; ++sl)
+        for (uint64_t e = h_slice_ptr_[sl]; e < h_slice_ptr_[sl + 1]; ++e) {
+          const uint32_t q = col[e];
+          if (q == kNoCol) continue;
+          lo = std::min<uint64_t>(lo, q);
+          hi = std::max<uint64_t>(hi, q);
+        }
+      const uint64_t cnt = hi - lo + 1;
+      wlo[b] = (uint32_t)lo;
+      wcnt[b] = cnt <= kStageMaxRecords ? (uint32_t)cnt : 0u;  // larger ranges read global memory
+      win_max_ = std::max(win_max_, wcnt[b]);
+    }
+    PD_TRY(dalloc(this, allocs_, &d_win_lo_, nb, err));
+    PD_TRY(dalloc(this, allocs_, &d_win_cnt_, nb, err));
+    PD_TRY(cpy(d_win_lo_, wlo.data(), nb * 4, "upload windows"));
+    PD_TRY(cpy(d_win_cnt_, wcnt.data(), nb * 4, "upload windows"));
+    if (win_max_) PD_TRY(prepare_staged_kernels(win_max_ * (uint32_t)sizeof(Rec32)));
+  }
   PD_TRY(dalloc(this, allocs_, &d_slice_ptr_, nslices_ + 1, err));
   PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));
   PD_TRY(dalloc(this, allocs_, &d_col_, col.size(), err));

@@ -34,6 +34,8 @@
 namespace pdg {
 
 constexpr int kSlice = 32;
+constexpr int kStageNodes = 512;          // nodes per block of the staged bond kernel
+constexpr uint32_t kStageMaxRecords = 6400;  // 200 KB of 32-byte records per block
 constexpr uint32_t kNoCol = 0xFFFFFFFFu;
 
 // Per-particle parameters (ParticleN scalars, particle2.h:51-59).
@@ -128,6 +130,10 @@ struct DevView {
   double *anchor_next;        // [P][3] anchor of rec_next[].u
   double break_band;     // relative band around snot where the FP64 stretch decides
   double *f_extra;       // [3][Ncap] FP64 non-bond force density of flagged nodes
+  // FP32 form, staged bond kernel: per block of kStageNodes nodes, the contiguous range of
+  // node records its bonds read ([win_lo, win_lo + win_cnt); win_cnt 0 = not staged)
+  const uint32_t *win_lo, *win_cnt;
+  uint32_t win_max;      // largest staged range (records): the kernel's shared-memory size
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
   float *wall_local;     // [P][6] wall planes in each particle's local frame
   unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
@@ -342,6 +348,8 @@ class Engine {
   double *d_bxi_ = nullptr, *d_bxin_ = nullptr, *d_brxin_ = nullptr;
   double *d_anchor_ = nullptr;
   double *d_f_extra_ = nullptr;
+  uint32_t *d_win_lo_ = nullptr, *d_win_cnt_ = nullptr;
+  uint32_t win_max_ = 0;
   uint8_t *d_extra_flag_ = nullptr;
   float *d_wall_local_ = nullptr;
   unsigned int *d_lrtb_local_ = nullptr;
@@ -366,6 +374,8 @@ void launch_predict(const DevView &v, int tpb, cudaStream_t s);
 void launch_step_kernel(const DevView &v, int precision, int variant, cudaStream_t s);
 void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s);
 int num_bond_variants();
+// Raises the dynamic shared-memory limit of the staged bond kernels (once per engine).
+int prepare_staged_kernels(uint32_t smem_bytes);
 void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
                      cudaStream_t s);
 void launch_centroids(const DevView &v, cudaStream_t s);

@@ -435,6 +435,158 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ De
   }
 }
 
+// Staged form of the bond kernel: one block of kStageNodes nodes first copies the contiguous
+// range of node records its bonds read into shared memory with bulk asynchronous copies
+// (cp.async.bulk, completion on an mbarrier), then gathers every partner from shared memory
+// instead of L1/L2. Blocks whose range does not fit (win_cnt == 0), or whose copy misses the
+// wait limit, read global memory as the plain kernel does; results are the same either way.
+constexpr uint32_t kStageWaitPolls = 1u << 22;  // bounded wait (~0.5 s) for the staging copy
+
+template <int U, int PF>
+__global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constant__ DevView v) {
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  Rec32 *win = reinterpret_cast<Rec32 *>(stage_raw);
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t wlo = v.win_lo[blockIdx.x];
+  const uint32_t wcnt = v.win_cnt[blockIdx.x];
+  bool staged = wcnt != 0;
+  bool copy_done = true;
+  if (staged) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      const uint32_t bytes = wcnt * (uint32_t)sizeof(Rec32);
+      mbar_expect_tx(&bar, bytes);
+      const char *src = reinterpret_cast<const char *>(v.rec + wlo);
+      for (uint32_t off = 0; off < bytes; off += 32768u)
+        bulk_g2s(stage_raw + off, src + off, bytes - off < 32768u ? bytes - off : 32768u, &bar);
+    }
+    __syncthreads();  // the barrier is initialised before anyone polls it
+    copy_done = mbar_wait_bounded(&bar, 0, kStageWaitPolls);
+    staged = __syncthreads_and(copy_done) != 0;
+    if (!staged && threadIdx.x == 0) atomicOr(&v.cnt->err, PD_DERR_STAGE_TIMEOUT);
+  }
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  const uint32_t k = v.pid[nn];
+  const DevPart &P = v.parts[k];
+  const int32_t movable = P.movable;
+  const DevSimState &st = v.ss[P.sim];
+  const bool run = valid && st.active;
+  const uint64_t C3 = v.Ncap;
+  float4 pi4, ui4;
+  ld_rec<1>(v.rec + nn, pi4, ui4);
+  Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  uint32_t live = 0;
+  if (run && movable) {
+    const uint32_t lane = (uint32_t)(nn & 31);
+    const uint64_t sbase = v.slice_ptr[nn >> 5];
+    const uint32_t *colp = v.col + sbase + lane;
+    uint32_t *maskp = v.mask + (sbase >> 5);
+    const int dg = v.deg[nn];
+    const bool brk = st.fracture && P.breakable && P.break_bonds;
+    const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
+    const Rec32 *__restrict__ rec = v.rec;
+    // partner record: shared memory when staged (and inside the staged range), else global
+    auto partner = [&](uint32_t q, float4 &p, float4 &u) {
+      const uint32_t o = q - wlo;
+      if (staged && o < wcnt) {
+        p = win[o].p;
+        u = win[o].u;
+      } else {
+        ld_rec<1>(rec + q, p, u);
+      }
+    };
+    int j = 0;
+    uint32_t qb[PF][U], mb[PF][U];
+#pragma unroll
+    for (int d = 0; d < PF; ++d) {
+      if ((d + 1) * U <= dg) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          qb[d][u] = __ldg(colp + 32 * (d * U + u));
+          mb[d][u] = maskp[d * U + u];
+        }
+      }
+    }
+    for (; j + U <= dg; j += U) {
+      uint32_t q[U], m[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        q[u] = qb[0][u];
+        m[u] = mb[0][u];
+      }
+#pragma unroll
+      for (int d = 0; d + 1 < PF; ++d) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          qb[d][u] = qb[d + 1][u];
+          mb[d][u] = mb[d + 1][u];
+        }
+      }
+      if (j + (PF + 1) * U <= dg) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
+          mb[PF - 1][u] = maskp[j + PF * U + u];
+        }
+      }
+      float4 pq[U], uq[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) partner(q[u], pq[u], uq[u]);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if ((m[u] >> lane) & 1u) {
+          ++live;
+          const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
+          if (brk && str > slo) {
+            if (str > shi) cut_bond(&maskp[j + u], lane);
+            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot);
+          }
+        }
+      }
+    }
+    for (; j < dg; ++j) {
+      const uint32_t mw = maskp[j];
+      if (!((mw >> lane) & 1u)) continue;
+      const uint32_t q = __ldg(colp + 32 * j);
+      ++live;
+      float4 pq, uq;
+      partner(q, pq, uq);
+      const float str = bond32(pi4, ui4, pq, uq, cn, a);
+      if (brk && str > slo) {
+        if (str > shi) cut_bond(&maskp[j], lane);
+        else band_check(v, nn, q, &maskp[j], lane, P.snot);
+      }
+    }
+  }
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (run) {
+    f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
+    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, C3);
+  }
+  verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
+  if (v.stats) {
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
+  }
+  // a copy that missed its wait limit may still be writing shared memory: let it land
+  if (!copy_done && threadIdx.x == 0) (void)mbar_wait_bounded(&bar, 0, kStageWaitPolls);
+  __syncthreads();
+}
+
+int prepare_staged_kernels(uint32_t smem_bytes) {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void *fn) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  };
+  set((const void *)k_bond32s<2, 2>);
+  set((const void *)k_bond32s<4, 2>);
+  set((const void *)k_bond32s<2, 3>);
+  set((const void *)k_bond32s<1, 4>);
+  return e == cudaSuccess ? PD_OK : PD_ECUDA;
+}
+
 // A_next := this step's predicted displacement of each particle's anchor node.
 __global__ void k_anchor_next(DevView v) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -449,7 +601,7 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
 // 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 10;
+const int kNumBondVariants = 14;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -457,8 +609,11 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
-  const bool fused_extra = variant >= 6;
+  const bool fused_extra = variant >= 6 && variant <= 9;
+  if (variant >= 10 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
   if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
+  const unsigned bs = (unsigned)((v.N + kStageNodes - 1) / kStageNodes);
+  const size_t sm = (size_t)v.win_max * sizeof(Rec32);
   switch (variant) {
     case 1: k_bond32<4, 6, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
     case 2: k_bond32<4, 4, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
@@ -469,6 +624,10 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
     case 7: k_bond32<4, 4, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
     case 8: k_bond32<4, 6, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
     case 9: k_bond32<2, 6, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
+    case 10: k_bond32s<2, 2><<<bs, kStageNodes, sm, s>>>(v); break;
+    case 11: k_bond32s<4, 2><<<bs, kStageNodes, sm, s>>>(v); break;
+    case 12: k_bond32s<2, 3><<<bs, kStageNodes, sm, s>>>(v); break;
+    case 13: k_bond32s<1, 4><<<bs, kStageNodes, sm, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
