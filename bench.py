@@ -293,6 +293,8 @@ def serving_run(args):
     summ = serve.summarize(res, wall)
     cohorts = [e for e in srv.log if e[1] == "admit"]
     summ.update(cohorts=len(cohorts), max_cohort=max((len(e[2]) for e in cohorts), default=0),
+                create_s_mean=float(np.mean(srv.create_s)) if srv.create_s else 0.0,
+                create_s_max=float(np.max(srv.create_s)) if srv.create_s else 0.0, finish_s_total=srv.finish_s,
                 peak_device_gb=srv.peak_used / 1e9, setup_gen_s=t_gen, chunk_steps=args.serve_chunk,
                 nodes_mean=float(np.mean([len(r.setup.pos) for r in reqs])),
                 steps_mean=float(np.mean([r.steps for r in reqs])))

@@ -2,6 +2,7 @@
 // pd_engine.h from one or more simulations, captures one step as a CUDA graph and replays
 // it, and reads results back in the reference's shapes.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -186,26 +187,63 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   return alloc_and_upload();
 }
 
+namespace {
+// Runs f(i) for i in [0, n) on the host's cores (work handed out one index at a time).
+template <class F>
+void parallel_items(uint64_t n, F f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned T = (unsigned)std::min<uint64_t>(std::min(hw, 32u), n);
+  if (T <= 1) {
+    for (uint64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<uint64_t> next(0);
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < T; ++t)
+    th.emplace_back([&] {
+      for (uint64_t i = next++; i < n; i = next++) f(i);
+    });
+  for (auto &x : th) x.join();
+}
+}  // namespace
+
 int Engine::build_bonds() {
   // conn2NArr (load_hdf5.h:27-37): for every Connectivity row (i, j) push j onto row i and
-  // i onto row j; rows keep that push order.
-  std::vector<uint32_t> deg(Ncap_, 0);
-  uint64_t gnode = 0;
-  for (auto &s : sims_) {
-    for (uint32_t p = 0; p < s.np; ++p) {
-      uint64_t g0 = gnode + s.node_offset[p];
-      uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
-      for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
-        uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
-        if (i >= nloc || j >= nloc) {
-          err = "Connectivity index out of range in particle " + std::to_string(p);
-          return PD_EINVAL;
-        }
-        deg[g0 + i]++;
-        deg[g0 + j]++;
-      }
+  // i onto row j; rows keep that push order. Particles own disjoint rows, so they are filled
+  // in parallel; the live masks (all bonds live at the start) follow from the degrees alone.
+  struct PartRef {
+    const HostSim *s;
+    uint32_t p;
+    uint64_t g0;
+  };
+  std::vector<PartRef> parts;
+  {
+    uint64_t gnode = 0;
+    for (auto &s : sims_) {
+      for (uint32_t p = 0; p < s.np; ++p) parts.push_back({&s, p, gnode + s.node_offset[p]});
+      gnode += s.node_offset[s.np];
     }
-    gnode += s.node_offset[s.np];
+  }
+  std::vector<uint32_t> deg(Ncap_, 0);
+  std::atomic<int64_t> bad(-1);
+  parallel_items(parts.size(), [&](uint64_t x) {
+    const HostSim &s = *parts[x].s;
+    const uint32_t p = parts[x].p;
+    const uint64_t g0 = parts[x].g0;
+    const uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
+    for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
+      const uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
+      if (i >= nloc || j >= nloc) {
+        bad = (int64_t)p;
+        return;
+      }
+      deg[g0 + i]++;
+      deg[g0 + j]++;
+    }
+  });
+  if (bad >= 0) {
+    err = "Connectivity index out of range in particle " + std::to_string(bad.load());
+    return PD_EINVAL;
   }
   uint32_t maxdeg = 0;
   for (uint64_t n = 0; n < N_; ++n) maxdeg = std::max(maxdeg, deg[n]);
@@ -224,25 +262,30 @@ int Engine::build_bonds() {
   E_ = h_slice_ptr_[nslices_];
   std::vector<uint32_t> col(std::max<uint64_t>(E_, 1), kNoCol);
   std::vector<uint32_t> mask(std::max<uint64_t>(E_ / 32, 1), 0u);
-  std::vector<uint32_t> fill(Ncap_, 0);
-  gnode = 0;
-  for (auto &s : sims_) {
-    for (uint32_t p = 0; p < s.np; ++p) {
-      uint64_t g0 = gnode + s.node_offset[p];
-      for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
-        uint64_t a = g0 + s.conn[2 * l], b = g0 + s.conn[2 * l + 1];
-        uint64_t ea = h_slice_ptr_[a >> 5] + 32ull * fill[a] + (a & 31);
-        col[ea] = (uint32_t)b;
-        mask[(h_slice_ptr_[a >> 5] >> 5) + fill[a]] |= 1u << (a & 31);
-        fill[a]++;
-        uint64_t eb = h_slice_ptr_[b >> 5] + 32ull * fill[b] + (b & 31);
-        col[eb] = (uint32_t)a;
-        mask[(h_slice_ptr_[b >> 5] >> 5) + fill[b]] |= 1u << (b & 31);
-        fill[b]++;
-      }
+  parallel_items(nslices_, [&](uint64_t sl) {
+    // padding entries, and the live bits: position j of lane l is a bond iff j < deg
+    const uint64_t e0 = h_slice_ptr_[sl], e1 = h_slice_ptr_[sl + 1];
+    const uint64_t w = (e1 - e0) / 32;
+    for (uint64_t j = 0; j < w; ++j) {
+      uint32_t bits = 0;
+      for (int l = 0; l < 32; ++l)
+        if (j < deg[sl * 32 + l]) bits |= 1u << l;
+      mask[(e0 >> 5) + j] = bits;
     }
-    gnode += s.node_offset[s.np];
-  }
+  });
+  std::vector<uint32_t> fill(Ncap_, 0);
+  parallel_items(parts.size(), [&](uint64_t x) {
+    const HostSim &s = *parts[x].s;
+    const uint32_t p = parts[x].p;
+    const uint64_t g0 = parts[x].g0;
+    for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
+      const uint64_t a = g0 + s.conn[2 * l], b = g0 + s.conn[2 * l + 1];
+      col[h_slice_ptr_[a >> 5] + 32ull * fill[a] + (a & 31)] = (uint32_t)b;
+      fill[a]++;
+      col[h_slice_ptr_[b >> 5] + 32ull * fill[b] + (b & 31)] = (uint32_t)a;
+      fill[b]++;
+    }
+  });
   initial_bonds_ = 0;
   for (uint64_t n = 0; n < N_; ++n) initial_bonds_ += deg[n];
   if (precision_ == PD_FP32C) {
@@ -251,7 +294,7 @@ int Engine::build_bonds() {
     const uint64_t nb = (N_ + kStageNodes - 1) / kStageNodes;
     std::vector<uint32_t> wlo(nb), wcnt(nb);
     win_max_ = 0;
-    for (uint64_t b = 0; b < nb; ++b) {
+    parallel_items(nb, [&](uint64_t b) {
       const uint64_t n0 = b * kStageNodes, n1 = std::min<uint64_t>(N_, n0 + kStageNodes);
       uint64_t lo = n0, hi = n1 - 1;
       for (uint64_t sl = n0 / 32; sl < (n1 + 31) / 32; ++sl)
@@ -264,8 +307,8 @@ int Engine::build_bonds() {
       const uint64_t cnt = hi - lo + 1;
       wlo[b] = (uint32_t)lo;
       wcnt[b] = cnt <= kStageMaxRecords ? (uint32_t)cnt : 0u;  // larger ranges read global memory
-      win_max_ = std::max(win_max_, wcnt[b]);
-    }
+    });
+    for (uint64_t b = 0; b < nb; ++b) win_max_ = std::max(win_max_, wcnt[b]);
     PD_TRY(dalloc(this, allocs_, &d_win_lo_, nb, err));
     PD_TRY(dalloc(this, allocs_, &d_win_cnt_, nb, err));
     PD_TRY(cpy(d_win_lo_, wlo.data(), nb * 4, "upload windows"));

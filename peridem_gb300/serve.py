@@ -107,6 +107,8 @@ class Server:
         self.peak_used = 0
         self.cohorts: list[_Cohort] = []
         self.log: list[tuple] = []   # (time, event, detail)
+        self.create_s: list[float] = []  # host+device time to build each cohort's handle
+        self.finish_s = 0.0              # time spent reading finished simulations back
 
     # -- admission ------------------------------------------------------------------------
     def _pick(self, waiting: deque, est: dict) -> list:
@@ -120,6 +122,7 @@ class Server:
         return pick
 
     def _create(self, reqs: list, out: dict):
+        t0 = time.perf_counter()
         try:
             b = self.make_batch([r.setup for r in reqs], [dict(r.config, timesteps=r.steps) for r in reqs],
                                 self.precision)
@@ -128,6 +131,7 @@ class Server:
             out["batch"] = b
         except Exception as e:  # reported per request
             out["error"] = str(e)
+        out["create_s"] = time.perf_counter() - t0
 
     # -- main loop ------------------------------------------------------------------------
     def run(self, requests: list[Request], realtime: bool = True, idle_sleep: float = 2e-4) -> list[Result]:
@@ -159,6 +163,7 @@ class Server:
                 th, out, areqs, reserved, ta = admit
                 admit = None
                 busy = True
+                self.create_s.append(out.get("create_s", 0.0))
                 if "batch" in out:
                     b = out["batch"]
                     nb = int(b.device_bytes()) if hasattr(b, "device_bytes") else reserved
@@ -197,10 +202,12 @@ class Server:
                 tdone = now()
                 for i, r in enumerate(c.members):
                     if c.remaining[i] == 0 and i not in c.finished:
+                        tf = time.perf_counter()
                         c.batch.finish(i)
                         st = c.batch.sim_state(i) if self.keep_state else None
                         wl = c.batch.sim_wall(i) if self.keep_state else None
                         c.finished.append(i)
+                        self.finish_s += time.perf_counter() - tf
                         results[r.rid] = Result(r.rid, st, wl, r.arrival if realtime else 0.0, c.admitted, now(),
                                                 r.steps, len(r.setup.pos), directed_bonds(r.setup))
                         self.log.append((tdone, "done", r.rid))
