@@ -60,22 +60,24 @@ def barrier(dist):
         dist.barrier()
 
 
-def max_over_ranks(dist, x: float) -> float:
+def _reduce(dist, x: float, op) -> float:
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(dist, x: float) -> float:
+    """Slowest rank's time: the job's time (replicas run independent simulations)."""
+    return _reduce(dist, x, dist.ReduceOp.MAX) if dist is not None else x
 
 
 def sum_over_ranks(dist, x: float) -> float:
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    """Bond-updates of all ranks: the whole job's work."""
+    return _reduce(dist, x, dist.ReduceOp.SUM) if dist is not None else x
 
 
 def load_workload(name: str):
@@ -410,9 +412,14 @@ def ours(args):
         v64 = sum_over_ranks(dist, K64 * 0.5 * (l0 + l1)) / (ms64 * 1e-3)
         ph64 = sim64.profile(3) / 3
         ach64 = (4.125 * sim64.live_bonds() + 224.0 * s.n_nodes) / (ph64[2] * 1e-3) / 1e9
+        # FP64 operations per bond in k_step, counted from its source: eta (6 add), |eta| (3 mul,
+        # 2 add, IEEE sqrt ~9), stretch (1 add + Markstein division 3), magnitude (2 mul),
+        # RN(1/|eta|) (~5), unit vector (3 divisions, 9), accumulation (3 mul, 3 add), test (1)
+        ops_per_bond = 47
         fp64 = {"value": v64, "unit": UNIT, "steps": K64, "ms_per_step": ms64 / K64,
                 "kernel_ms": ph64[2], "roofline_hbm_frac": ach64 / peak,
-                "note": "bound by FP64 issue rate (sqrt/div per bond), not HBM"}
+                "fp64_ops_per_s": v64 * ops_per_bond, "fp64_ops_per_bond": ops_per_bond,
+                "note": "bound by the FP64 issue rate (sqrt, reciprocal and divisions per bond), not HBM"}
         # accuracy of FP32C vs FP64 after the same number of steps on this workload
         done64 = W + K64 + 3
         if steps32 > done64:
