@@ -307,7 +307,7 @@ class Engine {
   bool stats_ = false;
   bool use_graphs_ = true;
   bool use_conditional_ = true;  // broad phase in a conditional graph node
-  int variant_ = 0;
+  int variant_ = 3;  // FP32 bond-kernel variant (the autotuner's usual choice)
   std::vector<std::pair<void *, size_t>> mutable_;  // device buffers that change while stepping
   void *backup_ = nullptr;
   size_t backup_bytes_ = 0;
