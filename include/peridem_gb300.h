@@ -215,7 +215,10 @@ int pd_close(pd_sim *sim);
 
 /* Tuning knobs: contact skin as a fraction of the contact radius (<= 0 keeps it), per-node
  * candidate capacity (0 keeps it, at most 64), threads per block (<= 0 keeps it), per-step
- * statistics on/off (< 0 keeps it; on adds the pair-count kernel), CUDA-graph replay on/off. */
+ * statistics on/off (< 0 keeps it; on adds the pair-count kernel), step launch mode
+ * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the default, 2 the same
+ * graph with the broad-phase rebuild kernels in a conditional node: fewer launches per step,
+ * but the conditional node itself costs a few microseconds, which small handles feel). */
 int pd_set_tuning(pd_sim *sim, double skin_frac, uint32_t cand_cap, int threads_per_block,
                   int stats, int use_graphs);
 /* Clears the device error word after the caller has handled it. */
@@ -230,13 +233,13 @@ double pd_step_bytes(const pd_sim *sim);
 int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 /* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM)
  * for steps_per_variant steps from the same snapshot of the live state, restores the state
- * and keeps the fastest. Results do not depend on the variant (same per-node summation
+ * and keeps the fastest; then times the two step-graph modes of pd_set_tuning the same way. Results do not depend on the variant (same per-node summation
  * order). variant_ms (may be NULL) receives pd_num_variants() timings in ms per step. */
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);
 /* How steps are launched: 0 separate launches, 1 one CUDA graph per step, 2 a step graph whose
- * broad-phase rebuild kernels sit in a conditional node (after the first pd_step). */
+ * broad-phase rebuild kernels sit in a conditional node (see pd_set_tuning). */
 int pd_graph_mode(const pd_sim *sim);
 /* Copy of all device state that stepping changes, and its restore (checkpoint in HBM). */
 int pd_snapshot(pd_sim *sim);

@@ -172,6 +172,9 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   }
   Ncap_ = round_up(N_, 32);
   nslices_ = Ncap_ / 32;
+  // default bond-kernel variant: the autotuner's choice on small and on large handles (small
+  // handles are launch-latency bound and prefer the lighter variant)
+  variant_ = N_ < 131072 ? 0 : 3;
   sim_node0_.assign(S_ + 1, 0);
   sim_p0_.assign(S_ + 1, 0);
   for (uint32_t i = 0; i < S_; ++i) {
@@ -1023,7 +1026,11 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
     stats_ = stats != 0;
     relaunch = true;
   }
-  if (use_graphs >= 0) use_graphs_ = use_graphs != 0;
+  if (use_graphs >= 0) {  // 0: separate launches, 1: plain step graph, 2: conditional broad phase
+    use_graphs_ = use_graphs != 0;
+    use_conditional_ = use_graphs != 1;
+    graphs_ok_ = false;
+  }
   if (relaunch) graphs_ok_ = false;
   return PD_OK;
 }
@@ -1297,6 +1304,41 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
   variant_ = best;
   graphs_ok_ = false;
   if (chosen) *chosen = best;
+  // launch mode: the plain step graph or the one with the conditional broad phase, timed as
+  // graph replays from the same snapshot
+  if (use_graphs_) {
+    cudaEvent_t e0, e1;
+    PD_TRY(check(cudaEventCreate(&e0), "event"));
+    PD_TRY(check(cudaEventCreate(&e1), "event"));
+    float best_mode_ms = 1e30f;
+    bool best_cond = use_conditional_;
+    for (int mode = 1; mode <= 2; ++mode) {
+      use_conditional_ = mode == 2;
+      graphs_ok_ = false;
+      int rc = step(2);
+      if (rc == PD_OK) rc = check(cudaEventRecord(e0, stream_), "event");
+      if (rc == PD_OK) rc = step(steps_per_variant);
+      if (rc == PD_OK) rc = check(cudaEventRecord(e1, stream_), "event");
+      if (rc == PD_OK) rc = check(cudaEventSynchronize(e1), "event");
+      float ms = 0;
+      if (rc == PD_OK) cudaEventElapsedTime(&ms, e0, e1);
+      // the conditional graph counts only if it was really captured (it falls back otherwise)
+      if (rc == PD_OK && (mode == 1 || use_conditional_) && ms < best_mode_ms) {
+        best_mode_ms = ms;
+        best_cond = mode == 2;
+      }
+      if (rc == PD_OK) rc = restore();
+      if (rc != PD_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    use_conditional_ = best_cond;
+    graphs_ok_ = false;
+  }
   return PD_OK;
 }
 
