@@ -113,8 +113,6 @@ DevView Engine::view(int cur) const {
   v.win_lo = d_win_lo_;
   v.win_cnt = d_win_cnt_;
   v.win_max = win_max_;
-  v.tile_ctr = d_tile_ctr_;
-  v.n_chunks = n_sm_;
   v.extra_flag = d_extra_flag_;
   v.wall_local = d_wall_local_;
   v.lrtb_local_next = d_lrtb_local_;
@@ -319,12 +317,6 @@ int Engine::build_bonds() {
     PD_TRY(cpy(d_win_lo_, wlo.data(), nb * 4, "upload windows"));
     PD_TRY(cpy(d_win_cnt_, wcnt.data(), nb * 4, "upload windows"));
     if (win_max_) PD_TRY(prepare_staged_kernels(win_max_ * (uint32_t)sizeof(Rec32)));
-    int dev = 0, nsm = 0;
-    PD_TRY(check(cudaGetDevice(&dev), "device"));
-    PD_TRY(check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count"));
-    n_sm_ = (uint32_t)std::max(1, nsm);
-    PD_TRY(dalloc(this, allocs_, &d_tile_ctr_, n_sm_, err));
-    PD_TRY(mset(d_tile_ctr_, 0, n_sm_ * 4, "tile counters"));
   }
   PD_TRY(dalloc(this, allocs_, &d_slice_ptr_, nslices_ + 1, err));
   PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));

@@ -134,9 +134,6 @@ struct DevView {
   // node records its bonds read ([win_lo, win_lo + win_cnt); win_cnt 0 = not staged)
   const uint32_t *win_lo, *win_cnt;
   uint32_t win_max;      // largest staged range (records): the kernel's shared-memory size
-  // persistent bond kernel: one chunk of tiles per SM and its tile counter
-  uint32_t *tile_ctr;
-  uint32_t n_chunks;
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
   float *wall_local;     // [P][6] wall planes in each particle's local frame
   unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
@@ -352,8 +349,6 @@ class Engine {
   double *d_anchor_ = nullptr;
   double *d_f_extra_ = nullptr;
   uint32_t *d_win_lo_ = nullptr, *d_win_cnt_ = nullptr;
-  uint32_t *d_tile_ctr_ = nullptr;
-  uint32_t n_sm_ = 0;
   uint32_t win_max_ = 0;
   uint8_t *d_extra_flag_ = nullptr;
   float *d_wall_local_ = nullptr;

@@ -439,32 +439,6 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ De
   bond_node<U, W, PF, FX>(v, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// Persistent form: one chunk of consecutive 128-node tiles per SM, taken in order by the
-// blocks resident on that SM (the SM index picks the chunk), so that co-resident blocks gather
-// from overlapping node ranges and share L1; a block whose chunk is exhausted helps the next
-// chunks, so every tile is processed whatever the placement. tile_ctr holds one counter per
-// chunk, zeroed before each launch.
-template <int U, int MINB, int W, int PF, int FX>
-__global__ void __launch_bounds__(128, MINB) k_bond32p(const __grid_constant__ DevView v) {
-  __shared__ uint32_t s_tile;
-  uint32_t smid;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-  const uint32_t nc = v.n_chunks;
-  const uint64_t T = (v.N + 127) / 128;
-  for (uint32_t c0 = 0; c0 < nc; ++c0) {
-    const uint32_t c = (smid + c0) % nc;
-    const uint64_t t0 = T * c / nc, t1 = T * (c + 1) / nc;
-    for (;;) {
-      if (threadIdx.x == 0) s_tile = atomicAdd(&v.tile_ctr[c], 1u);
-      __syncthreads();
-      const uint64_t t = t0 + s_tile;
-      __syncthreads();
-      if (t >= t1) break;
-      bond_node<U, W, PF, FX>(v, t * 128 + threadIdx.x);
-    }
-  }
-}
-
 // Staged form of the bond kernel: one block of kStageNodes nodes first copies the contiguous
 // range of node records its bonds read into shared memory with bulk asynchronous copies
 // (cp.async.bulk, completion on an mbarrier), then gathers every partner from shared memory
@@ -631,7 +605,7 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
 // 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 17;
+const int kNumBondVariants = 14;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -640,12 +614,10 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
   const bool fused_extra = variant >= 6 && variant <= 9;
-  if (variant >= 10 && variant <= 13 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
-  if (variant >= 14 && !v.tile_ctr) variant = 3;
+  if (variant >= 10 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
   if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
   const unsigned bs = (unsigned)((v.N + kStageNodes - 1) / kStageNodes);
   const size_t sm = (size_t)v.win_max * sizeof(Rec32);
-  if (variant >= 14) cudaMemsetAsync(v.tile_ctr, 0, v.n_chunks * sizeof(uint32_t), s);
   switch (variant) {
     case 1: k_bond32<4, 6, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
     case 2: k_bond32<4, 4, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
@@ -660,9 +632,6 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
     case 11: k_bond32s<4, 2><<<bs, kStageNodes, sm, s>>>(v); break;
     case 12: k_bond32s<2, 3><<<bs, kStageNodes, sm, s>>>(v); break;
     case 13: k_bond32s<1, 4><<<bs, kStageNodes, sm, s>>>(v); break;
-    case 14: k_bond32p<2, 6, 1, 2, 0><<<v.n_chunks * 6, 128, 0, s>>>(v); break;
-    case 15: k_bond32p<4, 4, 1, 1, 0><<<v.n_chunks * 4, 128, 0, s>>>(v); break;
-    case 16: k_bond32p<4, 6, 1, 1, 0><<<v.n_chunks * 6, 128, 0, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
