@@ -15,6 +15,8 @@ Named workloads (seeded):
                x1e4, dt 2e-8, 20000 steps
   crush512     512 spheres/cubes/ellipsoids, sizes U[0.6, 1.4] mm, h from {0.05, 0.075, 0.1}
                mm, 12 mm box whose top wall moves down at 1 m/s, dt 5e-9, 10000 steps
+  notched_plate  100 x 200 x 9 mm steel plate with two 50 mm x 1.5 mm edge notches, h = 0.5 mm,
+               hit between the notches by a 50 mm wide steel block at 32 m/s, dt 2e-8, 5000 steps
 """
 from __future__ import annotations
 
@@ -220,6 +222,65 @@ def cubes125(n=5, edge=1.0 * MM, h=0.125 * MM, seed=1, steps=20000, dt=2e-8, g=9
     return s, base_config(dt, steps)
 
 
+def notch_cut(pos: np.ndarray, conn: np.ndarray, x_wall: float, y0: float, y1: float, z0: float,
+              z_extrusion: float) -> np.ndarray:
+    """Removes the bonds whose segment crosses the notch face x = x_wall, y in [y0, y1],
+    z in [z0, z0 + z_extrusion] (wall_line_intrsect, exp_dict.py:96-122: inclusive bounds)."""
+    keep = np.ones(len(conn), dtype=bool)
+    for a in range(0, len(conn), 1 << 22):
+        c = conn[a:a + (1 << 22)].astype(np.int64)
+        p6, p7 = pos[c[:, 0]], pos[c[:, 1]]
+        x6, x7 = p6[:, 0], p7[:, 0]
+        cross = (np.minimum(x6, x7) <= x_wall) & (x_wall <= np.maximum(x6, x7))
+        idx = np.nonzero(cross)[0]
+        if len(idx):
+            dx = x7[idx] - x6[idx]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                t = (x_wall - x6[idx]) / dx
+            ip = p6[idx] + t[:, None] * (p7[idx] - p6[idx])
+            hit = (y0 <= ip[:, 1]) & (ip[:, 1] <= y1) & (z0 <= ip[:, 2]) & (ip[:, 2] <= z0 + z_extrusion)
+            keep[a + idx[hit]] = False
+    return conn[keep]
+
+
+def notched_plate(Lx=100.0 * MM, Ly=200.0 * MM, Lz=9.0 * MM, h=0.5 * MM, notch_len=50.0 * MM,
+                  notch_w=1.5 * MM, notch_x=(25.0 * MM, 75.0 * MM), imp_w=50.0 * MM, imp_len=10.0 * MM, v=32.0,
+                  seed=4, steps=5000, dt=2e-8, jitter=0.05, gap=0.2):
+    """Config 3: a steel plate Lx x Ly x Lz with two edge notches of length notch_len and width
+    notch_w running from the edge y = 0 at x = notch_x; bonds across the notch faces are cut
+    like the reference's Kalthoff setup (exp_dict.py:1095-1163). A steel impactor block, imp_w
+    wide and unbreakable, hits the notched edge between the notches at v along +y; the surface
+    gap between them is gap*h."""
+    rng = np.random.default_rng(seed)
+    Rc = 0.5 * h
+
+    def block(ex, ey, ez, origin):
+        ax = [(np.arange(max(1, int(round(e / h)))) + 0.5) * h for e in (ex, ey, ez)]
+        X, Y, Z = np.meshgrid(*ax, indexing="ij")
+        P = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1) + np.asarray(origin)
+        return P + rng.uniform(-jitter * h, jitter * h, size=P.shape)
+
+    P = block(Lx, Ly, Lz, (0.0, 0.0, 0.0))
+    inside = np.zeros(len(P), dtype=bool)
+    for xc in notch_x:  # the notch slots carry no material
+        inside |= (np.abs(P[:, 0] - xc) < 0.5 * notch_w) & (P[:, 1] < notch_len)
+    P = P[~inside]
+    delta = 3.0 * h
+    conn = bonds(P, delta).astype(np.int64)
+    for xc in notch_x:
+        conn = notch_cut(P, conn, xc, -h, notch_len, -h, Lz + 2 * h)
+    m = material_3d(STEEL, delta)
+    plate = dict(pos=P, vol=np.full(len(P), h ** 3), conn=conn.astype(np.uint32), h=h, **m)
+    x0 = 0.5 * (notch_x[0] + notch_x[1]) - 0.5 * imp_w
+    # facing node layers (1 + gap) h apart, like two lattices whose surfaces are gap*h apart
+    Q = block(imp_w, imp_len, Lz, (x0, -imp_len - gap * h, 0.0))
+    imp = dict(pos=Q, vol=np.full(len(Q), h ** 3), conn=bonds(Q, delta), h=h,
+               vel=np.tile([0.0, v, 0.0], (len(Q), 1)), breakable=0, **material_3d(STEEL, delta))
+    s = finish([plate, imp], Rc, dt)
+    s.meta["name"] = "notched_plate"
+    return s, base_config(dt, steps)
+
+
 def _grid_pack(rng, m: int, count: int, pitch: float, hs, smin: float, smax: float) -> list:
     """`count` particles of random shape/size/resolution on the first cells of an m^3 grid of
     pitch `pitch` centred on the origin (cells in z, y, x order)."""
@@ -295,7 +356,7 @@ def serving_stream(n: int = 256, rate: float = 4.0, seed: int = 3, pmin: int = 8
     return out
 
 
-WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512}
+WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512, "notched_plate": notched_plate}
 
 
 def build_aggregate(kw: dict):

@@ -66,6 +66,14 @@ def prescribed(steps=30):
     return s, cfg
 
 
+def notched(steps=45):
+    """Config 3 in miniature: steel plate with two edge notches hit by an unbreakable block."""
+    s, cfg = gen.notched_plate(Lx=6.0 * MM, Ly=8.0 * MM, Lz=1.5 * MM, h=0.5 * MM, notch_len=3.0 * MM,
+                               notch_x=(2.0 * MM, 4.0 * MM), imp_w=2.0 * MM, imp_len=1.5 * MM, v=150.0,
+                               steps=steps, dt=2e-8, gap=-0.6)
+    return s, cfg
+
+
 CASES = {
     "impact_walls": impact_walls,
     "impact_free": impact_free,
@@ -73,4 +81,5 @@ CASES = {
     "toggles": toggles,
     "bdry_only": bdry_only,
     "prescribed": prescribed,
+    "notched": notched,
 }
