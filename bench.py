@@ -272,6 +272,36 @@ def accuracy_run(name: str, nsteps: int, eps: float = 1e-7, **over):
     return out
 
 
+def config_line(name: str, args, dist, torch) -> dict:
+    """Bond-updates/s of one more configuration in both forms (autotuned FP32C, plain FP64),
+    device-timed like the headline; bonds built on the GPU (pd_query_pairs)."""
+    from peridem_gb300 import gen
+    from peridem_gb300.sim import Sim
+    gen.set_bond_builder("gpu")
+    t0 = time.perf_counter()
+    try:
+        s, cfg = gen.WORKLOADS[name]()
+    finally:
+        gen.set_bond_builder("cpu")
+    t_gen = time.perf_counter() - t0
+    out = {"workload": name, "particles": s.n_particles, "nodes": s.n_nodes, "directed_bonds": s.n_bonds_directed,
+           "setup_s": t_gen}
+    sim = Sim(s, cfg, "fp32c")
+    variant, _ = sim.autotune(4)
+    K = args.other_steps
+    ms, l0, l1 = time_device(sim, K, 3, dist, torch)
+    out["fp32c"] = {"value": K * 0.5 * (l0 + l1) / (ms * 1e-3), "ms_per_step": ms / K, "variant": int(variant),
+                    "graph_mode": sim.graph_mode()}
+    sim.close()
+    K64 = max(3, min(K, args.fp64_steps))
+    sim64 = Sim(s, cfg, "fp64")
+    ms64, a0, a1 = time_device(sim64, K64, 3, dist, torch)
+    out["fp64"] = {"value": K64 * 0.5 * (a0 + a1) / (ms64 * 1e-3), "ms_per_step": ms64 / K64}
+    sim64.close()
+    out["fp32c_over_fp64"] = out["fp32c"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def serving_run(args):
     """Config 4: the Poisson request stream served with continuous batching in the FP32-
     compensated form, beside a one-at-a-time plain FP64 queue modelled from measured service
@@ -469,6 +499,19 @@ def ours(args):
         acc_dyn.append(accuracy_run("cubes125", args.acc_steps_c1, steps=args.acc_steps_c1))
         if args.acc_steps_c2 > 0:
             acc_dyn.append(accuracy_run(args.workload, args.acc_steps_c2))
+        if args.acc_steps_c3 > 0:
+            from peridem_gb300 import gen as _gen
+            _gen.set_bond_builder("gpu")
+            try:
+                acc_dyn.append(accuracy_run("notched_plate", args.acc_steps_c3))
+            finally:
+                _gen.set_bond_builder("cpu")
+
+    # ---- the other configurations' throughput (both forms, same timing rules), rank 0 at N=1
+    others = []
+    if r == 0 and world == 1 and args.other_configs:
+        for name in [x for x in args.other_configs.split(",") if x]:
+            others.append(config_line(name, args, dist, torch))
 
     # ---- serving stream (continuous batching), rank 0 at N=1 only
     serving = None
@@ -496,7 +539,7 @@ def ours(args):
                      "autotune_ms_per_variant": [round(float(x), 4) for x in variant_ms],
                      "phase_ms": {"predict": ph[0], "broadphase": ph[1], "step": ph[2], "end": ph[3]}},
         "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64, "accuracy_vs_fp64": acc,
-        "accuracy_dynamic": acc_dyn, "serving": serving,
+        "accuracy_dynamic": acc_dyn, "serving": serving, "other_configs": others,
         "gpu_launches": gpu_launches, "broadphase_rebuilds_timed": sim.rebuilds_timed, "clocks": clocks,
         "graph_mode": {0: "separate launches", 1: "step graph", 2: "step graph, conditional broad phase"}.get(graph_mode),
     }
@@ -525,6 +568,10 @@ def main():
     ap.add_argument("--acc-steps-c0", type=int, default=2000)
     ap.add_argument("--acc-steps-c1", type=int, default=4000)
     ap.add_argument("--acc-steps-c2", type=int, default=0, help="also compare both forms on the bench workload")
+    ap.add_argument("--acc-steps-c3", type=int, default=0, help="also compare both forms on the notched plate")
+    ap.add_argument("--other-configs", default="two_sphere,cubes125,notched_plate",
+                    help="comma-separated workloads timed beside the headline ('' to skip)")
+    ap.add_argument("--other-steps", type=int, default=200)
     ap.add_argument("--serve", type=int, default=256, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-chunk", type=int, default=500)
     ap.add_argument("--serve-burst", type=int, default=1, help="also serve the stream with every request waiting at t=0")
