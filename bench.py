@@ -287,7 +287,8 @@ def config_line(name: str, args, dist, torch) -> dict:
     out = {"workload": name, "particles": s.n_particles, "nodes": s.n_nodes, "directed_bonds": s.n_bonds_directed,
            "setup_s": t_gen}
     sim = Sim(s, cfg, "fp32c")
-    variant, _ = sim.autotune(4)
+    variant, vms = sim.autotune(4)
+    out["autotune_ms_per_variant"] = [round(float(x), 4) for x in vms]
     K = args.other_steps
     ms, l0, l1 = time_device(sim, K, 3, dist, torch)
     out["fp32c"] = {"value": K * 0.5 * (l0 + l1) / (ms * 1e-3), "ms_per_step": ms / K, "variant": int(variant),
