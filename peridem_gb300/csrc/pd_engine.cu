@@ -113,7 +113,6 @@ DevView Engine::view(int cur) const {
   v.win_lo = d_win_lo_;
   v.win_cnt = d_win_cnt_;
   v.win_max = win_max_;
-  v.row_wmax = row_wmax_;
   v.extra_flag = d_extra_flag_;
   v.wall_local = d_wall_local_;
   v.lrtb_local_next = d_lrtb_local_;
@@ -174,8 +173,9 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   Ncap_ = round_up(N_, 32);
   nslices_ = Ncap_ / 32;
   // default bond-kernel variant: the autotuner's choice on small and on large handles (small
-  // handles are launch-latency bound and prefer the lighter variant)
-  variant_ = N_ < 131072 ? 0 : 3;
+  // handles are launch-latency bound and gain most from doing the non-bond work in the bond
+  // kernel, one launch less per step)
+  variant_ = N_ < 131072 ? 6 : 3;
   sim_node0_.assign(S_ + 1, 0);
   sim_p0_.assign(S_ + 1, 0);
   for (uint32_t i = 0; i < S_; ++i) {
@@ -318,11 +318,6 @@ int Engine::build_bonds() {
     PD_TRY(cpy(d_win_lo_, wlo.data(), nb * 4, "upload windows"));
     PD_TRY(cpy(d_win_cnt_, wcnt.data(), nb * 4, "upload windows"));
     if (win_max_) PD_TRY(prepare_staged_kernels(win_max_ * (uint32_t)sizeof(Rec32)));
-    // row-parallel kernel: 516 bytes of shared memory per position of the widest slice
-    uint64_t wmax = 0;
-    for (uint64_t sl = 0; sl < nslices_; ++sl) wmax = std::max<uint64_t>(wmax, (h_slice_ptr_[sl + 1] - h_slice_ptr_[sl]) / 32);
-    row_wmax_ = (wmax > 0 && wmax * 516 <= 200 * 1024) ? (uint32_t)wmax : 0u;
-    if (row_wmax_) PD_TRY(prepare_row_kernels(row_wmax_ * 516));
   }
   PD_TRY(dalloc(this, allocs_, &d_slice_ptr_, nslices_ + 1, err));
   PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));

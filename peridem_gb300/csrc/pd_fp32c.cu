@@ -459,94 +459,6 @@ __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ De
   bond_node<U, W, PF, FX>(v, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// Row-parallel form for small handles, where one thread per node leaves most of the GPU idle
-// and the step time is the length of each thread's chain of ~100 dependent gathers: the four
-// warps of a block share one slice (32 nodes), warp w evaluating positions w, w+4, ... of every
-// row and parking the bond terms in shared memory; warp 0 then adds them up in position order
-// with the same Kahan steps as k_bond32, so the results are bit-identical to it.
-template <int U>
-__global__ void __launch_bounds__(128) k_bond32r(const __grid_constant__ DevView v) {
-  extern __shared__ __align__(16) float row_terms[];  // [W][4][32] terms, then [W] live words
-  const uint32_t W = v.row_wmax;
-  uint32_t *words = reinterpret_cast<uint32_t *>(row_terms + (size_t)W * 128);
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint64_t sl = blockIdx.x;
-  const uint64_t n = sl * 32 + lane;
-  const bool valid = n < v.N;
-  const uint64_t nn = valid ? n : 0;
-  const uint32_t k = v.pid[nn];
-  const DevPart &P = v.parts[k];
-  const int32_t movable = P.movable;
-  const DevSimState &st = v.ss[P.sim];
-  const bool run = valid && st.active;
-  float4 pi4, ui4;
-  ld_rec<1>(v.rec + nn, pi4, ui4);
-  const uint64_t sbase = v.slice_ptr[sl];
-  const uint32_t width = (uint32_t)((v.slice_ptr[sl + 1] - sbase) >> 5);
-  const int dg = (run && movable) ? v.deg[nn] : 0;
-  uint32_t *maskp = v.mask + (sbase >> 5);
-  // phase 1: bond terms of positions warp, warp+4, ... (breaking decided here, as in k_bond32)
-  {
-    const uint32_t *colp = v.col + sbase + lane;
-    const bool brk = st.fracture && P.breakable && P.break_bonds;
-    const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
-    for (uint32_t j0 = warp; j0 < width; j0 += 4 * U) {
-      uint32_t q[U], m[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const uint32_t j = j0 + 4 * u;
-        m[u] = j < width ? maskp[j] : 0u;
-        q[u] = (j < width && (int)j < dg) ? __ldg(colp + 32 * j) : 0u;
-        if (lane == 0 && j < width) words[j] = m[u];  // live bits before this step's breaking
-      }
-      float4 pq[U], uq[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const uint32_t j = j0 + 4 * u;
-        const bool live = (int)j < dg && ((m[u] >> lane) & 1u);
-        if (live) ld_rec<1>(v.rec + q[u], pq[u], uq[u]);
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const uint32_t j = j0 + 4 * u;
-        if ((int)j < dg && ((m[u] >> lane) & 1u)) {
-          const BondTerms b = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
-          float *t = row_terms + (size_t)j * 128;
-          t[lane] = b.g;
-          t[32 + lane] = b.yx;
-          t[64 + lane] = b.yy;
-          t[96 + lane] = b.yz;
-          if (brk && b.str > slo) {
-            if (b.str > shi) cut_bond(&maskp[j], lane);
-            else band_check(v, nn, q[u], &maskp[j], lane, P.snot);
-          }
-        }
-      }
-    }
-  }
-  __syncthreads();
-  if (warp != 0) return;
-  // phase 2: the node's sum in position order, then the per-node tail
-  Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  uint32_t live = 0;
-  for (int j = 0; j < dg; ++j) {
-    if (!((words[j] >> lane) & 1u)) continue;
-    ++live;
-    const float *t = row_terms + (size_t)j * 128;
-    kahan_add(a, t[lane], t[32 + lane], t[64 + lane], t[96 + lane]);
-  }
-  D3 f = d3(0.0, 0.0, 0.0);
-  if (run) {
-    f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
-    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, v.Ncap);
-  }
-  verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
-  if (v.stats) {
-    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
-    if (lane == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
-  }
-}
-
 // Staged form of the bond kernel: one block of kStageNodes nodes first copies the contiguous
 // range of node records its bonds read into shared memory with bulk asynchronous copies
 // (cp.async.bulk, completion on an mbarrier), then gathers every partner from shared memory
@@ -699,15 +611,6 @@ int prepare_staged_kernels(uint32_t smem_bytes) {
   return e == cudaSuccess ? PD_OK : PD_ECUDA;
 }
 
-int prepare_row_kernels(uint32_t smem_bytes) {
-  cudaError_t e = cudaSuccess;
-  auto set = [&](const void *fn) {
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-  };
-  set((const void *)k_bond32r<1>);
-  set((const void *)k_bond32r<2>);
-  return e == cudaSuccess ? PD_OK : PD_ECUDA;
-}
 
 // A_next := this step's predicted displacement of each particle's anchor node.
 __global__ void k_anchor_next(DevView v) {
@@ -723,7 +626,7 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
 // 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 16;
+const int kNumBondVariants = 14;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -732,8 +635,7 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
   const bool fused_extra = variant >= 6 && variant <= 9;
-  if (variant >= 10 && variant <= 13 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
-  if (variant >= 14 && !v.row_wmax) variant = 3;                   // rows too wide for shared memory
+  if (variant >= 10 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
   if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
   const unsigned bs = (unsigned)((v.N + kStageNodes - 1) / kStageNodes);
   const size_t sm = (size_t)v.win_max * sizeof(Rec32);
@@ -751,8 +653,6 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
     case 11: k_bond32s<4, 2><<<bs, kStageNodes, sm, s>>>(v); break;
     case 12: k_bond32s<2, 3><<<bs, kStageNodes, sm, s>>>(v); break;
     case 13: k_bond32s<1, 4><<<bs, kStageNodes, sm, s>>>(v); break;
-    case 14: k_bond32r<1><<<(unsigned)((v.N + 31) / 32), 128, (size_t)v.row_wmax * 516, s>>>(v); break;
-    case 15: k_bond32r<2><<<(unsigned)((v.N + 31) / 32), 128, (size_t)v.row_wmax * 516, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
