@@ -108,17 +108,24 @@ class Server:
         self.cohorts: list[_Cohort] = []
         self.log: list[tuple] = []   # (time, event, detail)
         self.create_s: list[float] = []  # host+device time to build each cohort's handle
+        self._solo: set = set()          # requests to admit alone (their cohort failed to build)
         self.finish_s = 0.0              # time spent reading finished simulations back
 
     # -- admission ------------------------------------------------------------------------
     def _pick(self, waiting: deque, est: dict) -> list:
+        """First fit in arrival order; a request whose cohort failed to build is retried alone."""
         free = self.capacity - self.used
         pick, tot = [], 0
         for r in list(waiting):
             b = est[r.rid]
+            alone = r.rid in self._solo
+            if alone and pick:
+                continue
             if tot + b <= free and len(pick) < self.max_batch:
                 pick.append(r)
                 tot += b
+                if alone:
+                    break
         return pick
 
     def _create(self, reqs: list, out: dict):
@@ -178,9 +185,9 @@ class Server:
                         results[r.rid] = Result(r.rid, None, None, r.arrival if realtime else 0.0, ta, now(), 0,
                                                 len(r.setup.pos), directed_bonds(r.setup), error=out.get("error"))
                     else:  # retry one by one
-                        for r in reversed(areqs):
+                        for r in reversed(areqs):  # retry each of them alone
+                            self._solo.add(r.rid)
                             waiting.appendleft(r)
-                        self.max_batch = 1
             # start an admission
             if admit is None and waiting:
                 pick = self._pick(waiting, est)

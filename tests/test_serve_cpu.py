@@ -106,3 +106,24 @@ def test_sequential_queue_arithmetic():
     ttc = serve.sequential_ttc(arr, svc)
     # done: 2, 4, 5, 10.5
     np.testing.assert_allclose(ttc, [2.0, 3.0, 3.5, 0.5])
+
+
+class FailingPairBatch(FakeBatch):
+    """Fails to build any cohort of more than one request containing request 1."""
+
+    def __init__(self, setups, configs, precision):
+        if len(setups) > 1 and any(c.get("tag") == 1 for c in configs):
+            raise RuntimeError("cohort build failed")
+        super().__init__(setups, configs, precision)
+
+
+def test_failed_cohort_is_retried_one_by_one():
+    reqs = [_req(i, 100, 10) for i in range(4)]
+    for r in reqs:
+        r.config = dict(r.config, tag=r.rid)
+    FakeBatch.instances.clear()
+    srv = serve.Server("fp32c", capacity_bytes=10 ** 9, make_batch=FailingPairBatch, estimate=fake_estimate,
+                       max_batch=4)
+    res = srv.run(reqs, realtime=False)
+    assert all(r.error is None and r.state["steps"] == 10 for r in res)
+    assert srv.max_batch == 4  # only the failed requests were retried alone
