@@ -77,6 +77,7 @@ uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision,
   } else {
     b += 2 * C * 32 + 3 * C * 8 + 2 * 3 * P * 8 + C + 3 * C * 8 + C + 2 * 6 * P * 4;
     b += 2 * 4 * atleast1((N + kStageNodes - 1) / kStageNodes);  // staged-kernel record ranges
+    b += C * 4 + atleast1(P) * 4 + 2 * 4;                          // non-bond work lists
   }
   // broad phase
   uint32_t bits = 10;

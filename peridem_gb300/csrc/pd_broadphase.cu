@@ -66,6 +66,7 @@ __global__ void k_bp_decide(DevView v, double half_skin, cudaGraphConditionalHan
 
 __global__ void k_bp_clear(DevView v, uint32_t *count, uint64_t T) {
   if (!v.cnt->rebuild) return;
+  if (v.xcount && blockIdx.x == 0 && threadIdx.x == 0) v.xcount[0] = 0;  // contact-node list restarts
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += (uint64_t)gridDim.x * blockDim.x)
     count[i] = 0;
 }
@@ -206,6 +207,7 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
   uint32_t *out = cand + n * cap;
   for (int i = 0; i < cnt; ++i) out[i] = list[i];
   cand_n[n] = (uint16_t)cnt;
+  if (cnt && v.xnodes) v.xnodes[atomicAdd(&v.xcount[0], 1u)] = (uint32_t)n;  // FP32 form: work list
   if (overflow) atomicOr(&v.cnt->err, PD_DERR_CAND_OVERFLOW);
 }
 

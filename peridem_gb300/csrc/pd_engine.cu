@@ -113,6 +113,9 @@ DevView Engine::view(int cur) const {
   v.win_lo = d_win_lo_;
   v.win_cnt = d_win_cnt_;
   v.win_max = win_max_;
+  v.xnodes = bp_.xnodes;
+  v.xparts = bp_.xparts;
+  v.xcount = bp_.xcount;
   v.extra_flag = d_extra_flag_;
   v.wall_local = d_wall_local_;
   v.lrtb_local_next = d_lrtb_local_;
@@ -604,6 +607,12 @@ int Engine::alloc_and_upload() {
   PD_TRY(dalloc(this, allocs_, &bp_.slot, C, err));
   PD_TRY(dalloc(this, allocs_, &bp_.sorted, C, err));
   PD_TRY(dalloc(this, allocs_, &bp_.block_sums, (T + 4095) / 4096 + 1, err));
+  if (precision_ == PD_FP32C) {
+    PD_TRY(dalloc(this, allocs_, &bp_.xnodes, C, err));
+    PD_TRY(dalloc(this, allocs_, &bp_.xparts, P_, err));
+    PD_TRY(dalloc(this, allocs_, &bp_.xcount, 2, err));
+    PD_TRY(mset(bp_.xcount, 0, 8, "work lists"));
+  }
   PD_TRY(alloc_candidates());
 
   if (precision_ == PD_FP64) {
@@ -631,6 +640,7 @@ int Engine::prepare_fused(int cur) {
   DevView v = view(cur);
   launch_predict(v, tpb_, stream_);
   launch_anchor_next(v, stream_);
+  launch_xparts_all(v, stream_);  // every particle on the non-bond work list until the next step ends
   return check(cudaGetLastError(), "prepare fused");
 }
 
@@ -1221,6 +1231,11 @@ int Engine::snapshot() {
   }
   reg(bp_.cand, (size_t)C * bp_.cand_cap * 4);
   reg(bp_.cand_n, (size_t)C * 2);
+  if (bp_.xcount) {
+    reg(bp_.xnodes, (size_t)C * 4);
+    reg(bp_.xparts, (size_t)P_ * 4);
+    reg(bp_.xcount, 8);
+  }
   size_t total = 0;
   for (auto &m : mutable_) total += (m.second + 255) & ~(size_t)255;
   if (total > backup_bytes_) {

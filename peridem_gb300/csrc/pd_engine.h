@@ -92,6 +92,7 @@ struct DevCounters {
   unsigned long long pairwise;
   unsigned long long rebuilds;
   unsigned long long live_bonds;
+  double last_stepmax;              // movement bound of the step that just ended
 };
 
 // FP32 form: one 32-byte record per node, so that a bond gathers its partner with a single
@@ -134,6 +135,8 @@ struct DevView {
   // node records its bonds read ([win_lo, win_lo + win_cnt); win_cnt 0 = not staged)
   const uint32_t *win_lo, *win_cnt;
   uint32_t win_max;      // largest staged range (records): the kernel's shared-memory size
+  // FP32 form: work lists of k_extra32 (see BroadPhase)
+  uint32_t *xnodes, *xparts, *xcount;
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
   float *wall_local;     // [P][6] wall planes in each particle's local frame
   unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
@@ -167,6 +170,9 @@ struct BroadPhase {
   uint16_t *cand_n = nullptr;
   uint32_t cand_cap = 0;
   double skin_frac = 0.5;
+  // FP32 form: the nodes that have contact candidates (rebuilt with the lists), the particles
+  // that need FP64 non-bond work next step, and their counts ([0] nodes, [1] particles)
+  uint32_t *xnodes = nullptr, *xparts = nullptr, *xcount = nullptr;
 };
 
 // A frame's worth of device state in pinned host memory, copied in stream order: the copies
@@ -386,6 +392,7 @@ void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
+void launch_xparts_all(const DevView &v, cudaStream_t s);
 void launch_prescribed(const DevView &v, cudaStream_t s);
 void launch_reset_y(const DevView &v, cudaStream_t s);
 

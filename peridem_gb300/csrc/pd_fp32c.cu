@@ -168,20 +168,41 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
   return f;
 }
 
-// Separate-kernel form: the FP64 non-bond force of every node that has some, for the bond
-// kernel to add (f_extra, extra_flag).
-__global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView v) {
-  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N) return;
+// Separate-kernel form: the FP64 non-bond force of the nodes that have some, for the bond
+// kernel to add (f_extra, extra_flag; the bond kernel clears the flag when it takes the force).
+// Only listed work is visited: the nodes with contact candidates (listed when the candidate
+// lists are built) and the nodes of the particles listed at the end of the previous step
+// (external force, torque, or a wall nearby); the cost follows the work, not the node count.
+__device__ __forceinline__ void extra_node(const DevView &v, uint64_t n) {
   const uint32_t k = v.pid[n];
   const DevPart &P = v.parts[k];
   const DevSimState &st = v.ss[P.sim];
-  if (!st.active || !extra_needed(v, n, k, P, v.sp[P.sim], st, v.rec[n].p, v.rec[n].u)) {
-    v.extra_flag[n] = 0;
-    return;
-  }
+  if (!st.active || !extra_needed(v, n, k, P, v.sp[P.sim], st, v.rec[n].p, v.rec[n].u)) return;
   st3(v.f_extra, n, v.Ncap, extra_force(v, n));
   v.extra_flag[n] = 1;
+}
+
+__global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView v) {
+  const uint32_t nx = v.xcount[0], np = v.xcount[1];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nx; i += gridDim.x * blockDim.x)
+    extra_node(v, v.xnodes[i]);
+  for (uint32_t i = blockIdx.x; i < np; i += gridDim.x) {
+    const DevPart &P = v.parts[v.xparts[i]];
+    for (uint32_t l = threadIdx.x; l < P.n; l += blockDim.x) {
+      const uint64_t n = (uint64_t)P.g0 + l;
+      if (v.cand_n[n] == 0) extra_node(v, n);  // nodes with candidates are on the node list
+    }
+  }
+}
+
+// Fills the particle list with every particle (after setup or a state change).
+__global__ void k_xparts_all(DevView v) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < v.P; k += gridDim.x * blockDim.x) v.xparts[k] = k;
+  if (blockIdx.x == 0 && threadIdx.x == 0) v.xcount[1] = v.P;
+}
+
+void launch_xparts_all(const DevView &v, cudaStream_t s) {
+  if (v.xparts && v.P) k_xparts_all<<<(v.P + 255) / 256, 256, 0, s>>>(v);
 }
 
 // FP64 stretch of the reference formula (particle2.h:139-149) for a bond whose FP32 stretch
@@ -445,6 +466,7 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
       if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
     } else if (v.extra_flag[nn]) {
       f = f + ld3(v.f_extra, nn, C3);
+      v.extra_flag[nn] = 0;
     }
   }
   verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
@@ -587,7 +609,10 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
   D3 f = d3(0.0, 0.0, 0.0);
   if (run) {
     f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
-    if (v.extra_flag[nn]) f = f + ld3(v.f_extra, nn, C3);
+    if (v.extra_flag[nn]) {
+      f = f + ld3(v.f_extra, nn, C3);
+      v.extra_flag[nn] = 0;
+    }
   }
   verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
   if (v.stats) {
@@ -636,7 +661,7 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const unsigned b = (unsigned)blocks;
   const bool fused_extra = variant >= 6 && variant <= 9;
   if (variant >= 10 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
-  if (!fused_extra) k_extra32<<<b, 128, 0, s>>>(v);
+  if (!fused_extra) k_extra32<<<152 * 8, 128, 0, s>>>(v);
   const unsigned bs = (unsigned)((v.N + kStageNodes - 1) / kStageNodes);
   const size_t sm = (size_t)v.win_max * sizeof(Rec32);
   switch (variant) {

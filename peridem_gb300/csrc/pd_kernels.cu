@@ -343,6 +343,23 @@ __global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const ui
   if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
       (uint32_t)sp.set_stoppable_ts == tn)
     P.stoppable = 1;
+  // FP32 form: does any node of this particle need FP64 non-bond work next step besides contact
+  // (which the contact-node list covers)? External force, torque, or a wall within the contact
+  // radius of the particle's box grown by this step's movement bound (k_extra32 then tests each
+  // node exactly).
+  if (v.xparts) {
+    bool need = (P.movable && P.has_ext) || st.torque;
+    if (!need && P.movable && P.stoppable && sp.allow_wall) {
+      const double lim = sp.Rc * 1.001 + 2.0 * v.cnt->last_stepmax + 1e-12;
+      const double *b = v.lrtb + 6 * (uint64_t)k;
+      for (int f = 0; f < 6 && !need; ++f) {
+        const int c = f % 3;
+        const double w = st.wall[f];
+        need = (b[c] - lim <= w) && (b[3 + c] + lim >= w);
+      }
+    }
+    if (need) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;
+  }
 }
 
 // Flags a simulation uses in step t (the sticky toggles of timeloop.h:405-464).
@@ -383,7 +400,9 @@ __global__ void k_end_sims(DevView v, double half_skin) {
       c.moved += stepmax;
     }
     // clamped-node jumps recorded after the rebuild test count towards the next one
+    c.last_stepmax = stepmax;
     c.stepmax_bits = 0;
+    if (v.xcount) v.xcount[1] = 0;  // k_end_particles lists the particles of the next step
     c.rebuild = 0;
     (void)half_skin;
   }
