@@ -165,10 +165,10 @@ __device__ __forceinline__ bool nonfinite(double x) {
 }
 
 // End-of-step work of the FP32 form for one particle: AABB from the local-frame keys of this
-// step (widened by a few float ulps each way), anchors moved on by one step, walls expressed in
-// the frame of the next step's records.
+// step (widened by a few float ulps each way), anchors moved on by one step, the next step's
+// wall planes (wall_next) expressed in the frame of the next step's records.
 __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const DevPart &P,
-                                                   const DevSimState &st) {
+                                                   const double *wall_next) {
   double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
   double *ann = v.anchor_next + 3 * (uint64_t)k;
   unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
@@ -193,7 +193,7 @@ __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k,
   float *wl = v.wall_local + 6 * (uint64_t)k;
   for (int f = 0; f < 6; ++f) {
     const int c = f % 3;
-    wl[f] = (float)(st.wall[f] - (P.anchor_pos[c] + an[c]));
+    wl[f] = (float)(wall_next[f] - (P.anchor_pos[c] + an[c]));
   }
 }
 

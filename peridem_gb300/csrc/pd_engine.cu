@@ -640,7 +640,8 @@ int Engine::prepare_fused(int cur) {
   DevView v = view(cur);
   launch_predict(v, tpb_, stream_);
   launch_anchor_next(v, stream_);
-  launch_xparts_all(v, stream_);  // every particle on the non-bond work list until the next step ends
+  // the next step's non-bond kernel visits every node (the work lists are rebuilt by then)
+  PD_TRY(check(cudaMemsetAsync(&d_cnt_->xall, 1, sizeof(uint32_t), stream_), "work lists"));
   return check(cudaGetLastError(), "prepare fused");
 }
 

@@ -93,6 +93,8 @@ struct DevCounters {
   unsigned long long rebuilds;
   unsigned long long live_bonds;
   double last_stepmax;              // movement bound of the step that just ended
+  uint32_t end_blocks;              // blocks of k_end_step done (the last one advances the sims)
+  uint32_t xall;                    // FP32 form: k_extra32 visits every node this step (no lists)
 };
 
 // FP32 form: one 32-byte record per node, so that a bond gathers its partner with a single
@@ -392,7 +394,6 @@ void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
-void launch_xparts_all(const DevView &v, cudaStream_t s);
 void launch_prescribed(const DevView &v, cudaStream_t s);
 void launch_reset_y(const DevView &v, cudaStream_t s);
 

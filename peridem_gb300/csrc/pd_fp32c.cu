@@ -183,6 +183,11 @@ __device__ __forceinline__ void extra_node(const DevView &v, uint64_t n) {
 }
 
 __global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView v) {
+  if (v.cnt->xall) {  // after setup or a state change: every node, once
+    for (uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; n < v.N; n += (uint64_t)gridDim.x * blockDim.x)
+      extra_node(v, n);
+    return;
+  }
   const uint32_t nx = v.xcount[0], np = v.xcount[1];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nx; i += gridDim.x * blockDim.x)
     extra_node(v, v.xnodes[i]);
@@ -193,16 +198,6 @@ __global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView
       if (v.cand_n[n] == 0) extra_node(v, n);  // nodes with candidates are on the node list
     }
   }
-}
-
-// Fills the particle list with every particle (after setup or a state change).
-__global__ void k_xparts_all(DevView v) {
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < v.P; k += gridDim.x * blockDim.x) v.xparts[k] = k;
-  if (blockIdx.x == 0 && threadIdx.x == 0) v.xcount[1] = v.P;
-}
-
-void launch_xparts_all(const DevView &v, cudaStream_t s) {
-  if (v.xparts && v.P) k_xparts_all<<<(v.P + 255) / 256, 256, 0, s>>>(v);
 }
 
 // FP64 stretch of the reference formula (particle2.h:139-149) for a bond whose FP32 stretch
@@ -478,6 +473,11 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
 
 template <int U, int MINB, int W, int PF, int FX>
 __global__ void __launch_bounds__(128, MINB) k_bond32(const __grid_constant__ DevView v) {
+  // the work lists of k_extra32 have been consumed: k_end_step builds the next particle list
+  if (blockIdx.x == 0 && threadIdx.x == 0 && v.xcount) {
+    v.xcount[1] = 0;
+    v.cnt->xall = 0;
+  }
   bond_node<U, W, PF, FX>(v, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -493,6 +493,10 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
   extern __shared__ __align__(128) unsigned char stage_raw[];
   Rec32 *win = reinterpret_cast<Rec32 *>(stage_raw);
   __shared__ __align__(8) uint64_t bar;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && v.xcount) {  // as in k_bond32
+    v.xcount[1] = 0;
+    v.cnt->xall = 0;
+  }
   const uint32_t wlo = v.win_lo[blockIdx.x];
   const uint32_t wcnt = v.win_cnt[blockIdx.x];
   bool staged = wcnt != 0;

@@ -9,8 +9,8 @@
 //                    (timeloop.h:544-634), node-node contact of particle pairs in
 //                    ascending partner order (timeloop.h:636-651, contact.h:744-942) and
 //                    the velocity-Verlet corrector (timeloop.h:661-781)
-//   k_end_particles  AABB refresh, clamped nodes, anchors, per-particle toggles
-//   k_end_sims       wall motion (timeloop.h:784-797), scheduled toggles, step counter
+//   k_end_step       AABB refresh, clamped nodes, anchors, per-particle toggles; its last
+//                    block: wall motion (timeloop.h:784-797), scheduled toggles, step counter
 // Each node's force is gathered by one thread in the reference's summation order, so the
 // FP64 form reproduces the reference bit for bit without atomics on forces.
 #include <cuda_runtime.h>
@@ -294,74 +294,6 @@ void launch_step_kernel(const DevView &v, int precision, int variant, cudaStream
 // ------------------------------------------------------------------------------------
 // end of step
 
-__global__ void k_end_particles(DevView v, const uint32_t *clamped_ptr, const uint32_t *clamped,
-                                double *clamped_disp) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= v.P) return;
-  DevPart &P = v.parts[k];
-  const DevSimState &st = v.ss[P.sim];
-  const DevSimParams &sp = v.sp[P.sim];
-  if (!st.active) return;
-  if (v.rec) {
-    end_particle_fp32c(v, k, P, st);
-  } else {
-    unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
-    if (P.movable) {
-      for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
-    }
-    for (int c = 0; c < 3; ++c) {
-      L[c] = ord_key(INFINITY);
-      L[3 + c] = ord_key(-INFINITY);
-    }
-  }
-  // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
-  // keeps this step's predicted displacement, saved for the readback (the fused FP32 form
-  // zeroes them in its corrector and keeps this step's displacement buffer intact)
-  if (clamped_ptr && !v.fused) {
-    double jump = 0;
-    for (uint32_t c = clamped_ptr[k]; c < clamped_ptr[k + 1]; ++c) {
-      uint64_t g = clamped[c];
-      D3 d = ld3(v.disp, g, v.Ncap);
-      clamped_disp[3 * (uint64_t)c] = d.x;
-      clamped_disp[3 * (uint64_t)c + 1] = d.y;
-      clamped_disp[3 * (uint64_t)c + 2] = d.z;
-      if (P.movable) {
-        jump = fmax(jump, norm3(d));
-        st3(v.disp, g, v.Ncap, d3(0.0, 0.0, 0.0));
-        st3(v.vel_out, g, v.Ncap, d3(0.0, 0.0, 0.0));
-        st3(v.acc, g, v.Ncap, d3(0.0, 0.0, 0.0));
-      }
-    }
-    if (jump > 0) atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(jump));
-  }
-  // per-particle toggles for the next step (timeloop.h:481-498); k_end_sims has already
-  // advanced st.t to the next step's index
-  const uint32_t tn = st.t;
-  const uint32_t kl = k - sp.p0;
-  if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
-    P.movable = 1;
-  if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
-      (uint32_t)sp.set_stoppable_ts == tn)
-    P.stoppable = 1;
-  // FP32 form: does any node of this particle need FP64 non-bond work next step besides contact
-  // (which the contact-node list covers)? External force, torque, or a wall within the contact
-  // radius of the particle's box grown by this step's movement bound (k_extra32 then tests each
-  // node exactly).
-  if (v.xparts) {
-    bool need = (P.movable && P.has_ext) || st.torque;
-    if (!need && P.movable && P.stoppable && sp.allow_wall) {
-      const double lim = sp.Rc * 1.001 + 2.0 * v.cnt->last_stepmax + 1e-12;
-      const double *b = v.lrtb + 6 * (uint64_t)k;
-      for (int f = 0; f < 6 && !need; ++f) {
-        const int c = f % 3;
-        const double w = st.wall[f];
-        need = (b[c] - lim <= w) && (b[3 + c] + lim >= w);
-      }
-    }
-    if (need) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;
-  }
-}
-
 // Flags a simulation uses in step t (the sticky toggles of timeloop.h:405-464).
 __device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t) {
   if (sp.set_torque_ts != -1 && t == (uint32_t)sp.set_torque_ts) st.torque = 1;
@@ -378,9 +310,90 @@ __device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint3
   }
 }
 
-__global__ void k_end_sims(DevView v, double half_skin) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < v.S) {
+// Per-particle end of step, then (last block) the simulations' advance. One kernel: the
+// particles read their simulation's state of this step and derive the next step's wall planes
+// and step index themselves, with the same arithmetic as the advance, which the last block to
+// finish applies once every other block is done reading.
+__device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t);
+
+__global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_t *clamped, double *clamped_disp) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < v.P) {
+    DevPart &P = v.parts[k];
+    const DevSimState &st = v.ss[P.sim];
+    const DevSimParams &sp = v.sp[P.sim];
+    if (st.active) {
+      double wall_next[6];
+      for (int c = 0; c < 6; ++c) wall_next[c] = st.wall[c] + st.spd[c] * sp.dt;  // timeloop.h:791-796
+      const uint32_t tn = st.t + 1;
+      if (v.rec) {
+        end_particle_fp32c(v, k, P, wall_next);
+      } else {
+        unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+        if (P.movable) {
+          for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
+        }
+        for (int c = 0; c < 3; ++c) {
+          L[c] = ord_key(INFINITY);
+          L[3 + c] = ord_key(-INFINITY);
+        }
+      }
+      // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
+      // keeps this step's predicted displacement, saved for the readback (the fused FP32 form
+      // zeroes them in its corrector and keeps this step's displacement buffer intact)
+      if (clamped_ptr && !v.fused) {
+        double jump = 0;
+        for (uint32_t c = clamped_ptr[k]; c < clamped_ptr[k + 1]; ++c) {
+          uint64_t g = clamped[c];
+          D3 d = ld3(v.disp, g, v.Ncap);
+          clamped_disp[3 * (uint64_t)c] = d.x;
+          clamped_disp[3 * (uint64_t)c + 1] = d.y;
+          clamped_disp[3 * (uint64_t)c + 2] = d.z;
+          if (P.movable) {
+            jump = fmax(jump, norm3(d));
+            st3(v.disp, g, v.Ncap, d3(0.0, 0.0, 0.0));
+            st3(v.vel_out, g, v.Ncap, d3(0.0, 0.0, 0.0));
+            st3(v.acc, g, v.Ncap, d3(0.0, 0.0, 0.0));
+          }
+        }
+        if (jump > 0) atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(jump));
+      }
+      // per-particle toggles for the next step (timeloop.h:481-498)
+      const uint32_t kl = k - sp.p0;
+      if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
+        P.movable = 1;
+      if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
+          (uint32_t)sp.set_stoppable_ts == tn)
+        P.stoppable = 1;
+      // FP32 form: does any node of this particle need FP64 non-bond work next step besides
+      // contact (which the contact-node list covers)? External force, torque, or a wall within
+      // the contact radius of the particle's box grown by this step's movement bound
+      // (k_extra32 then tests each node exactly).
+      if (v.xparts) {
+        const bool torque_next = st.torque || (sp.set_torque_ts != -1 && tn == (uint32_t)sp.set_torque_ts);
+        bool need = (P.movable && P.has_ext) || torque_next;
+        if (!need && P.movable && P.stoppable && sp.allow_wall) {
+          const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);
+          const double lim = sp.Rc * 1.001 + 2.0 * move + 1e-12;
+          const double *b = v.lrtb + 6 * (uint64_t)k;
+          for (int f = 0; f < 6 && !need; ++f) {
+            const int c = f % 3;
+            need = (b[c] - lim <= wall_next[f]) && (b[3 + c] + lim >= wall_next[f]);
+          }
+        }
+        if (need) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;
+      }
+    }
+  }
+  // the last block to finish advances the simulations and the step counters
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&v.cnt->end_blocks, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (uint32_t s = threadIdx.x; s < v.S; s += blockDim.x) {
     const DevSimParams &sp = v.sp[s];
     DevSimState &st = v.ss[s];
     if (st.active) {
@@ -389,7 +402,7 @@ __global__ void k_end_sims(DevView v, double half_skin) {
       apply_sim_toggles(sp, st, st.t);
     }
   }
-  if (s == 0) {
+  if (threadIdx.x == 0) {
     DevCounters &c = *v.cnt;
     double stepmax = __longlong_as_double((long long)c.stepmax_bits);
     if (c.rebuild) {
@@ -399,12 +412,10 @@ __global__ void k_end_sims(DevView v, double half_skin) {
     } else {
       c.moved += stepmax;
     }
-    // clamped-node jumps recorded after the rebuild test count towards the next one
     c.last_stepmax = stepmax;
     c.stepmax_bits = 0;
-    if (v.xcount) v.xcount[1] = 0;  // k_end_particles lists the particles of the next step
     c.rebuild = 0;
-    (void)half_skin;
+    c.end_blocks = 0;
   }
 }
 
@@ -412,8 +423,7 @@ void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamp
                      cudaStream_t s) {
   const uint32_t *cptr = n_clamped ? clamped : nullptr;
   const uint32_t *clist = n_clamped ? clamped + (v.P + 1) : nullptr;
-  k_end_sims<<<(v.S + 127) / 128, 128, 0, s>>>(v, 0.0);
-  k_end_particles<<<(v.P + 127) / 128, 128, 0, s>>>(v, cptr, clist, clamped_disp);
+  k_end_step<<<(v.P + 127) / 128, 128, 0, s>>>(v, cptr, clist, clamped_disp);
 }
 
 // ------------------------------------------------------------------------------------
@@ -579,6 +589,7 @@ __global__ void k_reset_y(DevView v) {
     }
     const double dest = (max_bulk_y + sp.wheel_rad) + sp.Rc;
     move = dest - m0[1];
+    v.cnt->xall = 1;  // particle 0 moved: the non-bond work lists are stale for this step
     if (v.fused) {  // the FP32 form keeps positions relative to the particle's anchor
       DevPart &Pw = v.parts[sp.p0];
       Pw.anchor_pos[1] = Pw.anchor_pos[1] + move;
