@@ -519,10 +519,10 @@ def ours(args):
     if r == 0 and world == 1 and args.serve > 0:
         serving = serving_run(args)
 
-    # our kernels per step: bp_decide, k_extra32 (unless fused), k_bond32, k_end_sims,
-    # k_end_particles; the 7 broad-phase kernels run only in rebuild steps when the step graph
-    # holds them in a conditional node, else every step (exiting at once unless due)
-    per_step = 4 if 6 <= variant <= 9 else 5  # variants 6-9 fuse k_extra32 into the bond kernel
+    # our kernels per step: k_bp_decide, k_extra32 (unless fused into the bond kernel: variants
+    # 6-9), the bond kernel, k_end_step; the 7 broad-phase kernels run only in rebuild steps when
+    # the step graph holds them in a conditional node, else every step (exiting at once unless due)
+    per_step = 3 if 6 <= variant <= 9 else 4
     bp = 7 * (sim.rebuilds_timed if graph_mode == 2 else K)
     gpu_launches = per_step * K + bp
     line = {
