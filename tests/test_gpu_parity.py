@@ -91,7 +91,8 @@ def test_two_sphere_full_size_bitexact():
         np.testing.assert_array_equal(a[k], b[k])
 
 
-@pytest.mark.parametrize("name", ["impact_free", "cubes_gravity", "impact_walls", "prescribed"])
+@pytest.mark.parametrize("name", ["impact_free", "cubes_gravity", "impact_walls", "prescribed", "toggles",
+                                  "bdry_only", "notched"])
 def test_fp32c_within_tolerance(name):
     s, cfg = cases.CASES[name]()
     steps = cfg["timesteps"]
