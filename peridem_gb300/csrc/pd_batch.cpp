@@ -42,22 +42,10 @@ uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision,
     ncl += s.clamped.size();
   }
   const uint64_t C = up32(N), nsl = C / 32;
+  std::vector<uint32_t> file_of, node_of, deg_file;
+  order_nodes(sims, file_of, node_of, deg_file);
   std::vector<uint32_t> deg(C, 0);
-  uint64_t g = 0;
-  for (auto &s : sims) {
-    for (uint32_t p = 0; p < s.np; ++p) {
-      const uint64_t g0 = g + s.node_offset[p];
-      const uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
-      for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
-        const uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
-        if (i < nloc && j < nloc) {
-          deg[g0 + i]++;
-          deg[g0 + j]++;
-        }
-      }
-    }
-    g += s.node_offset[s.np];
-  }
+  for (uint64_t n = 0; n < N; ++n) deg[n] = deg_file[file_of[n]];
   uint64_t E = 0;
   for (uint64_t sl = 0; sl < nsl; ++sl) {
     uint32_t w = 0;
@@ -69,6 +57,7 @@ uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision,
   b += (nsl + 1) * 8 + C * 2 + atleast1(E) * 4 + atleast1(E / 32) * 4;
   // node state, particles, simulations
   b += 7 * 3 * C * 8 + C * 8 + C * 4 + C;
+  b += 2 * C * 4;  // node order maps
   b += P * sizeof(DevPart) + 6 * P * 8 * 2 + 3 * P * 8;
   b += S * sizeof(DevSimParams) + S * sizeof(DevSimState) + sizeof(DevCounters);
   if (ncl) b += (P + 1 + ncl) * 4 + 3 * ncl * 8;
@@ -98,15 +87,18 @@ int Engine::sim_range(uint32_t sim, uint64_t *node0, uint64_t *n_nodes, uint32_t
   return PD_OK;
 }
 
-// [3][Ncap] device array, nodes [node0, node0+nn) -> nn*3 row vectors.
+// [3][Ncap] device array, engine nodes [node0, node0+nn) -> nn*3 row vectors in file order
+// (a simulation's node range is the same in both numberings).
 int Engine::read_nodes(const double *d, uint64_t node0, uint64_t nn, double *dst) {
   std::vector<double> buf(3 * nn);
   for (int c = 0; c < 3; ++c)
     PD_TRY(check(cudaMemcpyAsync(buf.data() + c * nn, d + c * Ncap_ + node0, nn * 8, cudaMemcpyDeviceToHost, stream_),
                  "read state"));
   PD_TRY(check(cudaStreamSynchronize(stream_), "read state"));
-  for (uint64_t k = 0; k < nn; ++k)
-    for (int c = 0; c < 3; ++c) dst[3 * k + c] = buf[c * nn + k];
+  for (uint64_t k = 0; k < nn; ++k) {
+    const uint64_t f = file_of_[node0 + k] - node0;
+    for (int c = 0; c < 3; ++c) dst[3 * f + c] = buf[c * nn + k];
+  }
   return PD_OK;
 }
 

@@ -173,7 +173,7 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
   long long cx, cy, cz;
   double x, y, z;
   node_cell(v, n, sp.cell, cx, cy, cz, x, y, z);
-  uint32_t list[kMaxCand];
+  uint32_t list[kMaxCand];  // file indices: the reference visits contact partners in its numbering
   int cnt = 0;
   bool overflow = false;
   for (int dz = -1; dz <= 1; ++dz)
@@ -190,22 +190,23 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
           double mz = v.pos[m + 2 * v.Ncap] + v.disp[m + 2 * v.Ncap];
           double ddx = mx - x, ddy = my - y, ddz = mz - z;
           if (ddx * ddx + ddy * ddy + ddz * ddz > sp.cand_r2) continue;
-          // insert keeping ascending order; drop duplicates (hash collisions can make two
-          // stencil cells share a bucket)
+          // insert keeping ascending file order; drop duplicates (hash collisions can make
+          // two stencil cells share a bucket)
+          const uint32_t fm = v.file_of[m];
           int pos = cnt;
-          while (pos > 0 && list[pos - 1] > m) --pos;
-          if (pos > 0 && list[pos - 1] == m) continue;
+          while (pos > 0 && list[pos - 1] > fm) --pos;
+          if (pos > 0 && list[pos - 1] == fm) continue;
           if (cnt >= (int)cap) {
             overflow = true;
             continue;
           }
           for (int q = cnt; q > pos; --q) list[q] = list[q - 1];
-          list[pos] = m;
+          list[pos] = fm;
           ++cnt;
         }
       }
   uint32_t *out = cand + n * cap;
-  for (int i = 0; i < cnt; ++i) out[i] = list[i];
+  for (int i = 0; i < cnt; ++i) out[i] = v.node_of[list[i]];
   cand_n[n] = (uint16_t)cnt;
   if (cnt && v.xnodes) v.xnodes[atomicAdd(&v.xcount[0], 1u)] = (uint32_t)n;  // FP32 form: work list
   if (overflow) atomicOr(&v.cnt->err, PD_DERR_CAND_OVERFLOW);

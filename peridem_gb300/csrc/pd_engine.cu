@@ -89,6 +89,8 @@ DevView Engine::view(int cur) const {
   v.ext = d_ext_;
   v.vol = d_vol_;
   v.pid = d_pid_;
+  v.node_of = d_node_of_;
+  v.file_of = d_file_of_;
   v.bdry = d_bdry_;
   v.slice_ptr = d_slice_ptr_;
   v.deg = d_deg_;
@@ -188,6 +190,10 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   sim_steps_.assign(S_, 0);
   finished_.assign(S_, 0);
   final_.assign(S_, std::vector<double>());
+  {
+    std::vector<uint32_t> deg_file;
+    order_nodes(sims_, file_of_, node_of_, deg_file);
+  }
   PD_TRY(check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate"));
   own_stream_ = true;
   capture_stream_ = stream_;
@@ -213,6 +219,57 @@ void parallel_items(uint64_t n, F f) {
   for (auto &x : th) x.join();
 }
 }  // namespace
+
+void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
+                         std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file) {
+  // The SELL-32 layout pads every row of a slice to the slice's longest row. In file order a
+  // slice mixes interior nodes (full neighbourhoods) with surface nodes (truncated ones);
+  // sorting by bond count makes the rows of a slice nearly equal (crush512: padded entries
+  // 1.23x the bonds in file order, 1.03x sorted). The sort runs inside windows of
+  // kOrderWindow consecutive nodes of a particle and is stable, so a node moves less than a
+  // window and interior nodes keep their lattice order: partners stay close in memory (a
+  // whole-particle sort of a 1.5 M-node plate made the FP32 bond kernel slower).
+  // Per-node results do not depend on the order: each node's sums keep the reference's row
+  // order, and every sequence that the reference takes in node order (contact partners,
+  // particle means) is taken in file order through node_of / file_of.
+  struct PartRef {
+    const HostSim *s;
+    uint32_t p;
+    uint64_t g0;
+  };
+  std::vector<PartRef> parts;
+  uint64_t N = 0;
+  for (auto &s : sims) {
+    for (uint32_t p = 0; p < s.np; ++p) parts.push_back({&s, p, N + s.node_offset[p]});
+    N += s.node_offset[s.np];
+  }
+  deg_file.assign(N, 0);
+  file_of.assign(N, 0);
+  node_of.assign(N, 0);
+  parallel_items(parts.size(), [&](uint64_t x) {
+    const HostSim &s = *parts[x].s;
+    const uint32_t p = parts[x].p;
+    const uint64_t g0 = parts[x].g0;
+    const uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
+    uint32_t *dg = deg_file.data() + g0;
+    for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
+      const uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
+      if (i < nloc && j < nloc) {
+        dg[i]++;
+        dg[j]++;
+      }
+    }
+    std::vector<uint32_t> idx(nloc);
+    for (uint64_t k = 0; k < nloc; ++k) idx[k] = (uint32_t)k;
+    for (uint64_t w0 = 0; w0 < nloc; w0 += kOrderWindow)
+      std::stable_sort(idx.begin() + w0, idx.begin() + std::min<uint64_t>(nloc, w0 + kOrderWindow),
+                       [&](uint32_t a, uint32_t b) { return dg[a] > dg[b]; });
+    for (uint64_t k = 0; k < nloc; ++k) {
+      file_of[g0 + k] = (uint32_t)(g0 + idx[k]);
+      node_of[g0 + idx[k]] = (uint32_t)(g0 + k);
+    }
+  });
+}
 
 int Engine::build_bonds() {
   // conn2NArr (load_hdf5.h:27-37): for every Connectivity row (i, j) push j onto row i and
@@ -244,8 +301,8 @@ int Engine::build_bonds() {
         bad = (int64_t)p;
         return;
       }
-      deg[g0 + i]++;
-      deg[g0 + j]++;
+      deg[node_of_[g0 + i]]++;
+      deg[node_of_[g0 + j]]++;
     }
   });
   if (bad >= 0) {
@@ -286,7 +343,7 @@ int Engine::build_bonds() {
     const uint32_t p = parts[x].p;
     const uint64_t g0 = parts[x].g0;
     for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
-      const uint64_t a = g0 + s.conn[2 * l], b = g0 + s.conn[2 * l + 1];
+      const uint64_t a = node_of_[g0 + s.conn[2 * l]], b = node_of_[g0 + s.conn[2 * l + 1]];
       col[h_slice_ptr_[a >> 5] + 32ull * fill[a] + (a & 31)] = (uint32_t)b;
       fill[a]++;
       col[h_slice_ptr_[b >> 5] + 32ull * fill[b] + (b & 31)] = (uint32_t)a;
@@ -342,7 +399,7 @@ int Engine::alloc_and_upload() {
   std::vector<DevPart> parts(P_);
   std::vector<DevSimParams> sps(S_);
   std::vector<DevSimState> sss(S_);
-  std::vector<uint32_t> clamped_ptr(P_ + 1, 0), clamped_list;
+  std::vector<uint32_t> clamped_ptr(P_ + 1, 0), clamped_list, clamped_file;
   h_g0_.assign(P_, 0);
   uint64_t gnode = 0;
   uint32_t gpart = 0;
@@ -353,7 +410,7 @@ int Engine::alloc_and_upload() {
     const pd_config &cf = s.cfg;
     const uint64_t ns = s.node_offset[s.np];
     for (uint64_t k = 0; k < ns; ++k) {
-      uint64_t g = gnode + k;
+      const uint64_t g = node_of_[gnode + k];
       for (int c = 0; c < 3; ++c) {
         pos[c * C + g] = s.pos[3 * k + c];
         disp[c * C + g] = s.disp[3 * k + c];
@@ -393,11 +450,22 @@ int Engine::alloc_and_upload() {
       h_g0_[gp] = P.g0;
       for (uint32_t k = 0; k < P.n; ++k) h_pid_[P.g0 + k] = gp;
       if (!s.bdry_offset.empty())
-        for (uint64_t l = s.bdry_offset[p]; l < s.bdry_offset[p + 1]; ++l) bdry[P.g0 + s.bdry[l]] = 1;
+        for (uint64_t l = s.bdry_offset[p]; l < s.bdry_offset[p + 1]; ++l) {
+          if (s.bdry[l] >= P.n) {
+            err = "bdry_nodes index out of range in particle " + std::to_string(p);
+            return PD_EINVAL;
+          }
+          bdry[node_of_[P.g0 + s.bdry[l]]] = 1;
+        }
       clamped_ptr[gp + 1] = clamped_ptr[gp];
       if (!s.clamped_offset.empty())
         for (uint64_t l = s.clamped_offset[p]; l < s.clamped_offset[p + 1]; ++l) {
-          clamped_list.push_back(P.g0 + s.clamped[l]);
+          if (s.clamped[l] >= P.n) {
+            err = "clamped_nodes index out of range in particle " + std::to_string(p);
+            return PD_EINVAL;
+          }
+          clamped_list.push_back(node_of_[P.g0 + s.clamped[l]]);
+          clamped_file.push_back(P.g0 + s.clamped[l]);
           clamped_ptr[gp + 1]++;
         }
     }
@@ -505,6 +573,8 @@ int Engine::alloc_and_upload() {
   PD_TRY(dalloc(this, allocs_, &d_ext_, 3 * C, err));
   PD_TRY(dalloc(this, allocs_, &d_vol_, C, err));
   PD_TRY(dalloc(this, allocs_, &d_pid_, C, err));
+  PD_TRY(dalloc(this, allocs_, &d_node_of_, C, err));
+  PD_TRY(dalloc(this, allocs_, &d_file_of_, C, err));
   PD_TRY(dalloc(this, allocs_, &d_bdry_, C, err));
   PD_TRY(dalloc(this, allocs_, &d_parts_, P_, err));
   PD_TRY(dalloc(this, allocs_, &d_lrtb_, 6ull * P_, err));
@@ -523,6 +593,15 @@ int Engine::alloc_and_upload() {
   PD_TRY(up(d_ext_, ext.data(), 3 * C * 8, "upload extforce"));
   PD_TRY(up(d_vol_, vol.data(), C * 8, "upload vol"));
   PD_TRY(up(d_pid_, h_pid_.data(), C * 4, "upload pid"));
+  {
+    std::vector<uint32_t> no(C), fo(C);
+    for (uint64_t g = 0; g < C; ++g) {
+      no[g] = g < N_ ? node_of_[g] : (uint32_t)g;
+      fo[g] = g < N_ ? file_of_[g] : (uint32_t)g;
+    }
+    PD_TRY(up(d_node_of_, no.data(), C * 4, "upload node order"));
+    PD_TRY(up(d_file_of_, fo.data(), C * 4, "upload node order"));
+  }
   PD_TRY(up(d_bdry_, bdry.data(), C, "upload bdry"));
   PD_TRY(up(d_parts_, parts.data(), P_ * sizeof(DevPart), "upload particles"));
   PD_TRY(up(d_sp_, sps.data(), S_ * sizeof(DevSimParams), "upload sim params"));
@@ -539,7 +618,7 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_clamped_, cl.size(), err));
     PD_TRY(up(d_clamped_, cl.data(), cl.size() * 4, "upload clamped"));
     PD_TRY(dalloc(this, allocs_, &d_clamped_disp_, 3 * n_clamped_, err));
-    h_clamped_ = clamped_list;
+    h_clamped_ = clamped_file;
   }
 
   if (pv_possible_) {
@@ -835,9 +914,9 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
   const uint64_t C = Ncap_;
   std::vector<double> buf(3 * C);
   auto scatter = [&](double *dst) {
-    // [3][Ncap] device layout -> N*3 row vectors
+    // [3][Ncap] device layout, engine order -> N*3 row vectors, file order
     for (uint64_t n = 0; n < N_; ++n)
-      for (int c = 0; c < 3; ++c) dst[3 * n + c] = buf[c * C + n];
+      for (int c = 0; c < 3; ++c) dst[3 * (uint64_t)file_of_[n] + c] = buf[c * C + n];
   };
   auto fetch = [&](const double *d, double *dst) -> int {
     PD_TRY(cpy(buf.data(), d, 3 * C * 8, "read state"));
@@ -889,7 +968,7 @@ int Engine::set_state(const double *disp, const double *vel, const double *acc) 
   std::vector<double> buf(3 * C, 0.0);
   auto put = [&](double *d, const double *src) -> int {
     for (uint64_t n = 0; n < N_; ++n)
-      for (int c = 0; c < 3; ++c) buf[c * C + n] = src[3 * n + c];
+      for (int c = 0; c < 3; ++c) buf[c * C + node_of_[n]] = src[3 * n + c];
     return cpy(d, buf.data(), 3 * C * 8, "write state");
   };
   const bool fused = precision_ == PD_FP32C;
@@ -936,13 +1015,13 @@ int Engine::get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, u
     PD_TRY(cpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, "read mask"));
   }
   uint64_t c = 0;
-  for (uint64_t i = 0; i < nloc; ++i) {
-    const uint64_t g = g0 + i;
+  for (uint64_t i = 0; i < nloc; ++i) {  // file order
+    const uint64_t g = node_of_[g0 + i];
     const uint64_t base = h_slice_ptr_[g >> 5] - e0 + (g & 31);
     const uint64_t mbase = (h_slice_ptr_[g >> 5] - e0) >> 5;
     for (uint32_t j = 0; j < h_deg_[g]; ++j) {
       if (!((mask[mbase + j] >> (g & 31)) & 1u)) continue;
-      uint64_t q = col[base + 32ull * j] - g0;
+      uint64_t q = file_of_[col[base + 32ull * j]] - g0;
       if (i < q) {
         if (pairs && c < cap) {
           pairs[2 * c] = (uint32_t)i;
@@ -1106,7 +1185,7 @@ int Engine::get_afd(double *afd) {
   std::vector<double> buf(3 * Ncap_);
   PD_TRY(cpy(buf.data(), d_afd_, 3 * Ncap_ * 8, "read applied force density"));
   for (uint64_t n = 0; n < N_; ++n)
-    for (int c = 0; c < 3; ++c) afd[3 * n + c] = buf[c * Ncap_ + n];
+    for (int c = 0; c < 3; ++c) afd[3 * (uint64_t)file_of_[n] + c] = buf[c * Ncap_ + n];
   return PD_OK;
 }
 
@@ -1164,12 +1243,12 @@ int Engine::set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t 
   PD_TRY(cpy(col.data(), d_col_ + e0, (e1 - e0) * 4, "read col"));
   PD_TRY(cpy(mask.data(), d_mask_ + e0 / 32, (e1 - e0) / 32 * 4, "read mask"));
   for (uint64_t i = 0; i < nloc; ++i) {
-    const uint64_t g = g0 + i;
+    const uint64_t g = node_of_[g0 + i];
     const uint64_t base = h_slice_ptr_[g >> 5] - e0 + (g & 31);
     const uint64_t mbase = (h_slice_ptr_[g >> 5] - e0) >> 5;
     const uint32_t bit = 1u << (g & 31);
     for (uint32_t j = 0; j < h_deg_[g]; ++j) {
-      uint64_t q = col[base + 32ull * j] - g0;
+      uint64_t q = file_of_[col[base + 32ull * j]] - g0;
       uint64_t a = std::min<uint64_t>(i, q), b = std::max<uint64_t>(i, q);
       const bool live = std::binary_search(keys.begin(), keys.end(), a * nloc + b);
       if (live)

@@ -1,7 +1,10 @@
 // pd_engine.h -- device data layout and host engine of the GB300 explicit step.
 //
-// Layout in HBM (all particles of all simulations of a batch concatenated in file order;
-// node n of particle p is global node node_offset[p] + local index):
+// Layout in HBM (all particles of all simulations of a batch concatenated in file order; the
+// nodes of particle p occupy the engine indices [node_offset[p], node_offset[p+1]) as in the
+// file, but inside each window of kOrderWindow of them they are sorted by descending bond
+// count (stable), so that the 32 rows of a SELL slice have nearly equal lengths; node_of /
+// file_of map the two numberings and every host-facing array is in file order):
 //   * node state, FP64 structure-of-arrays: pos/disp/vel/acc/force/extforce as [3][Ncap]
 //     (x block, y block, z block), vol[N]; vel is double-buffered (the fused kernel reads
 //     partners' step-start velocity while it writes the corrected one);
@@ -19,7 +22,7 @@
 //     particle's anchor node;
 //   * contact broad phase: hashed cell list (counting sort) rebuilt only when the nodes may
 //     have moved more than half the skin since the last build; per-node candidate lists
-//     (fixed capacity, ascending global index) of nodes within contact radius + skin.
+//     (fixed capacity, ascending file index) of nodes within contact radius + skin.
 #ifndef PD_ENGINE_H
 #define PD_ENGINE_H
 
@@ -37,6 +40,7 @@ constexpr int kSlice = 32;
 constexpr int kStageNodes = 512;          // nodes per block of the staged bond kernel
 constexpr uint32_t kStageMaxRecords = 6400;  // 200 KB of 32-byte records per block
 constexpr uint32_t kNoCol = 0xFFFFFFFFu;
+constexpr uint64_t kOrderWindow = 1024;     // nodes per window of the bond-count sort (order_nodes)
 
 // Per-particle parameters (ParticleN scalars, particle2.h:51-59).
 struct DevPart {
@@ -115,6 +119,8 @@ struct DevView {
   double *acc, *force;
   const double *ext, *vol;
   const uint32_t *pid;   // particle of each node
+  const uint32_t *node_of;  // file-order global index -> engine index
+  const uint32_t *file_of;  // engine index -> file-order global index
   const uint8_t *bdry;   // 1 if node is in its particle's bdry_nodes list
   // bonds
   const uint64_t *slice_ptr;
@@ -269,6 +275,11 @@ class Engine {
   // before anything is allocated.
   uint64_t device_bytes() const { return device_bytes_; }
   static uint64_t estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap);
+  // Engine node order: inside each window of kOrderWindow nodes of a particle, nodes by
+  // descending bond count (stable: equal counts keep their file order). file_of[engine index] = file index, node_of = its inverse,
+  // deg_file = bond count of each node in file order (indices out of range are not counted).
+  static void order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
+                          std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file);
   int raw_alloc(void **p, size_t bytes);
   double step_bytes(uint64_t live_bonds) const;
   uint64_t initial_bonds() const { return initial_bonds_; }
@@ -334,11 +345,12 @@ class Engine {
   double half_skin_ = 0;
 
   // host mirrors used when reading results back
+  std::vector<uint32_t> file_of_, node_of_;  // see order_nodes
   std::vector<uint32_t> h_pid_;
   std::vector<uint64_t> h_slice_ptr_;
   std::vector<uint16_t> h_deg_;
   std::vector<uint32_t> h_g0_;
-  std::vector<uint32_t> h_clamped_;
+  std::vector<uint32_t> h_clamped_;  // clamped nodes, file-order global indices
   std::vector<uint32_t> h_col_;  // SELL column indices, read back once for staged frames
 
   // device buffers
@@ -349,6 +361,7 @@ class Engine {
   uint8_t *d_clamp_flag_ = nullptr;
   double *d_force_ = nullptr, *d_ext_ = nullptr, *d_vol_ = nullptr;
   uint32_t *d_pid_ = nullptr;
+  uint32_t *d_node_of_ = nullptr, *d_file_of_ = nullptr;
   uint8_t *d_bdry_ = nullptr;
   uint64_t *d_slice_ptr_ = nullptr;
   uint16_t *d_deg_ = nullptr;
@@ -366,7 +379,7 @@ class Engine {
   DevSimParams *d_sp_ = nullptr;
   DevSimState *d_ss_ = nullptr;
   DevCounters *d_cnt_ = nullptr;
-  uint32_t *d_clamped_ = nullptr;  // [P+1] offsets followed by global node ids
+  uint32_t *d_clamped_ = nullptr;  // [P+1] offsets followed by engine node indices
   double *d_clamped_disp_ = nullptr;
   uint64_t n_clamped_ = 0;
   double *d_afd_ = nullptr;

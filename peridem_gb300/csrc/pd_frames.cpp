@@ -71,9 +71,9 @@ void Engine::frame_state(const HostFrame &f, double *curpos, double *vel, double
                          double *afd) const {
   const uint64_t C = Ncap_;
   const bool fused = precision_ == PD_FP32C;
-  auto rows = [&](const double *src, double *dst) {
+  auto rows = [&](const double *src, double *dst) {  // engine order -> file order
     for (uint64_t n = 0; n < N_; ++n)
-      for (int c = 0; c < 3; ++c) dst[3 * n + c] = src[c * C + n];
+      for (int c = 0; c < 3; ++c) dst[3 * (uint64_t)file_of_[n] + c] = src[c * C + n];
   };
   if (curpos) {
     std::vector<double> dsp(3 * N_);
@@ -120,13 +120,13 @@ void Engine::frame_connectivity(const HostFrame &f, uint32_t particle, std::vect
       pacc += s.np;
     }
   }
-  for (uint64_t i = 0; i < nloc; ++i) {
-    const uint64_t g = g0 + i;
+  for (uint64_t i = 0; i < nloc; ++i) {  // file order
+    const uint64_t g = node_of_[g0 + i];
     const uint64_t base = h_slice_ptr_[g >> 5] + (g & 31);
     const uint64_t mbase = h_slice_ptr_[g >> 5] >> 5;
     for (uint32_t j = 0; j < h_deg_[g]; ++j) {
       if (!((f.mask[mbase + j] >> (g & 31)) & 1u)) continue;
-      const uint64_t q = h_col_[base + 32ull * j] - g0;
+      const uint64_t q = file_of_[h_col_[base + 32ull * j]] - g0;
       if (i < q) {
         pairs.push_back((uint32_t)i);
         pairs.push_back((uint32_t)q);

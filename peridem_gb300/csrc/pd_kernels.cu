@@ -184,8 +184,8 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
   }
 
   // ---- node-node contact of particle pairs (timeloop.h:636-651, contact.h:754-937):
-  // partners in ascending global index; a partner in a lower particle index acts as the
-  // "C" node of the pair (reaction form), a partner in a higher index as the "N" node.
+  // partners in ascending file-order global index; a partner in a lower particle index acts as
+  // the "C" node of the pair (reaction form), a partner in a higher index as the "N" node.
   if (run && P.stoppable && (!sp.nl_bdry_only || bdry_i)) {
     const uint32_t *cl = v.cand + nn * v.cand_cap;
     const int nc = v.cand_n[nn];
@@ -429,7 +429,7 @@ void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamp
 // ------------------------------------------------------------------------------------
 // auxiliary kernels
 
-// mean_CurrPos per particle (particle2.h:94-103): a sequential sum in node order.
+// mean_CurrPos per particle (particle2.h:94-103): a sequential sum in file node order.
 __global__ void k_centroids(DevView v) {
   const uint32_t k = blockIdx.x;
   const int c = threadIdx.x;
@@ -438,7 +438,10 @@ __global__ void k_centroids(DevView v) {
   if (!v.ss[P.sim].torque) return;
   double m = 0.0;
   const double *pp = v.pos + c * v.Ncap, *dd = v.disp + c * v.Ncap;
-  for (uint32_t i = 0; i < P.n; ++i) m = m + (pp[P.g0 + i] + dd[P.g0 + i]);
+  for (uint32_t i = 0; i < P.n; ++i) {
+    const uint32_t g = v.node_of[P.g0 + i];
+    m = m + (pp[g] + dd[g]);
+  }
   const_cast<double *>(v.centroid)[3 * (uint64_t)k + c] = m / (double)P.n;
 }
 
@@ -451,7 +454,7 @@ void launch_centroids(const DevView &v, cudaStream_t s) {
 // (fix_velocity_mean_x) and the rest (fix_velocity_angular: rotation about z at the
 // prescribed rate, about mean_CurrPos) are replaced. applied_force_density =
 // rho*((2/dt)*(pv - vel) - acc_old) - force, with vel already equal to pv (as in the
-// reference). The means are sequential sums in node order, like Eigen's += loop.
+// reference). The means are sequential sums in file node order, like Eigen's += loop.
 __global__ void k_prescribed(DevView v) {
   const uint32_t s = blockIdx.x;
   if (s >= v.S) return;
@@ -465,11 +468,14 @@ __global__ void k_prescribed(DevView v) {
   __shared__ double sh[6];
   if (threadIdx.x == 0) {
     D3 mv = d3(0.0, 0.0, 0.0), mp = d3(0.0, 0.0, 0.0);
-    for (uint32_t i = 0; i < P.n; ++i) mv = mv + ld3(v.vel_out, P.g0 + i, C3);
+    for (uint32_t i = 0; i < P.n; ++i) mv = mv + ld3(v.vel_out, v.node_of[P.g0 + i], C3);
     const double nn = (double)P.n;
     mv = d3(mv.x / nn, mv.y / nn, mv.z / nn);
     if (sp.fix_angular) {  // mean_CurrPos (particle2.h:94-103)
-      for (uint32_t i = 0; i < P.n; ++i) mp = mp + (ld3(v.pos, P.g0 + i, C3) + ld3(v.disp, P.g0 + i, C3));
+      for (uint32_t i = 0; i < P.n; ++i) {
+        const uint32_t g = v.node_of[P.g0 + i];
+        mp = mp + (ld3(v.pos, g, C3) + ld3(v.disp, g, C3));
+      }
       mp = d3(mp.x / nn, mp.y / nn, mp.z / nn);
     }
     sh[0] = mv.x;
@@ -553,8 +559,10 @@ __global__ void k_reset_y(DevView v) {
   __shared__ double move;
   if (threadIdx.x == 0) {
     D3 m = d3(0.0, 0.0, 0.0);
-    for (uint32_t i = 0; i < P0.n; ++i)
-      m = m + (ld3(v.pos, P0.g0 + i, C3) + disp_after_corrector(v, P0.g0 + i, st.t));
+    for (uint32_t i = 0; i < P0.n; ++i) {  // file node order
+      const uint32_t g = v.node_of[P0.g0 + i];
+      m = m + (ld3(v.pos, g, C3) + disp_after_corrector(v, g, st.t));
+    }
     const double nn = (double)P0.n;
     m0[0] = m.x / nn;
     m0[1] = m.y / nn;
@@ -583,9 +591,9 @@ __global__ void k_reset_y(DevView v) {
     double max_bulk_y;
     if (found) {
       max_bulk_y = ord_val(best);
-    } else {  // the reference's initial value: pos[0] of particle 1 plus disp[1]
+    } else {  // the reference's initial value: pos[0] of particle 1 plus disp[1] (file order)
       const uint64_t j = P1.n > 1 ? 1 : 0;
-      max_bulk_y = v.pos[P1.g0 + C3] + disp_after_corrector(v, P1.g0 + j, st.t).y;
+      max_bulk_y = v.pos[v.node_of[P1.g0] + C3] + disp_after_corrector(v, v.node_of[P1.g0 + j], st.t).y;
     }
     const double dest = (max_bulk_y + sp.wheel_rad) + sp.Rc;
     move = dest - m0[1];
