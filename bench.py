@@ -443,10 +443,10 @@ def ours(args):
         v64 = sum_over_ranks(dist, K64 * 0.5 * (l0 + l1)) / (ms64 * 1e-3)
         ph64 = sim64.profile(3) / 3
         ach64 = (4.125 * sim64.live_bonds() + 224.0 * s.n_nodes) / (ph64[2] * 1e-3) / 1e9
-        # FP64 operations per bond in k_step, counted from its source: eta (6 add), |eta| (3 mul,
-        # 2 add, IEEE sqrt ~9), stretch (1 add + Markstein division 3), magnitude (2 mul),
-        # RN(1/|eta|) (~5), unit vector (3 divisions, 9), accumulation (3 mul, 3 add), test (1)
-        ops_per_bond = 47
+        # FP64 add + multiply + fused multiply-add thread instructions per directed bond of
+        # k_step, counted by ncu on crush512 (sass_thread_inst_executed_op_{dadd,dmul,dfma}:
+        # 3.41e9 per launch, 7.52e7 bonds)
+        ops_per_bond = 45.4
         fp64 = {"value": v64, "unit": UNIT, "steps": K64, "ms_per_step": ms64 / K64,
                 "kernel_ms": ph64[2], "roofline_hbm_frac": ach64 / peak,
                 "fp64_ops_per_s": v64 * ops_per_bond, "fp64_ops_per_bond": ops_per_bond,
