@@ -18,7 +18,7 @@ namespace pdg {
 
 int set_global_error(int rc, const std::string &msg) { return fail_global(rc, msg); }
 
-// Copies caller arrays into a HostSim (the particle vector the reference loads in
+// Reads caller arrays into a HostSim (the particle vector the reference loads in
 // load_particles<3>, load_hdf5.h:41-113).
 int host_sim_from_arrays(const pd_setup_arrays *su, const pd_config *cfg, HostSim &hs, std::string &err) {
   if (!su || !cfg) {
@@ -64,18 +64,19 @@ int host_sim_from_arrays(const pd_setup_arrays *su, const pd_config *cfg, HostSi
   hs.np = np;
   hs.node_offset.assign(su->node_offset, su->node_offset + np + 1);
   hs.pos.assign(su->pos, su->pos + 3 * N);
-  hs.vol.assign(su->vol, su->vol + N);
-  hs.disp.assign(su->disp, su->disp + 3 * N);
-  hs.vel.assign(su->vel, su->vel + 3 * N);
-  hs.acc.assign(su->acc, su->acc + 3 * N);
-  hs.ext.assign(su->extforce, su->extforce + 3 * N);
+  // read only while the engine is built, which happens before the creating call returns
+  hs.vol.view(su->vol, N);
+  hs.disp.view(su->disp, 3 * N);
+  hs.vel.view(su->vel, 3 * N);
+  hs.acc.view(su->acc, 3 * N);
+  hs.ext.view(su->extforce, 3 * N);
   hs.conn_offset.assign(su->conn_offset, su->conn_offset + np + 1);
   if (M) {
     if (!su->conn) {
       err = "conn missing";
       return PD_EINVAL;
     }
-    hs.conn.assign(su->conn, su->conn + 2 * M);
+    hs.conn.view(su->conn, 2 * M);
   }
   if (su->bdry_offset && su->bdry) {
     hs.bdry_offset.assign(su->bdry_offset, su->bdry_offset + np + 1);

@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <thread>
 
 #include "pd_engine.h"
@@ -197,7 +198,17 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   PD_TRY(check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate"));
   own_stream_ = true;
   capture_stream_ = stream_;
-  return alloc_and_upload();
+  const int rc = alloc_and_upload();
+  // arrays read only while building (possibly views of the caller's buffers)
+  for (auto &s : sims_) {
+    s.vol.release();
+    s.disp.release();
+    s.vel.release();
+    s.acc.release();
+    s.ext.release();
+    s.conn.release();
+  }
+  return rc;
 }
 
 namespace {
@@ -324,17 +335,25 @@ int Engine::build_bonds() {
     h_slice_ptr_[s + 1] = h_slice_ptr_[s] + 32ull * w;
   }
   E_ = h_slice_ptr_[nslices_];
-  std::vector<uint32_t> col(std::max<uint64_t>(E_, 1), kNoCol);
-  std::vector<uint32_t> mask(std::max<uint64_t>(E_ / 32, 1), 0u);
-  parallel_items(nslices_, [&](uint64_t sl) {
+  const uint64_t ncol = std::max<uint64_t>(E_, 1), nmask = std::max<uint64_t>(E_ / 32, 1);
+  std::unique_ptr<uint32_t[]> col(new uint32_t[ncol]), mask(new uint32_t[nmask]);  // every entry set below
+  col[0] = kNoCol;
+  mask[0] = 0u;
+  parallel_items((nslices_ + 63) / 64, [&](uint64_t chunk) {
     // padding entries, and the live bits: position j of lane l is a bond iff j < deg
-    const uint64_t e0 = h_slice_ptr_[sl], e1 = h_slice_ptr_[sl + 1];
-    const uint64_t w = (e1 - e0) / 32;
-    for (uint64_t j = 0; j < w; ++j) {
-      uint32_t bits = 0;
-      for (int l = 0; l < 32; ++l)
-        if (j < deg[sl * 32 + l]) bits |= 1u << l;
-      mask[(e0 >> 5) + j] = bits;
+    for (uint64_t sl = chunk * 64; sl < std::min<uint64_t>(nslices_, chunk * 64 + 64); ++sl) {
+      const uint64_t e0 = h_slice_ptr_[sl], e1 = h_slice_ptr_[sl + 1];
+      const uint64_t w = (e1 - e0) / 32;
+      for (uint64_t j = 0; j < w; ++j) {
+        uint32_t bits = 0;
+        for (int l = 0; l < 32; ++l)
+          if (j < deg[sl * 32 + l]) {
+            bits |= 1u << l;
+          } else {
+            col[e0 + 32 * j + l] = kNoCol;
+          }
+        mask[(e0 >> 5) + j] = bits;
+      }
     }
   });
   std::vector<uint32_t> fill(Ncap_, 0);
@@ -381,19 +400,26 @@ int Engine::build_bonds() {
   }
   PD_TRY(dalloc(this, allocs_, &d_slice_ptr_, nslices_ + 1, err));
   PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));
-  PD_TRY(dalloc(this, allocs_, &d_col_, col.size(), err));
-  PD_TRY(dalloc(this, allocs_, &d_mask_, mask.size(), err));
+  PD_TRY(dalloc(this, allocs_, &d_col_, ncol, err));
+  PD_TRY(dalloc(this, allocs_, &d_mask_, nmask, err));
   PD_TRY(cpy(d_slice_ptr_, h_slice_ptr_.data(), (nslices_ + 1) * 8, "upload slice_ptr"));
   PD_TRY(cpy(d_deg_, h_deg_.data(), Ncap_ * 2, "upload deg"));
-  PD_TRY(cpy(d_col_, col.data(), col.size() * 4, "upload col"));
-  PD_TRY(cpy(d_mask_, mask.data(), mask.size() * 4, "upload mask"));
+  PD_TRY(cpy(d_col_, col.get(), ncol * 4, "upload col"));
+  PD_TRY(cpy(d_mask_, mask.get(), nmask * 4, "upload mask"));
   return PD_OK;
 }
 
 int Engine::alloc_and_upload() {
   const uint64_t C = Ncap_;
-  std::vector<double> pos(3 * C, 0.0), disp(3 * C, 0.0), vel(3 * C, 0.0), acc(3 * C, 0.0), ext(3 * C, 0.0);
-  std::vector<double> vol(C, 0.0);
+  // [3][Ncap] staging in engine order; every entry is written below (padding nodes zero)
+  std::unique_ptr<double[]> pos(new double[3 * C]), disp(new double[3 * C]), vel(new double[3 * C]),
+      acc(new double[3 * C]), ext(new double[3 * C]), vol(new double[C]);
+  for (uint64_t g = N_; g < C; ++g) {
+    for (int c = 0; c < 3; ++c)
+      pos[c * C + g] = disp[c * C + g] = vel[c * C + g] = acc[c * C + g] = ext[c * C + g] = 0.0;
+    vol[g] = 0.0;
+  }
+  std::vector<int32_t> part_ext(P_, 0);  // any non-zero extforce in the particle
   h_pid_.assign(C, 0);
   std::vector<uint8_t> bdry(C, 0);
   std::vector<DevPart> parts(P_);
@@ -409,17 +435,27 @@ int Engine::alloc_and_upload() {
     HostSim &s = sims_[si];
     const pd_config &cf = s.cfg;
     const uint64_t ns = s.node_offset[s.np];
-    for (uint64_t k = 0; k < ns; ++k) {
-      const uint64_t g = node_of_[gnode + k];
-      for (int c = 0; c < 3; ++c) {
-        pos[c * C + g] = s.pos[3 * k + c];
-        disp[c * C + g] = s.disp[3 * k + c];
-        vel[c * C + g] = s.vel[3 * k + c];
-        acc[c * C + g] = s.acc[3 * k + c];
-        ext[c * C + g] = s.ext[3 * k + c];
+    parallel_items((ns + 65535) / 65536, [&](uint64_t chunk) {
+      const uint64_t k0 = chunk * 65536, k1 = std::min<uint64_t>(ns, k0 + 65536);
+      uint32_t p = (uint32_t)(std::upper_bound(s.node_offset.begin(), s.node_offset.begin() + s.np + 1, k0) -
+                              s.node_offset.begin() - 1);
+      for (uint64_t k = k0; k < k1; ++k) {
+        while (k >= s.node_offset[p + 1]) ++p;
+        const uint64_t g = node_of_[gnode + k];
+        int32_t any = 0;
+        for (int c = 0; c < 3; ++c) {
+          pos[c * C + g] = s.pos[3 * k + c];
+          disp[c * C + g] = s.disp[3 * k + c];
+          vel[c * C + g] = s.vel[3 * k + c];
+          acc[c * C + g] = s.acc[3 * k + c];
+          const double e = s.ext[3 * k + c];
+          ext[c * C + g] = e;
+          any |= e != 0.0;
+        }
+        vol[g] = s.vol[k];
+        if (any) __atomic_store_n(&part_ext[gpart + p], 1, __ATOMIC_RELAXED);
       }
-      vol[g] = s.vol[k];
-    }
+    });
     for (uint32_t p = 0; p < s.np; ++p) {
       uint32_t gp = gpart + p;
       DevPart &P = parts[gp];
@@ -436,12 +472,10 @@ int Engine::alloc_and_upload() {
       P.breakable = s.breakable[p];
       P.stoppable = s.stoppable[p];
       P.break_bonds = 1;  // simulate3d.cpp:137-139
-      P.has_ext = 0;
+      P.has_ext = part_ext[gp];
       P.cnot32 = (float)P.cnot;
       P.snot_lo32 = (float)(P.snot * (1.0 - 1e-4));
       P.snot_hi32 = (float)(P.snot * (1.0 + 1e-4));
-      for (uint64_t q = s.node_offset[p]; q < s.node_offset[p + 1] && !P.has_ext; ++q)
-        if (s.ext[3 * q] != 0.0 || s.ext[3 * q + 1] != 0.0 || s.ext[3 * q + 2] != 0.0) P.has_ext = 1;
       if (P.n == 0) {
         err = "particle " + std::to_string(p) + " has no nodes";
         return PD_EINVAL;
@@ -584,14 +618,14 @@ int Engine::alloc_and_upload() {
   PD_TRY(dalloc(this, allocs_, &d_ss_, S_, err));
   PD_TRY(dalloc(this, allocs_, &d_cnt_, 1, err));
   auto up = [&](void *d, const void *h, size_t b, const char *w) { return cpy(d, h, b, w); };
-  PD_TRY(up(d_pos_, pos.data(), 3 * C * 8, "upload pos"));
-  PD_TRY(up(d_disp_, disp.data(), 3 * C * 8, "upload disp"));
-  PD_TRY(up(d_vel_[0], vel.data(), 3 * C * 8, "upload vel"));
-  PD_TRY(up(d_vel_[1], vel.data(), 3 * C * 8, "upload vel"));
-  PD_TRY(up(d_acc_, acc.data(), 3 * C * 8, "upload acc"));
+  PD_TRY(up(d_pos_, pos.get(), 3 * C * 8, "upload pos"));
+  PD_TRY(up(d_disp_, disp.get(), 3 * C * 8, "upload disp"));
+  PD_TRY(up(d_vel_[0], vel.get(), 3 * C * 8, "upload vel"));
+  PD_TRY(up(d_vel_[1], vel.get(), 3 * C * 8, "upload vel"));
+  PD_TRY(up(d_acc_, acc.get(), 3 * C * 8, "upload acc"));
   PD_TRY(mset(d_force_, 0, 3 * C * 8, "memset force"));
-  PD_TRY(up(d_ext_, ext.data(), 3 * C * 8, "upload extforce"));
-  PD_TRY(up(d_vol_, vol.data(), C * 8, "upload vol"));
+  PD_TRY(up(d_ext_, ext.get(), 3 * C * 8, "upload extforce"));
+  PD_TRY(up(d_vol_, vol.get(), C * 8, "upload vol"));
   PD_TRY(up(d_pid_, h_pid_.data(), C * 4, "upload pid"));
   {
     std::vector<uint32_t> no(C), fo(C);
@@ -634,17 +668,19 @@ int Engine::alloc_and_upload() {
     PD_TRY(dalloc(this, allocs_, &d_brxin_, std::max<uint64_t>(E_, 1), err));
   } else {
     std::vector<Rec32> r32(C);
-    for (uint64_t g = 0; g < C; ++g) {
-      Rec32 &r = r32[g];
-      r.u = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (g < N_) {
-        const DevPart &P = parts[h_pid_[g]];
-        r.p = make_float4((float)(pos[g] - P.anchor_pos[0]), (float)(pos[C + g] - P.anchor_pos[1]),
-                          (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)vol[g]);
-      } else {
-        r.p = make_float4(0.f, 0.f, 0.f, 0.f);
+    parallel_items((C + 65535) / 65536, [&](uint64_t chunk) {
+      for (uint64_t g = chunk * 65536; g < std::min<uint64_t>(C, chunk * 65536 + 65536); ++g) {
+        Rec32 &r = r32[g];
+        r.u = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (g < N_) {
+          const DevPart &P = parts[h_pid_[g]];
+          r.p = make_float4((float)(pos[g] - P.anchor_pos[0]), (float)(pos[C + g] - P.anchor_pos[1]),
+                            (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)vol[g]);
+        } else {
+          r.p = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
       }
-    }
+    });
     for (int b = 0; b < 2; ++b) {
       PD_TRY(dalloc(this, allocs_, &d_rec_[b], C, err));
       if (reinterpret_cast<uintptr_t>(d_rec_[b]) % 32) {  // the bond kernel reads records with 256-bit loads

@@ -198,14 +198,39 @@ struct HostFrame {
   cudaEvent_t done = nullptr;
 };
 
+// An array the engine reads only while it is built (Engine::init, estimate_bytes): it either
+// owns its elements or views the caller's, which then must stay valid until the call that
+// builds the engine returns. Engine::init releases it afterwards.
+template <class T>
+struct InitArray {
+  std::vector<T> own;
+  const T *ext = nullptr;
+  size_t n_ext = 0;
+  const T *data() const { return ext ? ext : own.data(); }
+  size_t size() const { return ext ? n_ext : own.size(); }
+  bool empty() const { return size() == 0; }
+  const T &operator[](size_t i) const { return data()[i]; }
+  void view(const T *p, size_t n) {
+    own.clear();
+    ext = p;
+    n_ext = n;
+  }
+  void release() {
+    std::vector<T>().swap(own);
+    ext = nullptr;
+    n_ext = 0;
+  }
+};
+
 // Host-side description of one simulation (setup + resolved config).
 struct HostSim {
   pd_config cfg;
   uint32_t np = 0;
   std::vector<uint64_t> node_offset;
-  std::vector<double> pos, vol, disp, vel, acc, ext;     // N*3 / N
+  std::vector<double> pos;                        // N*3, kept (CurrPos = pos + disp on output)
+  InitArray<double> vol, disp, vel, acc, ext;     // N / N*3
   std::vector<uint64_t> conn_offset;
-  std::vector<uint32_t> conn;
+  InitArray<uint32_t> conn;
   std::vector<uint64_t> bdry_offset, clamped_offset;
   std::vector<uint32_t> bdry, clamped;
   std::vector<double> delta, rho, cnot, snot, tval;

@@ -110,12 +110,12 @@ int load_setup(const std::string &fn, pdg::HostSim &hs, std::string &err) {
         !scalar("torque_axis", tax) || !scalar("torque_val", tval))
       return PD_EIO;
     hs.pos.insert(hs.pos.end(), pos.begin(), pos.end());
-    hs.vol.insert(hs.vol.end(), vol.begin(), vol.end());
-    hs.disp.insert(hs.disp.end(), disp.begin(), disp.end());
-    hs.vel.insert(hs.vel.end(), vel.begin(), vel.end());
-    hs.acc.insert(hs.acc.end(), acc.begin(), acc.end());
-    hs.ext.insert(hs.ext.end(), ext.begin(), ext.end());
-    hs.conn.insert(hs.conn.end(), conn.begin(), conn.end());
+    hs.vol.own.insert(hs.vol.own.end(), vol.begin(), vol.end());
+    hs.disp.own.insert(hs.disp.own.end(), disp.begin(), disp.end());
+    hs.vel.own.insert(hs.vel.own.end(), vel.begin(), vel.end());
+    hs.acc.own.insert(hs.acc.own.end(), acc.begin(), acc.end());
+    hs.ext.own.insert(hs.ext.own.end(), ext.begin(), ext.end());
+    hs.conn.own.insert(hs.conn.own.end(), conn.begin(), conn.end());
     hs.bdry.insert(hs.bdry.end(), bdry.begin(), bdry.end());
     hs.clamped.insert(hs.clamped.end(), clamped.begin(), clamped.end());
     hs.node_offset.push_back(hs.node_offset.back() + n);
