@@ -153,7 +153,9 @@ int pd_config_read(const char *path, pd_config *cfg);
 /* Copies the arrays to the device, applies the config the way simulate3d.cpp:125-139
  * and the apply_config methods (timeloop.h:184-225, contact.h:151-179, 325-372) do,
  * builds the bond lists (load_hdf5.h:27-37 + particle2.h:241-257) and initial AABBs
- * (timeloop.h:389-393). `precision` is PD_FP64 or PD_FP32C. */
+ * (timeloop.h:389-393). `precision` is PD_FP64 or PD_FP32C. The arrays are read during
+ * the call only; the handle keeps no pointer to them. Every per-node array in and out of
+ * a handle is in the setup's node order (the device layout's own order is internal). */
 int pd_create_from_arrays(const pd_setup_arrays *setup, const pd_config *cfg,
                           int precision, pd_sim **out);
 /* Reads main.conf + setup.h5 and prepares outdir, like simulate3d -c -i -o. */
@@ -262,7 +264,7 @@ int pd_count_live_bonds_noalloc(pd_sim *sim, uint64_t *live);
  * own setup and main.conf values, concatenated in one device layout: every phase of a step
  * is one launch over all of them and nothing couples two of them, so each computes exactly
  * what it computes in a handle of its own. pd_step advances every simulation that is not
- * finished. Simulation i's nodes are [node0, node0+n_nodes) of the handle's node order and
+ * finished. Simulation i's nodes are [node0, node0+n_nodes) of the handle's nodes and
  * its particles [particle0, particle0+n_particles) (pd_get_connectivity takes handle
  * particle indices). Errors of these calls are reported by pd_global_error(). */
 int pd_create_batch(const pd_setup_arrays *setups, const pd_config *cfgs, uint32_t n_sims,

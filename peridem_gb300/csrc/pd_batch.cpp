@@ -95,10 +95,7 @@ int Engine::read_nodes(const double *d, uint64_t node0, uint64_t nn, double *dst
     PD_TRY(check(cudaMemcpyAsync(buf.data() + c * nn, d + c * Ncap_ + node0, nn * 8, cudaMemcpyDeviceToHost, stream_),
                  "read state"));
   PD_TRY(check(cudaStreamSynchronize(stream_), "read state"));
-  for (uint64_t k = 0; k < nn; ++k) {
-    const uint64_t f = file_of_[node0 + k] - node0;
-    for (int c = 0; c < 3; ++c) dst[3 * f + c] = buf[c * nn + k];
-  }
+  rows_to_file(buf.data(), nn, node0, nn, dst);
   return PD_OK;
 }
 

@@ -211,25 +211,6 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   return rc;
 }
 
-namespace {
-// Runs f(i) for i in [0, n) on the host's cores (work handed out one index at a time).
-template <class F>
-void parallel_items(uint64_t n, F f) {
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const unsigned T = (unsigned)std::min<uint64_t>(std::min(hw, 32u), n);
-  if (T <= 1) {
-    for (uint64_t i = 0; i < n; ++i) f(i);
-    return;
-  }
-  std::atomic<uint64_t> next(0);
-  std::vector<std::thread> th;
-  for (unsigned t = 0; t < T; ++t)
-    th.emplace_back([&] {
-      for (uint64_t i = next++; i < n; i = next++) f(i);
-    });
-  for (auto &x : th) x.join();
-}
-}  // namespace
 
 void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
                          std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file) {
@@ -945,15 +926,20 @@ int Engine::set_stream(cudaStream_t s) {
   return PD_OK;
 }
 
+void Engine::rows_to_file(const double *src, uint64_t stride, uint64_t node0, uint64_t nn, double *dst) const {
+  parallel_items((nn + 65535) / 65536, [&](uint64_t chunk) {
+    for (uint64_t k = chunk * 65536; k < std::min<uint64_t>(nn, chunk * 65536 + 65536); ++k) {
+      const uint64_t f = file_of_[node0 + k] - node0;
+      for (int c = 0; c < 3; ++c) dst[3 * f + c] = src[c * stride + k];
+    }
+  });
+}
+
 int Engine::get_state(double *curpos, double *vel, double *acc, double *force, double *disp) {
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
   const uint64_t C = Ncap_;
   std::vector<double> buf(3 * C);
-  auto scatter = [&](double *dst) {
-    // [3][Ncap] device layout, engine order -> N*3 row vectors, file order
-    for (uint64_t n = 0; n < N_; ++n)
-      for (int c = 0; c < 3; ++c) dst[3 * (uint64_t)file_of_[n] + c] = buf[c * C + n];
-  };
+  auto scatter = [&](double *dst) { rows_to_file(buf.data(), C, 0, N_, dst); };
   auto fetch = [&](const double *d, double *dst) -> int {
     PD_TRY(cpy(buf.data(), d, 3 * C * 8, "read state"));
     scatter(dst);
@@ -984,10 +970,14 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
       } else {
         uint64_t off = 0;
         for (auto &s : sims_) {
-          uint64_t ns = s.node_offset[s.np];
-          for (uint64_t k = 0; k < ns; ++k)
-            for (int c = 0; c < 3; ++c) curpos[3 * (off + k) + c] = s.pos[3 * k + c] + dsp[3 * (off + k) + c];
-          off += ns;
+          const uint64_t n3 = 3 * s.node_offset[s.np];
+          const double *sp = s.pos.data(), *dp = dsp.data() + 3 * off;
+          double *cp = curpos + 3 * off;
+          parallel_items((n3 + 65535) / 65536, [&](uint64_t chunk) {
+            for (uint64_t k = chunk * 65536; k < std::min<uint64_t>(n3, chunk * 65536 + 65536); ++k)
+              cp[k] = sp[k] + dp[k];
+          });
+          off += n3 / 3;
         }
       }
     }
@@ -1220,8 +1210,7 @@ int Engine::get_afd(double *afd) {
   }
   std::vector<double> buf(3 * Ncap_);
   PD_TRY(cpy(buf.data(), d_afd_, 3 * Ncap_ * 8, "read applied force density"));
-  for (uint64_t n = 0; n < N_; ++n)
-    for (int c = 0; c < 3; ++c) afd[3 * (uint64_t)file_of_[n] + c] = buf[c * Ncap_ + n];
+  rows_to_file(buf.data(), Ncap_, 0, N_, afd);
   return PD_OK;
 }
 

@@ -29,12 +29,33 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "peridem_gb300.h"
 
 namespace pdg {
+
+// Runs f(i) for i in [0, n) on the host's cores (work handed out one index at a time).
+template <class F>
+void parallel_items(uint64_t n, F f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned T = (unsigned)std::min<uint64_t>(std::min(hw, 32u), n);
+  if (T <= 1) {
+    for (uint64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<uint64_t> next(0);
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < T; ++t)
+    th.emplace_back([&] {
+      for (uint64_t i = next++; i < n; i = next++) f(i);
+    });
+  for (auto &x : th) x.join();
+}
 
 constexpr int kSlice = 32;
 constexpr int kStageNodes = 512;          // nodes per block of the staged bond kernel
@@ -336,6 +357,9 @@ class Engine {
   int cpy(void *dst, const void *src, size_t bytes, const char *what);
   int mset(void *dst, int value, size_t bytes, const char *what);
   int read_nodes(const double *d, uint64_t node0, uint64_t nn, double *dst);
+  // Host copy of a [3][stride] array holding engine nodes node0 .. node0+nn-1 at columns
+  // 0 .. nn-1 -> nn*3 row vectors in file order (relative to node0).
+  void rows_to_file(const double *src, uint64_t stride, uint64_t node0, uint64_t nn, double *dst) const;
   DevView view(int cur) const;
 
   std::vector<HostSim> sims_;

@@ -71,10 +71,7 @@ void Engine::frame_state(const HostFrame &f, double *curpos, double *vel, double
                          double *afd) const {
   const uint64_t C = Ncap_;
   const bool fused = precision_ == PD_FP32C;
-  auto rows = [&](const double *src, double *dst) {  // engine order -> file order
-    for (uint64_t n = 0; n < N_; ++n)
-      for (int c = 0; c < 3; ++c) dst[3 * (uint64_t)file_of_[n] + c] = src[c * C + n];
-  };
+  auto rows = [&](const double *src, double *dst) { rows_to_file(src, C, 0, N_, dst); };
   if (curpos) {
     std::vector<double> dsp(3 * N_);
     rows(f.disp, dsp.data());
