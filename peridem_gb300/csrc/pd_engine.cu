@@ -192,13 +192,18 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   finished_.assign(S_, 0);
   final_.assign(S_, std::vector<double>());
   {
-    std::vector<uint32_t> deg_file;
-    order_nodes(sims_, file_of_, node_of_, deg_file);
+    int64_t bad = -1;
+    order_nodes(sims_, file_of_, node_of_, deg_file_, &bad);
+    if (bad >= 0) {
+      err = "Connectivity index out of range in particle " + std::to_string(bad);
+      return PD_EINVAL;
+    }
   }
   PD_TRY(check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate"));
   own_stream_ = true;
   capture_stream_ = stream_;
   const int rc = alloc_and_upload();
+  std::vector<uint32_t>().swap(deg_file_);
   // arrays read only while building (possibly views of the caller's buffers)
   for (auto &s : sims_) {
     s.vol.release();
@@ -213,7 +218,7 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
 
 
 void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
-                         std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file) {
+                         std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file, int64_t *bad) {
   // The SELL-32 layout pads every row of a slice to the slice's longest row. In file order a
   // slice mixes interior nodes (full neighbourhoods) with surface nodes (truncated ones);
   // sorting by bond count makes the rows of a slice nearly equal (crush512: padded entries
@@ -238,6 +243,7 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
   deg_file.assign(N, 0);
   file_of.assign(N, 0);
   node_of.assign(N, 0);
+  std::atomic<int64_t> bad_p(-1);
   parallel_items(parts.size(), [&](uint64_t x) {
     const HostSim &s = *parts[x].s;
     const uint32_t p = parts[x].p;
@@ -249,6 +255,8 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
       if (i < nloc && j < nloc) {
         dg[i]++;
         dg[j]++;
+      } else {
+        bad_p = (int64_t)p;
       }
     }
     std::vector<uint32_t> idx(nloc);
@@ -261,6 +269,7 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
       node_of[g0 + idx[k]] = (uint32_t)(g0 + k);
     }
   });
+  if (bad) *bad = bad_p.load();
 }
 
 int Engine::build_bonds() {
@@ -280,27 +289,9 @@ int Engine::build_bonds() {
       gnode += s.node_offset[s.np];
     }
   }
+  // bond counts per engine node (counted by order_nodes, which also checked the indices)
   std::vector<uint32_t> deg(Ncap_, 0);
-  std::atomic<int64_t> bad(-1);
-  parallel_items(parts.size(), [&](uint64_t x) {
-    const HostSim &s = *parts[x].s;
-    const uint32_t p = parts[x].p;
-    const uint64_t g0 = parts[x].g0;
-    const uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
-    for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
-      const uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
-      if (i >= nloc || j >= nloc) {
-        bad = (int64_t)p;
-        return;
-      }
-      deg[node_of_[g0 + i]]++;
-      deg[node_of_[g0 + j]]++;
-    }
-  });
-  if (bad >= 0) {
-    err = "Connectivity index out of range in particle " + std::to_string(bad.load());
-    return PD_EINVAL;
-  }
+  for (uint64_t g = 0; g < N_; ++g) deg[node_of_[g]] = deg_file_[g];
   uint32_t maxdeg = 0;
   for (uint64_t n = 0; n < N_; ++n) maxdeg = std::max(maxdeg, deg[n]);
   if (maxdeg > 65535) {
@@ -353,31 +344,13 @@ int Engine::build_bonds() {
   initial_bonds_ = 0;
   for (uint64_t n = 0; n < N_; ++n) initial_bonds_ += deg[n];
   if (precision_ == PD_FP32C) {
-    // record ranges of the staged bond kernel: per block of kStageNodes nodes, the smallest
-    // contiguous range holding its own nodes and every partner
+    // record ranges of the staged bond kernel: computed on the device the first time a staged
+    // variant is chosen (prepare_windows)
     const uint64_t nb = (N_ + kStageNodes - 1) / kStageNodes;
-    std::vector<uint32_t> wlo(nb), wcnt(nb);
-    win_max_ = 0;
-    parallel_items(nb, [&](uint64_t b) {
-      const uint64_t n0 = b * kStageNodes, n1 = std::min<uint64_t>(N_, n0 + kStageNodes);
-      uint64_t lo = n0, hi = n1 - 1;
-      for (uint64_t sl = n0 / 32; sl < (n1 + 31) / 32; ++sl)
-        for (uint64_t e = h_slice_ptr_[sl]; e < h_slice_ptr_[sl + 1]; ++e) {
-          const uint32_t q = col[e];
-          if (q == kNoCol) continue;
-          lo = std::min<uint64_t>(lo, q);
-          hi = std::max<uint64_t>(hi, q);
-        }
-      const uint64_t cnt = hi - lo + 1;
-      wlo[b] = (uint32_t)lo;
-      wcnt[b] = cnt <= kStageMaxRecords ? (uint32_t)cnt : 0u;  // larger ranges read global memory
-    });
-    for (uint64_t b = 0; b < nb; ++b) win_max_ = std::max(win_max_, wcnt[b]);
     PD_TRY(dalloc(this, allocs_, &d_win_lo_, nb, err));
     PD_TRY(dalloc(this, allocs_, &d_win_cnt_, nb, err));
-    PD_TRY(cpy(d_win_lo_, wlo.data(), nb * 4, "upload windows"));
-    PD_TRY(cpy(d_win_cnt_, wcnt.data(), nb * 4, "upload windows"));
-    if (win_max_) PD_TRY(prepare_staged_kernels(win_max_ * (uint32_t)sizeof(Rec32)));
+    win_max_ = 0;
+    windows_ready_ = false;
   }
   PD_TRY(dalloc(this, allocs_, &d_slice_ptr_, nslices_ + 1, err));
   PD_TRY(dalloc(this, allocs_, &d_deg_, Ncap_, err));
@@ -1392,11 +1365,27 @@ int Engine::restore() {
   return check(cudaStreamSynchronize(stream_), "restore");
 }
 
+int Engine::prepare_windows() {
+  if (windows_ready_ || precision_ != PD_FP32C) return PD_OK;
+  const uint64_t nb = (N_ + kStageNodes - 1) / kStageNodes;
+  launch_stage_windows(view(cur_), d_win_lo_, d_win_cnt_, stream_);
+  PD_TRY(check(cudaGetLastError(), "stage windows"));
+  std::vector<uint32_t> wcnt(nb);
+  PD_TRY(cpy(wcnt.data(), d_win_cnt_, nb * 4, "read windows"));
+  win_max_ = 0;
+  for (uint32_t c : wcnt) win_max_ = std::max(win_max_, c);
+  if (win_max_) PD_TRY(prepare_staged_kernels(win_max_ * (uint32_t)sizeof(Rec32)));
+  windows_ready_ = true;
+  graphs_ok_ = false;  // the kernels' view carries win_max
+  return PD_OK;
+}
+
 int Engine::set_variant(int variant) {
   if (variant < 0 || variant >= num_bond_variants()) {
     err = "bond kernel variant out of range";
     return PD_EINVAL;
   }
+  if (variant >= kFirstStagedVariant) PD_TRY(prepare_windows());
   variant_ = variant;
   graphs_ok_ = false;
   return PD_OK;
@@ -1405,6 +1394,7 @@ int Engine::set_variant(int variant) {
 int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms) {
   const int nv = precision_ == PD_FP32C ? num_bond_variants() : 1;
   if (steps_per_variant == 0) steps_per_variant = 8;
+  if (nv > kFirstStagedVariant) PD_TRY(prepare_windows());
   PD_TRY(snapshot());
   int best = variant_;
   double best_ms = 1e300;

@@ -325,7 +325,8 @@ class Engine {
   // descending bond count (stable: equal counts keep their file order). file_of[engine index] = file index, node_of = its inverse,
   // deg_file = bond count of each node in file order (indices out of range are not counted).
   static void order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
-                          std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file);
+                          std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file,
+                          int64_t *bad = nullptr);  // bad: a particle with an index out of range, or -1
   int raw_alloc(void **p, size_t bytes);
   double step_bytes(uint64_t live_bonds) const;
   uint64_t initial_bonds() const { return initial_bonds_; }
@@ -348,6 +349,9 @@ class Engine {
   int launch_step_seq(int cur, cudaStream_t s);
   int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
+  // FP32 form: record ranges of the staged bond kernel (win_lo / win_cnt / win_max), computed
+  // on the device the first time a staged variant is needed.
+  int prepare_windows();
   // One step graph whose broad-phase rebuild kernels sit in a conditional node set by
   // k_bp_decide (0 on success; falls back to the plain graph when unsupported).
   int capture_conditional(int cur, cudaGraphExec_t *out);
@@ -395,6 +399,7 @@ class Engine {
 
   // host mirrors used when reading results back
   std::vector<uint32_t> file_of_, node_of_;  // see order_nodes
+  std::vector<uint32_t> deg_file_;           // bond counts in file order, while building
   std::vector<uint32_t> h_pid_;
   std::vector<uint64_t> h_slice_ptr_;
   std::vector<uint16_t> h_deg_;
@@ -420,6 +425,7 @@ class Engine {
   double *d_f_extra_ = nullptr;
   uint32_t *d_win_lo_ = nullptr, *d_win_cnt_ = nullptr;
   uint32_t win_max_ = 0;
+  bool windows_ready_ = false;
   uint8_t *d_extra_flag_ = nullptr;
   float *d_wall_local_ = nullptr;
   unsigned int *d_lrtb_local_ = nullptr;
@@ -446,6 +452,10 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s);
 int num_bond_variants();
 // Raises the dynamic shared-memory limit of the staged bond kernels (once per engine).
 int prepare_staged_kernels(uint32_t smem_bytes);
+constexpr int kFirstStagedVariant = 10;  // variants >= this use the staged bond kernel
+// Per block of kStageNodes nodes, the smallest contiguous range of node records that holds the
+// block's own nodes and every partner of their bonds (win_cnt 0 when above kStageMaxRecords).
+void launch_stage_windows(const DevView &v, uint32_t *win_lo, uint32_t *win_cnt, cudaStream_t s);
 void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
                      cudaStream_t s);
 void launch_centroids(const DevView &v, cudaStream_t s);

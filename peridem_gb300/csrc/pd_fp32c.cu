@@ -641,6 +641,43 @@ int prepare_staged_kernels(uint32_t smem_bytes) {
 }
 
 
+__global__ void k_stage_windows(const __grid_constant__ DevView v, uint32_t *win_lo, uint32_t *win_cnt) {
+  const uint64_t b = blockIdx.x;
+  const uint64_t n0 = b * kStageNodes, n1 = min(v.N, n0 + kStageNodes);
+  uint32_t lo = (uint32_t)n0, hi = (uint32_t)(n1 - 1);
+  const uint64_t e0 = v.slice_ptr[n0 / 32], e1 = v.slice_ptr[(n1 + 31) / 32];
+  for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const uint32_t q = v.col[e];
+    if (q != kNoCol) {
+      lo = min(lo, q);
+      hi = max(hi, q);
+    }
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  __shared__ uint32_t slo[32], shi[32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    slo[w] = lo;
+    shi[w] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+      lo = min(lo, slo[i]);
+      hi = max(hi, shi[i]);
+    }
+    const uint64_t cnt = (uint64_t)hi - lo + 1;
+    win_lo[b] = lo;
+    win_cnt[b] = cnt <= kStageMaxRecords ? (uint32_t)cnt : 0u;
+  }
+}
+
+void launch_stage_windows(const DevView &v, uint32_t *win_lo, uint32_t *win_cnt, cudaStream_t s) {
+  const uint64_t nb = (v.N + kStageNodes - 1) / kStageNodes;
+  if (nb) k_stage_windows<<<(unsigned)nb, 256, 0, s>>>(v, win_lo, win_cnt);
+}
+
 // A_next := this step's predicted displacement of each particle's anchor node.
 __global__ void k_anchor_next(DevView v) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -664,7 +701,8 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
   const bool fused_extra = variant >= 6 && variant <= 9;
-  if (variant >= 10 && !v.win_max) variant = 3;  // nothing to stage: the plain kernel
+  // nothing to stage (or the ranges not computed): the plain kernel
+  if (variant >= kFirstStagedVariant && !v.win_max) variant = 3;
   if (!fused_extra) k_extra32<<<152 * 8, 128, 0, s>>>(v);
   const unsigned bs = (unsigned)((v.N + kStageNodes - 1) / kStageNodes);
   const size_t sm = (size_t)v.win_max * sizeof(Rec32);
