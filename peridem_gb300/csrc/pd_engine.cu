@@ -119,6 +119,7 @@ DevView Engine::view(int cur) const {
   v.xnodes = bp_.xnodes;
   v.xparts = bp_.xparts;
   v.xcount = bp_.xcount;
+  v.max_part_nodes = max_part_nodes_;
   v.extra_flag = d_extra_flag_;
   v.wall_local = d_wall_local_;
   v.lrtb_local_next = d_lrtb_local_;
@@ -415,6 +416,7 @@ int Engine::alloc_and_upload() {
       DevPart &P = parts[gp];
       P.g0 = (uint32_t)(gnode + s.node_offset[p]);
       P.n = (uint32_t)(s.node_offset[p + 1] - s.node_offset[p]);
+      max_part_nodes_ = std::max(max_part_nodes_, P.n);
       P.sim = si;
       P.taxis = s.taxis[p];
       P.rho = s.rho[p];

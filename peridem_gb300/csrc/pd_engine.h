@@ -166,6 +166,7 @@ struct DevView {
   uint32_t win_max;      // largest staged range (records): the kernel's shared-memory size
   // FP32 form: work lists of k_extra32 (see BroadPhase)
   uint32_t *xnodes, *xparts, *xcount;
+  uint32_t max_part_nodes;  // nodes of the largest particle
   uint8_t *extra_flag;   // 1 where f_extra holds this step's contribution
   float *wall_local;     // [P][6] wall planes in each particle's local frame
   unsigned int *lrtb_local_next;  // [P][6] ordered float keys of the local-frame AABB
@@ -370,6 +371,7 @@ class Engine {
   int precision_ = PD_FP64;
   uint64_t N_ = 0, Ncap_ = 0, E_ = 0, nslices_ = 0;
   uint32_t P_ = 0, S_ = 0;
+  uint32_t max_part_nodes_ = 0;
   cudaStream_t stream_ = nullptr;          // stream work is enqueued on
   cudaStream_t capture_stream_ = nullptr;  // the handle's own stream (graphs are captured here)
   bool own_stream_ = false;

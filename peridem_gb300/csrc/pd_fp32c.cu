@@ -191,9 +191,13 @@ __global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView
   const uint32_t nx = v.xcount[0], np = v.xcount[1];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nx; i += gridDim.x * blockDim.x)
     extra_node(v, v.xnodes[i]);
-  for (uint32_t i = blockIdx.x; i < np; i += gridDim.x) {
-    const DevPart &P = v.parts[v.xparts[i]];
-    for (uint32_t l = threadIdx.x; l < P.n; l += blockDim.x) {
+  // the listed particles' nodes in chunks of one block's threads, spread over all blocks (one
+  // block per particle left a 10k-node particle's nodes to 128 threads in turn)
+  const uint64_t cpp = (v.max_part_nodes + blockDim.x - 1) / blockDim.x;  // chunks per particle
+  for (uint64_t c = blockIdx.x; c < (uint64_t)np * cpp; c += gridDim.x) {
+    const DevPart &P = v.parts[v.xparts[c / cpp]];
+    const uint64_t l = (c % cpp) * blockDim.x + threadIdx.x;
+    if (l < P.n) {
       const uint64_t n = (uint64_t)P.g0 + l;
       if (v.cand_n[n] == 0) extra_node(v, n);  // nodes with candidates are on the node list
     }
