@@ -694,9 +694,10 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
   if (v.P) k_anchor_next<<<(v.P + 127) / 128, 128, 0, s>>>(v);
 }
 
-// Bond-kernel variants the autotuner chooses from: <positions per load group, min blocks/SM,
-// 256-bit record loads, column prefetch>.
-const int kNumBondVariants = 14;
+// Bond-kernel variants the autotuner chooses from: k_bond32 <positions per load group, min
+// blocks/SM, 256-bit record loads, column prefetch, fused non-bond work> with 128-thread blocks
+// (0-9) and with 32/64-thread blocks (14-17), and the staged k_bond32s (10-13).
+const int kNumBondVariants = 18;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -704,7 +705,7 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
-  const bool fused_extra = variant >= 6 && variant <= 9;
+  const bool fused_extra = (variant >= 6 && variant <= 9) || (variant >= 14 && variant <= 16);
   // nothing to stage (or the ranges not computed): the plain kernel
   if (variant >= kFirstStagedVariant && !v.win_max) variant = 3;
   if (!fused_extra) k_extra32<<<152 * 8, 128, 0, s>>>(v);
@@ -724,6 +725,12 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
     case 11: k_bond32s<4, 2><<<bs, kStageNodes, sm, s>>>(v); break;
     case 12: k_bond32s<2, 3><<<bs, kStageNodes, sm, s>>>(v); break;
     case 13: k_bond32s<1, 4><<<bs, kStageNodes, sm, s>>>(v); break;
+    // small handles: a few hundred 128-thread blocks leave some SMs one block more than others;
+    // 32- and 64-thread blocks of the same kernels spread the warps evenly
+    case 14: k_bond32<4, 4, 1, 1, 1><<<(unsigned)((v.N + 31) / 32), 32, 0, s>>>(v); break;
+    case 15: k_bond32<4, 4, 1, 2, 1><<<(unsigned)((v.N + 31) / 32), 32, 0, s>>>(v); break;
+    case 16: k_bond32<4, 4, 1, 2, 1><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
+    case 17: k_bond32<2, 6, 1, 2, 0><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
