@@ -173,8 +173,8 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
     err = "empty setup";
     return PD_EINVAL;
   }
-  if (N_ >= 0xFFFFFFF0ull) {
-    err = "too many nodes for 32-bit node indices";
+  if (N_ > 0x7FFFFFE0ull) {  // node indices use 31 bits (bit 31 of a column entry is a flag)
+    err = "too many nodes for 31-bit node indices";
     return PD_EINVAL;
   }
   Ncap_ = round_up(N_, 32);
@@ -1022,7 +1022,7 @@ int Engine::get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, u
     const uint64_t mbase = (h_slice_ptr_[g >> 5] - e0) >> 5;
     for (uint32_t j = 0; j < h_deg_[g]; ++j) {
       if (!((mask[mbase + j] >> (g & 31)) & 1u)) continue;
-      uint64_t q = file_of_[col[base + 32ull * j]] - g0;
+      uint64_t q = file_of_[col[base + 32ull * j] & kColIndex] - g0;
       if (i < q) {
         if (pairs && c < cap) {
           pairs[2 * c] = (uint32_t)i;
@@ -1248,7 +1248,7 @@ int Engine::set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t 
     const uint64_t mbase = (h_slice_ptr_[g >> 5] - e0) >> 5;
     const uint32_t bit = 1u << (g & 31);
     for (uint32_t j = 0; j < h_deg_[g]; ++j) {
-      uint64_t q = file_of_[col[base + 32ull * j]] - g0;
+      uint64_t q = file_of_[col[base + 32ull * j] & kColIndex] - g0;
       uint64_t a = std::min<uint64_t>(i, q), b = std::max<uint64_t>(i, q);
       const bool live = std::binary_search(keys.begin(), keys.end(), a * nloc + b);
       if (live)
@@ -1258,6 +1258,11 @@ int Engine::set_connectivity(uint32_t particle, const uint32_t *pairs, uint64_t 
     }
   }
   PD_TRY(cpy(d_mask_ + e0 / 32, mask.data(), (e1 - e0) / 32 * 4, "write mask"));
+  if (precision_ == PD_FP32C) {  // broken flags of the column entries from the new masks
+    launch_col_flags(view(cur_), stream_);
+    PD_TRY(check(cudaGetLastError(), "set connectivity"));
+    PD_TRY(check(cudaStreamSynchronize(stream_), "set connectivity"));
+  }
   return PD_OK;
 }
 
@@ -1355,6 +1360,8 @@ int Engine::restore() {
                  "restore"));
     off += (m.second + 255) & ~(size_t)255;
   }
+  if (precision_ == PD_FP32C) launch_col_flags(view(cur_), stream_);  // broken flags from the masks
+  PD_TRY(check(cudaGetLastError(), "restore"));
   cur_ = backup_cur_;
   steps_done_ = backup_steps_;
   sim_steps_ = backup_sim_steps_;

@@ -15,6 +15,10 @@
 //     (conn2NArr push order, ascending for a sorted Connectivity). One 32-bit word per
 //     (slice, position) holds the live bits of the 32 lanes: bit l of
 //     mask[slice_ptr[s]/32 + j]. Breaking clears a bit; bonds are never re-added;
+//   * FP32-compensated form: bit 31 of a column entry mirrors a cleared live bit (set by the
+//     FP32 kernels when they break the bond, re-derived from the masks after a restore or a
+//     set Connectivity), so that the FP32 bond loops read liveness with the column index;
+//     the masks stay the record every other reader uses;
 //   * FP64 form only: per-entry constants xi = pos[q]-pos[i] (3 doubles), |xi| and the
 //     correctly rounded reciprocal of |xi| (gen_xi, particle2.h:241-257);
 //   * FP32-compensated form only: a 32-byte record per node, float4 (local position,
@@ -61,6 +65,8 @@ constexpr int kSlice = 32;
 constexpr int kStageNodes = 512;          // nodes per block of the staged bond kernel
 constexpr uint32_t kStageMaxRecords = 6400;  // 200 KB of 32-byte records per block
 constexpr uint32_t kNoCol = 0xFFFFFFFFu;
+constexpr uint32_t kColBroken = 0x80000000u;  // FP32 form: broken flag in a column entry
+constexpr uint32_t kColIndex = 0x7FFFFFFFu;   // the partner index in a column entry
 constexpr uint64_t kOrderWindow = 1024;     // nodes per window of the bond-count sort (order_nodes)
 
 // Per-particle parameters (ParticleN scalars, particle2.h:51-59).
@@ -468,6 +474,7 @@ void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
+void launch_col_flags(const DevView &v, cudaStream_t s);
 void launch_prescribed(const DevView &v, cudaStream_t s);
 void launch_reset_y(const DevView &v, cudaStream_t s);
 

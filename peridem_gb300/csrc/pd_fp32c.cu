@@ -204,20 +204,29 @@ __global__ void __launch_bounds__(128) k_extra32(const __grid_constant__ DevView
   }
 }
 
+// Breaking a bond in the FP32 form: its live bit is cleared and the broken flag (bit 31) is set
+// in its column entry, which only the node's own thread writes. The bond loops read the flag
+// with the column index and need no live-mask loads.
+__device__ __noinline__ void cut_bond(uint32_t *word, uint32_t lane, uint32_t *cole, uint32_t q) {
+  atomicAnd(word, ~(1u << lane));
+  *cole = q | kColBroken;
+}
+
 // FP64 stretch of the reference formula (particle2.h:139-149) for a bond whose FP32 stretch
-// lies in the band around snot; clears the bond's live bit when it exceeds snot. Kept out of
-// line so that the compiler does not predicate its FP64 work into the bond loop.
+// lies in the band around snot; breaks the bond when it exceeds snot. Kept out of line so that
+// the compiler does not predicate its FP64 work into the bond loop.
 __device__ __noinline__ void band_check(const DevView &v, uint64_t n, uint32_t q, uint32_t *word, uint32_t lane,
-                                        double snot) {
+                                        double snot, uint32_t *cole) {
   const uint64_t C3 = v.Ncap;
   const D3 di = ld3(v.disp, n, C3), pi = ld3(v.pos, n, C3);
   D3 xi64 = ld3(v.pos, q, C3) - pi;
   D3 eta = (ld3(v.disp, q, C3) - di) + xi64;
   double en = norm3(eta), xn = norm3(xi64);
-  if (((en - xn) / xn) > snot) atomicAnd(word, ~(1u << lane));
+  if (((en - xn) / xn) > snot) {
+    atomicAnd(word, ~(1u << lane));
+    *cole = q | kColBroken;
+  }
 }
-
-__device__ __noinline__ void cut_bond(uint32_t *word, uint32_t lane) { atomicAnd(word, ~(1u << lane)); }
 
 // One bond in FP32: cancellation-free stretch and Kahan-compensated accumulation.
 struct Acc32 {
@@ -380,81 +389,66 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     const uint32_t lane = (uint32_t)(nn & 31);
     const uint64_t sbase = v.slice_ptr[nn >> 5];
     const uint32_t *colp = v.col + sbase + lane;
+    uint32_t *colw = const_cast<uint32_t *>(colp);  // broken flags of this node's entries
     uint32_t *maskp = v.mask + (sbase >> 5);
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
     const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
     const Rec32 *__restrict__ rec = v.rec;
     int j = 0;
-    // column indices and live masks of the next PF groups, loaded ahead (static indices only,
-    // so that the ring stays in registers)
-    uint32_t qb[PF > 0 ? PF : 1][U], mb[PF > 0 ? PF : 1][U];
+    // column entries (index + broken flag) of the next PF groups, loaded ahead (static
+    // indices only, so that the ring stays in registers)
+    uint32_t qb[PF > 0 ? PF : 1][U];
 #pragma unroll
     for (int d = 0; d < PF; ++d) {
       if ((d + 1) * U <= dg) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          qb[d][u] = __ldg(colp + 32 * (d * U + u));
-          mb[d][u] = maskp[d * U + u];
-        }
+        for (int u = 0; u < U; ++u) qb[d][u] = __ldg(colp + 32 * (d * U + u));
       }
     }
     for (; j + U <= dg; j += U) {
-      uint32_t q[U], m[U];
+      uint32_t q[U];
       if (PF > 0) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          q[u] = qb[0][u];
-          m[u] = mb[0][u];
-        }
+        for (int u = 0; u < U; ++u) q[u] = qb[0][u];
 #pragma unroll
         for (int d = 0; d + 1 < PF; ++d) {
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            qb[d][u] = qb[d + 1][u];
-            mb[d][u] = mb[d + 1][u];
-          }
+          for (int u = 0; u < U; ++u) qb[d][u] = qb[d + 1][u];
         }
         if (j + (PF + 1) * U <= dg) {
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
-            mb[PF - 1][u] = maskp[j + PF * U + u];
-          }
+          for (int u = 0; u < U; ++u) qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
         }
       } else {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          q[u] = __ldg(colp + 32 * (j + u));
-          m[u] = maskp[j + u];
-        }
+        for (int u = 0; u < U; ++u) q[u] = __ldg(colp + 32 * (j + u));
       }
       float4 pq[U], uq[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) ld_rec<W>(rec + q[u], pq[u], uq[u]);
+      for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        if ((m[u] >> lane) & 1u) {
+        if (!(q[u] & kColBroken)) {
           ++live;
           const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
           if (brk && str > slo) {
-            if (str > shi) cut_bond(&maskp[j + u], lane);
-            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot);
+            if (str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
+            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
           }
         }
       }
     }
     for (; j < dg; ++j) {
-      const uint32_t mw = maskp[j];
-      if (!((mw >> lane) & 1u)) continue;
       const uint32_t q = __ldg(colp + 32 * j);
+      if (q & kColBroken) continue;
       ++live;
       float4 pq, uq;
       ld_rec<W>(rec + q, pq, uq);
       const float str = bond32(pi4, ui4, pq, uq, cn, a);
       if (brk && str > slo) {
-        if (str > shi) cut_bond(&maskp[j], lane);
-        else band_check(v, nn, q, &maskp[j], lane, P.snot);
+        if (str > shi) cut_bond(&maskp[j], lane, colw + 32 * j, q);
+        else band_check(v, nn, q, &maskp[j], lane, P.snot, colw + 32 * j);
       }
     }
   }
@@ -536,6 +530,7 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
     const uint32_t lane = (uint32_t)(nn & 31);
     const uint64_t sbase = v.slice_ptr[nn >> 5];
     const uint32_t *colp = v.col + sbase + lane;
+    uint32_t *colw = const_cast<uint32_t *>(colp);
     uint32_t *maskp = v.mask + (sbase >> 5);
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
@@ -552,65 +547,52 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
       }
     };
     int j = 0;
-    uint32_t qb[PF][U], mb[PF][U];
+    uint32_t qb[PF][U];
 #pragma unroll
     for (int d = 0; d < PF; ++d) {
       if ((d + 1) * U <= dg) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          qb[d][u] = __ldg(colp + 32 * (d * U + u));
-          mb[d][u] = maskp[d * U + u];
-        }
+        for (int u = 0; u < U; ++u) qb[d][u] = __ldg(colp + 32 * (d * U + u));
       }
     }
     for (; j + U <= dg; j += U) {
-      uint32_t q[U], m[U];
+      uint32_t q[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        q[u] = qb[0][u];
-        m[u] = mb[0][u];
-      }
+      for (int u = 0; u < U; ++u) q[u] = qb[0][u];
 #pragma unroll
       for (int d = 0; d + 1 < PF; ++d) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          qb[d][u] = qb[d + 1][u];
-          mb[d][u] = mb[d + 1][u];
-        }
+        for (int u = 0; u < U; ++u) qb[d][u] = qb[d + 1][u];
       }
       if (j + (PF + 1) * U <= dg) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
-          mb[PF - 1][u] = maskp[j + PF * U + u];
-        }
+        for (int u = 0; u < U; ++u) qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
       }
       float4 pq[U], uq[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) partner(q[u], pq[u], uq[u]);
+      for (int u = 0; u < U; ++u) partner(q[u] & kColIndex, pq[u], uq[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        if ((m[u] >> lane) & 1u) {
+        if (!(q[u] & kColBroken)) {
           ++live;
           const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
           if (brk && str > slo) {
-            if (str > shi) cut_bond(&maskp[j + u], lane);
-            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot);
+            if (str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
+            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
           }
         }
       }
     }
     for (; j < dg; ++j) {
-      const uint32_t mw = maskp[j];
-      if (!((mw >> lane) & 1u)) continue;
       const uint32_t q = __ldg(colp + 32 * j);
+      if (q & kColBroken) continue;
       ++live;
       float4 pq, uq;
       partner(q, pq, uq);
       const float str = bond32(pi4, ui4, pq, uq, cn, a);
       if (brk && str > slo) {
-        if (str > shi) cut_bond(&maskp[j], lane);
-        else band_check(v, nn, q, &maskp[j], lane, P.snot);
+        if (str > shi) cut_bond(&maskp[j], lane, colw + 32 * j, q);
+        else band_check(v, nn, q, &maskp[j], lane, P.snot, colw + 32 * j);
       }
     }
   }
@@ -652,9 +634,9 @@ __global__ void k_stage_windows(const __grid_constant__ DevView v, uint32_t *win
   const uint64_t e0 = v.slice_ptr[n0 / 32], e1 = v.slice_ptr[(n1 + 31) / 32];
   for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const uint32_t q = v.col[e];
-    if (q != kNoCol) {
-      lo = min(lo, q);
-      hi = max(hi, q);
+    if (q != kNoCol) {  // a bond, live or broken
+      lo = min(lo, q & kColIndex);
+      hi = max(hi, q & kColIndex);
     }
   }
   lo = __reduce_min_sync(0xffffffffu, lo);
@@ -680,6 +662,26 @@ __global__ void k_stage_windows(const __grid_constant__ DevView v, uint32_t *win
 void launch_stage_windows(const DevView &v, uint32_t *win_lo, uint32_t *win_cnt, cudaStream_t s) {
   const uint64_t nb = (v.N + kStageNodes - 1) / kStageNodes;
   if (nb) k_stage_windows<<<(unsigned)nb, 256, 0, s>>>(v, win_lo, win_cnt);
+}
+
+// FP32 form: broken flags of the column entries from the live masks (after the masks were
+// restored from a snapshot or set from a saved Connectivity).
+__global__ void k_col_flags(const __grid_constant__ DevView v) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t lane = (uint32_t)(n & 31);
+  const uint64_t sbase = v.slice_ptr[n >> 5];
+  uint32_t *col = const_cast<uint32_t *>(v.col) + sbase + lane;
+  const uint32_t *maskp = v.mask + (sbase >> 5);
+  const int dg = v.deg[n];
+  for (int j = 0; j < dg; ++j) {
+    const uint32_t q = col[32 * j] & kColIndex;
+    col[32 * j] = ((maskp[j] >> lane) & 1u) ? q : (q | kColBroken);
+  }
+}
+
+void launch_col_flags(const DevView &v, cudaStream_t s) {
+  if (v.N) k_col_flags<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v);
 }
 
 // A_next := this step's predicted displacement of each particle's anchor node.

@@ -123,7 +123,7 @@ void Engine::frame_connectivity(const HostFrame &f, uint32_t particle, std::vect
     const uint64_t mbase = h_slice_ptr_[g >> 5] >> 5;
     for (uint32_t j = 0; j < h_deg_[g]; ++j) {
       if (!((f.mask[mbase + j] >> (g & 31)) & 1u)) continue;
-      const uint64_t q = file_of_[h_col_[base + 32ull * j]] - g0;
+      const uint64_t q = file_of_[h_col_[base + 32ull * j] & kColIndex] - g0;
       if (i < q) {
         pairs.push_back((uint32_t)i);
         pairs.push_back((uint32_t)q);
