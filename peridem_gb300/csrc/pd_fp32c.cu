@@ -427,13 +427,18 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
       float4 pq[U], uq[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
+      // the group's bond terms are evaluated unconditionally (a broken bond's are discarded),
+      // so that the independent bonds' arithmetic interleaves; the sums take live ones in order
+      BondTerms bt[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (!(q[u] & kColBroken)) {
           ++live;
-          const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
-          if (brk && str > slo) {
-            if (str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
+          kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
+          if (brk && bt[u].str > slo) {
+            if (bt[u].str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
             else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
           }
         }
@@ -571,13 +576,16 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
       float4 pq[U], uq[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) partner(q[u] & kColIndex, pq[u], uq[u]);
+      BondTerms bt[U];  // as in bond_node: terms unconditionally, live ones summed in order
+#pragma unroll
+      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (!(q[u] & kColBroken)) {
           ++live;
-          const float str = bond32(pi4, ui4, pq[u], uq[u], cn, a);
-          if (brk && str > slo) {
-            if (str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
+          kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
+          if (brk && bt[u].str > slo) {
+            if (bt[u].str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
             else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
           }
         }
