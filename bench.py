@@ -520,10 +520,10 @@ def ours(args):
         serving = serving_run(args)
 
     # our kernels per step: k_bp_decide, k_extra32 (unless fused into the bond kernel: variants
-    # 6-9 and 14-16), the bond kernel, k_end_step; the 7 broad-phase kernels run only in rebuild
-    # steps when the step graph holds them in a conditional node, else every step (exiting at
-    # once unless due)
-    per_step = 3 if (6 <= variant <= 9 or 14 <= variant <= 16) else 4
+    # 6-9, 14-16 and 19), the bond kernel, k_end_step; the 7 broad-phase kernels run only in
+    # rebuild steps when the step graph holds them in a conditional node, else every step
+    # (exiting at once unless due)
+    per_step = 3 if (6 <= variant <= 9 or 14 <= variant <= 16 or variant == 19) else 4
     bp = 7 * (sim.rebuilds_timed if graph_mode == 2 else K)
     gpu_launches = per_step * K + bp
     line = {

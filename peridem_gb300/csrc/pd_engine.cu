@@ -182,7 +182,7 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   // default bond-kernel variant: the autotuner's choice on small and on large handles (small
   // handles are launch-latency bound and gain most from doing the non-bond work in the bond
   // kernel, one launch less per step)
-  variant_ = N_ < 131072 ? 6 : 3;
+  variant_ = N_ < 131072 ? 6 : 18;
   sim_node0_.assign(S_ + 1, 0);
   sim_p0_.assign(S_ + 1, 0);
   for (uint32_t i = 0; i < S_; ++i) {

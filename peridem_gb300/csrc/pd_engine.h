@@ -387,7 +387,7 @@ class Engine {
   bool stats_ = false;
   bool use_graphs_ = true;
   bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning mode 2)
-  int variant_ = 3;  // FP32 bond-kernel variant; init() picks by size (the autotuner's usual choices)
+  int variant_ = 18;  // FP32 bond-kernel variant; init() picks by size (the autotuner's usual choices)
   std::vector<std::pair<void *, size_t>> mutable_;  // device buffers that change while stepping
   void *backup_ = nullptr;
   size_t backup_bytes_ = 0;

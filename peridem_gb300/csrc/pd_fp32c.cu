@@ -706,8 +706,8 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: k_bond32 <positions per load group, min
 // blocks/SM, 256-bit record loads, column prefetch, fused non-bond work> with 128-thread blocks
-// (0-9) and with 32/64-thread blocks (14-17), and the staged k_bond32s (10-13).
-const int kNumBondVariants = 18;
+// (0-9, 18-20) and with 32/64-thread blocks (14-17), and the staged k_bond32s (10-13).
+const int kNumBondVariants = 21;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -715,7 +715,7 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
-  const bool fused_extra = (variant >= 6 && variant <= 9) || (variant >= 14 && variant <= 16);
+  const bool fused_extra = (variant >= 6 && variant <= 9) || (variant >= 14 && variant <= 16) || variant == 19;
   // nothing to stage (or the ranges not computed): the plain kernel
   if (variant >= kFirstStagedVariant && !v.win_max) variant = 3;
   if (!fused_extra) k_extra32<<<152 * 8, 128, 0, s>>>(v);
@@ -741,6 +741,10 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
     case 15: k_bond32<4, 4, 1, 2, 1><<<(unsigned)((v.N + 31) / 32), 32, 0, s>>>(v); break;
     case 16: k_bond32<4, 4, 1, 2, 1><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
     case 17: k_bond32<2, 6, 1, 2, 0><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
+    // 5 blocks/SM (96 registers, no spills)
+    case 18: k_bond32<4, 5, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 19: k_bond32<4, 5, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
+    case 20: k_bond32<3, 5, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }
