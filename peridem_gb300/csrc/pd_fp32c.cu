@@ -444,16 +444,26 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
         }
       }
     }
-    for (; j < dg; ++j) {
-      const uint32_t q = __ldg(colp + 32 * j);
-      if (q & kColBroken) continue;
-      ++live;
-      float4 pq, uq;
-      ld_rec<W>(rec + q, pq, uq);
-      const float str = bond32(pi4, ui4, pq, uq, cn, a);
-      if (brk && str > slo) {
-        if (str > shi) cut_bond(&maskp[j], lane, colw + 32 * j, q);
-        else band_check(v, nn, q, &maskp[j], lane, P.snot, colw + 32 * j);
+    if (j < dg) {  // the row's last dg - j < U positions as one group; missing ones count as broken
+      uint32_t q[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? __ldg(colp + 32 * (j + u)) : kColBroken;
+      float4 pq[U], uq[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
+      BondTerms bt[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!(q[u] & kColBroken)) {
+          ++live;
+          kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
+          if (brk && bt[u].str > slo) {
+            if (bt[u].str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
+            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
+          }
+        }
       }
     }
   }
