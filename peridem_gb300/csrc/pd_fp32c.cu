@@ -353,6 +353,14 @@ __device__ __forceinline__ void verlet_tail(const DevView &v, uint64_t nn, uint3
   }
 }
 
+// A column entry: read once per step, so it is not allocated in L1, which is left to the
+// partner records (the bond kernel's working set).
+__device__ __forceinline__ uint32_t ld_col(const uint32_t *p) {
+  uint32_t r;
+  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
+  return r;
+}
+
 // A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector.
 template <int W>
 __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
@@ -403,7 +411,7 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     for (int d = 0; d < PF; ++d) {
       if ((d + 1) * U <= dg) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) qb[d][u] = __ldg(colp + 32 * (d * U + u));
+        for (int u = 0; u < U; ++u) qb[d][u] = ld_col(colp + 32 * (d * U + u));
       }
     }
     for (; j + U <= dg; j += U) {
@@ -418,11 +426,11 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
         }
         if (j + (PF + 1) * U <= dg) {
 #pragma unroll
-          for (int u = 0; u < U; ++u) qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
+          for (int u = 0; u < U; ++u) qb[PF - 1][u] = ld_col(colp + 32 * (j + PF * U + u));
         }
       } else {
 #pragma unroll
-        for (int u = 0; u < U; ++u) q[u] = __ldg(colp + 32 * (j + u));
+        for (int u = 0; u < U; ++u) q[u] = ld_col(colp + 32 * (j + u));
       }
       float4 pq[U], uq[U];
 #pragma unroll
@@ -447,7 +455,7 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     if (j < dg) {  // the row's last dg - j < U positions as one group; missing ones count as broken
       uint32_t q[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? __ldg(colp + 32 * (j + u)) : kColBroken;
+      for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? ld_col(colp + 32 * (j + u)) : kColBroken;
       float4 pq[U], uq[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
