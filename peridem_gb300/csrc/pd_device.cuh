@@ -164,21 +164,44 @@ __device__ __forceinline__ bool nonfinite(double x) {
   return ((__double2hiint(x) >> 20) & 0x7FF) == 0x7FF;
 }
 
+// Per-particle inputs of the FP32 form's end of step that depend only on the particle index,
+// loaded together before the kernel's branches (the kernel is a short chain of dependent loads).
+struct EndPre {
+  unsigned int L[6];       // local-frame AABB keys of this step
+  double an[3], ann[3];    // anchors of this step and of the next
+  double dn[3];            // the anchor node's predicted displacement for the next step
+  double apos[3];          // the anchor's reference position
+  int32_t movable;
+};
+
+__device__ __forceinline__ void end_pre_fp32c(const DevView &v, uint32_t k, uint32_t g0, const DevPart &P,
+                                              EndPre &e) {
+  const unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
+  for (int c = 0; c < 6; ++c) e.L[c] = L[c];
+  for (int c = 0; c < 3; ++c) {
+    e.an[c] = v.anchor[3 * (uint64_t)k + c];
+    e.ann[c] = v.anchor_next[3 * (uint64_t)k + c];
+    e.dn[c] = v.disp_next[g0 + c * v.Ncap];
+    e.apos[c] = P.anchor_pos[c];
+  }
+  e.movable = P.movable;
+}
+
 // End-of-step work of the FP32 form for one particle: AABB from the local-frame keys of this
 // step (widened by a few float ulps each way), anchors moved on by one step, the next step's
 // wall planes (wall_next) expressed in the frame of the next step's records.
-__device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const DevPart &P,
+__device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k, const EndPre &e,
                                                    const double *wall_next) {
   double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
   double *ann = v.anchor_next + 3 * (uint64_t)k;
   unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
-  if (P.movable) {
+  if (e.movable) {
     for (int c = 0; c < 3; ++c) {
-      const float lo = fval(L[c]), hi = fval(L[3 + c]);
-      const double base = P.anchor_pos[c] + an[c];
-      const double e = 8.0 * (double)FLT_EPSILON * fmax(fabs((double)lo), fabs((double)hi)) + 1e-30;
-      v.lrtb[6 * (uint64_t)k + c] = base + (double)lo - e;
-      v.lrtb[6 * (uint64_t)k + 3 + c] = base + (double)hi + e;
+      const float lo = fval(e.L[c]), hi = fval(e.L[3 + c]);
+      const double base = e.apos[c] + e.an[c];
+      const double w = 8.0 * (double)FLT_EPSILON * fmax(fabs((double)lo), fabs((double)hi)) + 1e-30;
+      v.lrtb[6 * (uint64_t)k + c] = base + (double)lo - w;
+      v.lrtb[6 * (uint64_t)k + 3 + c] = base + (double)hi + w;
     }
   }
   for (int c = 0; c < 3; ++c) {
@@ -187,13 +210,13 @@ __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k,
   }
   // disp_next holds the next step's predicted displacement of the anchor node
   for (int c = 0; c < 3; ++c) {
-    an[c] = ann[c];
-    ann[c] = v.disp_next[P.g0 + c * v.Ncap];
+    an[c] = e.ann[c];
+    ann[c] = e.dn[c];
   }
   float *wl = v.wall_local + 6 * (uint64_t)k;
   for (int f = 0; f < 6; ++f) {
     const int c = f % 3;
-    wl[f] = (float)(wall_next[f] - (P.anchor_pos[c] + an[c]));
+    wl[f] = (float)(wall_next[f] - (e.apos[c] + e.ann[c]));
   }
 }
 

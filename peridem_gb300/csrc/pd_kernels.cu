@@ -320,14 +320,18 @@ __global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < v.P) {
     DevPart &P = v.parts[k];
-    const DevSimState &st = v.ss[P.sim];
-    const DevSimParams &sp = v.sp[P.sim];
+    const uint32_t sim = P.sim;
+    EndPre pre;
+    if (v.rec) end_pre_fp32c(v, k, P.g0, P, pre);
+    const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);  // this step's bound
+    const DevSimState &st = v.ss[sim];
+    const DevSimParams &sp = v.sp[sim];
     if (st.active) {
       double wall_next[6];
       for (int c = 0; c < 6; ++c) wall_next[c] = st.wall[c] + st.spd[c] * sp.dt;  // timeloop.h:791-796
       const uint32_t tn = st.t + 1;
       if (v.rec) {
-        end_particle_fp32c(v, k, P, wall_next);
+        end_particle_fp32c(v, k, pre, wall_next);
       } else {
         unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
         if (P.movable) {
@@ -373,7 +377,6 @@ __global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_
         const bool torque_next = st.torque || (sp.set_torque_ts != -1 && tn == (uint32_t)sp.set_torque_ts);
         bool need = (P.movable && P.has_ext) || torque_next;
         if (!need && P.movable && P.stoppable && sp.allow_wall) {
-          const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);
           const double lim = sp.Rc * 1.001 + 2.0 * move + 1e-12;
           const double *b = v.lrtb + 6 * (uint64_t)k;
           for (int f = 0; f < 6 && !need; ++f) {
