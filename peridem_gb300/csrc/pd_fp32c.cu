@@ -375,8 +375,8 @@ __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
 }
 
 // U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register
-// cap); W: 256-bit record loads; PF: the column indices and live masks of the next PF groups
-// are loaded ahead of this group's partner records, so that the column stream's latency
+// cap); W: 256-bit record loads; PF: the column entries (index + broken flag) of the next PF
+// groups are loaded ahead of this group's partner records, so that the column stream's latency
 // overlaps the gathers and arithmetic of the current group; FX: the FP64 non-bond work is
 // done here (extra_force) instead of in a separate k_extra32 launch.
 template <int U, int W, int PF, int FX>
