@@ -32,7 +32,7 @@ inline uint64_t up32(uint64_t x) { return (x + 31) / 32 * 32; }
 inline uint64_t atleast1(uint64_t x) { return x ? x : 1; }
 }  // namespace
 
-// Mirrors every allocation of Engine::init (alloc_and_upload, build_bonds,
+// Mirrors every allocation of Engine::init (alloc_and_upload, upload_bonds,
 // alloc_candidates) for the same setups, without touching the device.
 uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap) {
   uint64_t N = 0, P = 0, S = sims.size(), ncl = 0;

@@ -273,10 +273,11 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
   if (bad) *bad = bad_p.load();
 }
 
-int Engine::build_bonds() {
+int Engine::build_bonds_host(SellHost &h) {
   // conn2NArr (load_hdf5.h:27-37): for every Connectivity row (i, j) push j onto row i and
   // i onto row j; rows keep that push order. Particles own disjoint rows, so they are filled
   // in parallel; the live masks (all bonds live at the start) follow from the degrees alone.
+  // Host work only (it runs beside the node arrays' staging and upload).
   struct PartRef {
     const HostSim *s;
     uint32_t p;
@@ -296,7 +297,7 @@ int Engine::build_bonds() {
   uint32_t maxdeg = 0;
   for (uint64_t n = 0; n < N_; ++n) maxdeg = std::max(maxdeg, deg[n]);
   if (maxdeg > 65535) {
-    err = "node degree above 65535";
+    h.err = "node degree above 65535";
     return PD_EINVAL;
   }
   h_deg_.assign(Ncap_, 0);
@@ -309,15 +310,23 @@ int Engine::build_bonds() {
   }
   E_ = h_slice_ptr_[nslices_];
   const uint64_t ncol = std::max<uint64_t>(E_, 1), nmask = std::max<uint64_t>(E_ / 32, 1);
-  std::unique_ptr<uint32_t[]> col(new uint32_t[ncol]), mask(new uint32_t[nmask]);  // every entry set below
+  h.ncol = ncol;
+  h.nmask = nmask;
+  h.col.reset(new uint32_t[ncol]);  // every entry set below
+  h.mask.reset(new uint32_t[nmask]);
+  uint32_t *col = h.col.get(), *mask = h.mask.get();
   col[0] = kNoCol;
   mask[0] = 0u;
   parallel_items((nslices_ + 63) / 64, [&](uint64_t chunk) {
-    // padding entries, and the live bits: position j of lane l is a bond iff j < deg
+    // padding entries, and the live bits: position j of lane l is a bond iff j < deg (below the
+    // slice's shortest row every lane has a bond)
     for (uint64_t sl = chunk * 64; sl < std::min<uint64_t>(nslices_, chunk * 64 + 64); ++sl) {
       const uint64_t e0 = h_slice_ptr_[sl], e1 = h_slice_ptr_[sl + 1];
       const uint64_t w = (e1 - e0) / 32;
-      for (uint64_t j = 0; j < w; ++j) {
+      uint64_t dmin = w;
+      for (int l = 0; l < 32; ++l) dmin = std::min<uint64_t>(dmin, deg[sl * 32 + l]);
+      for (uint64_t j = 0; j < dmin; ++j) mask[(e0 >> 5) + j] = 0xFFFFFFFFu;
+      for (uint64_t j = dmin; j < w; ++j) {
         uint32_t bits = 0;
         for (int l = 0; l < 32; ++l)
           if (j < deg[sl * 32 + l]) {
@@ -344,6 +353,11 @@ int Engine::build_bonds() {
   });
   initial_bonds_ = 0;
   for (uint64_t n = 0; n < N_; ++n) initial_bonds_ += deg[n];
+  return PD_OK;
+}
+
+int Engine::upload_bonds(SellHost &h) {
+  const uint64_t ncol = h.ncol, nmask = h.nmask;
   if (precision_ == PD_FP32C) {
     // record ranges of the staged bond kernel: computed on the device the first time a staged
     // variant is chosen (prepare_windows)
@@ -359,13 +373,23 @@ int Engine::build_bonds() {
   PD_TRY(dalloc(this, allocs_, &d_mask_, nmask, err));
   PD_TRY(cpy(d_slice_ptr_, h_slice_ptr_.data(), (nslices_ + 1) * 8, "upload slice_ptr"));
   PD_TRY(cpy(d_deg_, h_deg_.data(), Ncap_ * 2, "upload deg"));
-  PD_TRY(cpy(d_col_, col.get(), ncol * 4, "upload col"));
-  PD_TRY(cpy(d_mask_, mask.get(), nmask * 4, "upload mask"));
+  PD_TRY(cpy(d_col_, h.col.get(), ncol * 4, "upload col"));
+  PD_TRY(cpy(d_mask_, h.mask.get(), nmask * 4, "upload mask"));
   return PD_OK;
 }
 
 int Engine::alloc_and_upload() {
   const uint64_t C = Ncap_;
+  // the bond layout is built on the host beside the node arrays' staging and upload
+  SellHost sell;
+  int sell_rc = PD_OK;
+  std::thread sell_thread([&] { sell_rc = build_bonds_host(sell); });
+  struct Joiner {
+    std::thread &t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } sell_join{sell_thread};
   // [3][Ncap] staging in engine order; every entry is written below (padding nodes zero)
   std::unique_ptr<double[]> pos(new double[3 * C]), disp(new double[3 * C]), vel(new double[3 * C]),
       acc(new double[3 * C]), ext(new double[3 * C]), vol(new double[C]);
@@ -616,14 +640,19 @@ int Engine::alloc_and_upload() {
     PD_TRY(mset(d_afd_, 0, 3 * C * 8, "memset applied force density"));
   }
 
-  PD_TRY(build_bonds());
+  sell_thread.join();
+  if (sell_rc != PD_OK) {
+    err = sell.err;
+    return sell_rc;
+  }
+  PD_TRY(upload_bonds(sell));
 
   if (precision_ == PD_FP64) {
     PD_TRY(dalloc(this, allocs_, &d_bxi_, 3 * std::max<uint64_t>(E_, 1), err));
     PD_TRY(dalloc(this, allocs_, &d_bxin_, std::max<uint64_t>(E_, 1), err));
     PD_TRY(dalloc(this, allocs_, &d_brxin_, std::max<uint64_t>(E_, 1), err));
   } else {
-    std::vector<Rec32> r32(C);
+    std::unique_ptr<Rec32[]> r32(new Rec32[C]);  // every entry written below
     parallel_items((C + 65535) / 65536, [&](uint64_t chunk) {
       for (uint64_t g = chunk * 65536; g < std::min<uint64_t>(C, chunk * 65536 + 65536); ++g) {
         Rec32 &r = r32[g];
@@ -643,7 +672,7 @@ int Engine::alloc_and_upload() {
         err = "node records not 32-byte aligned";
         return PD_ECUDA;
       }
-      PD_TRY(up(d_rec_[b], r32.data(), C * sizeof(Rec32), "upload rec32"));
+      PD_TRY(up(d_rec_[b], r32.get(), C * sizeof(Rec32), "upload rec32"));
     }
     d_dispb_[0] = d_disp_;
     PD_TRY(dalloc(this, allocs_, &d_dispb_[1], 3 * C, err));
@@ -913,19 +942,20 @@ void Engine::rows_to_file(const double *src, uint64_t stride, uint64_t node0, ui
 int Engine::get_state(double *curpos, double *vel, double *acc, double *force, double *disp) {
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
   const uint64_t C = Ncap_;
-  std::vector<double> buf(3 * C);
-  auto scatter = [&](double *dst) { rows_to_file(buf.data(), C, 0, N_, dst); };
+  std::unique_ptr<double[]> buf(new double[3 * C]);  // staging, overwritten by each copy
+  auto scatter = [&](double *dst) { rows_to_file(buf.get(), C, 0, N_, dst); };
   auto fetch = [&](const double *d, double *dst) -> int {
-    PD_TRY(cpy(buf.data(), d, 3 * C * 8, "read state"));
+    PD_TRY(cpy(buf.get(), d, 3 * C * 8, "read state"));
     scatter(dst);
     return PD_OK;
   };
   if (curpos || disp) {
-    std::vector<double> dsp(3 * N_);
+    std::unique_ptr<double[]> dsp_buf(new double[3 * N_]);  // every entry written by fetch
+    double *dsp = dsp_buf.get();
     const bool fused = precision_ == PD_FP32C;
-    PD_TRY(fetch(fused ? d_dispb_[cur_ ^ 1] : d_disp_, dsp.data()));
+    PD_TRY(fetch(fused ? d_dispb_[cur_ ^ 1] : d_disp_, dsp));
     if (disp) {
-      std::memcpy(disp, dsp.data(), 3 * N_ * 8);
+      std::memcpy(disp, dsp, 3 * N_ * 8);
       if (fused && steps_done_ > 0)  // clamped nodes end each step at zero (timeloop.h:767-774)
         for (uint32_t g : h_clamped_)
           for (int c = 0; c < 3; ++c) disp[3 * (uint64_t)g + c] = 0.0;
@@ -946,7 +976,7 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
         uint64_t off = 0;
         for (auto &s : sims_) {
           const uint64_t n3 = 3 * s.node_offset[s.np];
-          const double *sp = s.pos.data(), *dp = dsp.data() + 3 * off;
+          const double *sp = s.pos.data(), *dp = dsp + 3 * off;
           double *cp = curpos + 3 * off;
           parallel_items((n3 + 65535) / 65536, [&](uint64_t chunk) {
             for (uint64_t k = chunk * 65536; k < std::min<uint64_t>(n3, chunk * 65536 + 65536); ++k)
@@ -1183,9 +1213,9 @@ int Engine::get_afd(double *afd) {
     std::memset(afd, 0, 3 * N_ * 8);
     return PD_OK;
   }
-  std::vector<double> buf(3 * Ncap_);
-  PD_TRY(cpy(buf.data(), d_afd_, 3 * Ncap_ * 8, "read applied force density"));
-  rows_to_file(buf.data(), Ncap_, 0, N_, afd);
+  std::unique_ptr<double[]> buf(new double[3 * Ncap_]);
+  PD_TRY(cpy(buf.get(), d_afd_, 3 * Ncap_ * 8, "read applied force density"));
+  rows_to_file(buf.get(), Ncap_, 0, N_, afd);
   return PD_OK;
 }
 

@@ -35,6 +35,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -352,7 +353,14 @@ class Engine {
  private:
   int alloc_and_upload();
   int alloc_candidates();
-  int build_bonds();
+  // Host-side SELL-32 arrays of the bonds, built by build_bonds_host and uploaded by upload_bonds.
+  struct SellHost {
+    std::unique_ptr<uint32_t[]> col, mask;
+    uint64_t ncol = 0, nmask = 0;
+    std::string err;
+  };
+  int build_bonds_host(SellHost &h);
+  int upload_bonds(SellHost &h);
   int launch_step_seq(int cur, cudaStream_t s);
   int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
