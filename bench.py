@@ -480,7 +480,7 @@ def ours(args):
         e2e = {"value": sum_over_ranks(dist, K * s.n_bonds_directed) / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                "what": "pd_create_from_arrays (host arrays -> HBM, bond lists built) + K steps + "
-                       "pd_get_state/pd_get_disp to host, wall clock",
+                       "pd_get_node_state to host, wall clock",
                "split_s": {"create": tc - t0, "steps": ts - tc, "readback": t1 - ts}}
         sim_e.close()
 

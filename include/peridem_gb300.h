@@ -176,6 +176,8 @@ int pd_set_stream(pd_sim *sim, void *cuda_stream);
 int pd_num_nodes(const pd_sim *sim, uint64_t *n_nodes, uint32_t *n_particles);
 int pd_get_state(pd_sim *sim, double *curpos, double *vel, double *acc, double *force);
 int pd_get_disp(pd_sim *sim, double *disp);
+/* pd_get_state and pd_get_disp in one call (the displacement is read from the device once). */
+int pd_get_node_state(pd_sim *sim, double *curpos, double *vel, double *acc, double *force, double *disp);
 /* applied_force_density (N*3): non-zero on the particle_w_fixed_velocity particle once the
  * velocity constraint is on (timeloop.h:760-764, saved at timeloop.h:844-848). */
 int pd_get_applied_force_density(pd_sim *sim, double *afd);

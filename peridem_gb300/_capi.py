@@ -99,6 +99,7 @@ SIGNATURES = [
     ("pd_num_nodes", C.c_int, [_P, C.POINTER(_u64), C.POINTER(_u32)]),
     ("pd_get_state", C.c_int, [_P, _P, _P, _P, _P]),
     ("pd_get_disp", C.c_int, [_P, _P]),
+    ("pd_get_node_state", C.c_int, [_P, _P, _P, _P, _P, _P]),
     ("pd_get_applied_force_density", C.c_int, [_P, _P]),
     ("pd_set_state", C.c_int, [_P, _P, _P, _P]),
     ("pd_get_connectivity", C.c_int, [_P, _u32, _P, _u64, C.POINTER(_u64)]),

@@ -183,6 +183,11 @@ int pd_get_disp(pd_sim *s, double *disp) {
   return s->eng.get_state(nullptr, nullptr, nullptr, nullptr, disp);
 }
 
+int pd_get_node_state(pd_sim *s, double *curpos, double *vel, double *acc, double *force, double *disp) {
+  if (!s) return fail_global(PD_EINVAL, "null handle");
+  return s->eng.get_state(curpos, vel, acc, force, disp);
+}
+
 int pd_set_state(pd_sim *s, const double *disp, const double *vel, const double *acc) {
   if (!s) return fail_global(PD_EINVAL, "null handle");
   return s->eng.set_state(disp, vel, acc);

@@ -261,10 +261,21 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
       }
     }
     std::vector<uint32_t> idx(nloc);
-    for (uint64_t k = 0; k < nloc; ++k) idx[k] = (uint32_t)k;
-    for (uint64_t w0 = 0; w0 < nloc; w0 += kOrderWindow)
-      std::stable_sort(idx.begin() + w0, idx.begin() + std::min<uint64_t>(nloc, w0 + kOrderWindow),
-                       [&](uint32_t a, uint32_t b) { return dg[a] > dg[b]; });
+    std::vector<uint32_t> hist;
+    for (uint64_t w0 = 0; w0 < nloc; w0 += kOrderWindow) {
+      const uint64_t w1 = std::min<uint64_t>(nloc, w0 + kOrderWindow);
+      uint32_t dmax = 0;
+      for (uint64_t k = w0; k < w1; ++k) dmax = std::max(dmax, dg[k]);
+      if (dmax < 4096) {  // stable counting sort by descending count
+        hist.assign(dmax + 2, 0);
+        for (uint64_t k = w0; k < w1; ++k) hist[dmax - dg[k] + 1]++;
+        for (uint32_t d = 1; d <= dmax + 1; ++d) hist[d] += hist[d - 1];
+        for (uint64_t k = w0; k < w1; ++k) idx[w0 + hist[dmax - dg[k]]++] = (uint32_t)k;
+      } else {
+        for (uint64_t k = w0; k < w1; ++k) idx[k] = (uint32_t)k;
+        std::stable_sort(idx.begin() + w0, idx.begin() + w1, [&](uint32_t a, uint32_t b) { return dg[a] > dg[b]; });
+      }
+    }
     for (uint64_t k = 0; k < nloc; ++k) {
       file_of[g0 + k] = (uint32_t)(g0 + idx[k]);
       node_of[g0 + idx[k]] = (uint32_t)(g0 + k);

@@ -83,8 +83,8 @@ class Sim:
     # -- state -----------------------------------------------------------------------------
     def state(self) -> dict:
         out = {k: np.empty((self.N, 3)) for k in ("curpos", "vel", "acc", "force", "disp")}
-        self._ck(lib().pd_get_state(self.h, ptr(out["curpos"]), ptr(out["vel"]), ptr(out["acc"]), ptr(out["force"])))
-        self._ck(lib().pd_get_disp(self.h, ptr(out["disp"])))
+        self._ck(lib().pd_get_node_state(self.h, ptr(out["curpos"]), ptr(out["vel"]), ptr(out["acc"]),
+                                         ptr(out["force"]), ptr(out["disp"])))
         return out
 
     def applied_force_density(self) -> np.ndarray:
