@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <thread>
 
 #include "pd_engine.h"
@@ -394,7 +395,14 @@ int Engine::alloc_and_upload() {
   // the bond layout is built on the host beside the node arrays' staging and upload
   SellHost sell;
   int sell_rc = PD_OK;
-  std::thread sell_thread([&] { sell_rc = build_bonds_host(sell); });
+  std::thread sell_thread([&] {
+    try {
+      sell_rc = build_bonds_host(sell);
+    } catch (const std::bad_alloc &) {  // an exception must not leave the thread
+      sell.err = "host memory exhausted while building the bond lists";
+      sell_rc = PD_ENOMEM;
+    }
+  });
   struct Joiner {
     std::thread &t;
     ~Joiner() {
