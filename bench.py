@@ -571,7 +571,7 @@ def main():
     ap.add_argument("--acc-steps-c1", type=int, default=4000)
     ap.add_argument("--acc-steps-c2", type=int, default=0, help="also compare both forms on the bench workload")
     ap.add_argument("--acc-steps-c3", type=int, default=0, help="also compare both forms on the notched plate")
-    ap.add_argument("--other-configs", default="two_sphere,cubes125,notched_plate",
+    ap.add_argument("--other-configs", default="two_sphere,cubes125,notched_plate,crush512_4m",
                     help="comma-separated workloads timed beside the headline ('' to skip)")
     ap.add_argument("--other-steps", type=int, default=200)
     ap.add_argument("--serve", type=int, default=256, help="requests of the serving stream (0: skip)")

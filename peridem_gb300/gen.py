@@ -320,6 +320,16 @@ def crush512(n=8, box=12.0 * MM, seed=2, steps=10000, dt=5e-9, hs=(0.05 * MM, 0.
     return s, base_config(dt, steps, speed_wall_z_max=wall_speed)
 
 
+def crush512_4m(steps=10000):
+    """Config 2 at the node count quoted beside it (~4 M nodes, ~3.5e8 directed bonds): the same
+    512-particle packing with every lattice spacing scaled by 0.6 (h from {0.03, 0.045, 0.06}
+    mm) and dt lowered to 3e-9 s, below the bond-based critical step delta*sqrt(rho/(18 K))
+    of the finest lattice (4.8e-9 s at h = 0.03 mm)."""
+    s, cfg = crush512(steps=steps, dt=3e-9, hs=(0.03 * MM, 0.045 * MM, 0.06 * MM))
+    s.meta["name"] = "crush512_4m"
+    return s, cfg
+
+
 def aggregate(n_particles: int, seed: int, steps: int, wall_speed: float = -1.0, dt=5e-9, pitch=1.5 * MM,
               hs=(0.05 * MM, 0.075 * MM, 0.1 * MM), smin=0.6 * MM, smax=1.4 * MM):
     """One aggregate of the serving stream: n_particles drawn like config 2's particles, packed
@@ -356,7 +366,8 @@ def serving_stream(n: int = 256, rate: float = 4.0, seed: int = 3, pmin: int = 8
     return out
 
 
-WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512, "notched_plate": notched_plate}
+WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512, "crush512_4m": crush512_4m,
+             "notched_plate": notched_plate}
 
 
 def build_aggregate(kw: dict):
