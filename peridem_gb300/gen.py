@@ -308,24 +308,27 @@ def _grid_pack(rng, m: int, count: int, pitch: float, hs, smin: float, smax: flo
 
 
 def crush512(n=8, box=12.0 * MM, seed=2, steps=10000, dt=5e-9, hs=(0.05 * MM, 0.075 * MM, 0.1 * MM),
-             smin=0.6 * MM, smax=1.4 * MM, wall_speed=-1.0):
-    """Config 2: n^3 particles of random shape/size/resolution in a box; top wall moves down."""
+             smin=0.6 * MM, smax=1.4 * MM, wall_speed=-1.0, count=None):
+    """Config 2: n^3 particles of random shape/size/resolution in a box; top wall moves down.
+    count: only the first `count` particles of the same packing (the contact stiffness is the
+    whole packing's, whose largest nodal volume is max(hs)^3)."""
     rng = np.random.default_rng(seed)
     Rc = 0.5 * min(hs)
-    parts = _grid_pack(rng, n, n ** 3, box / n, hs, smin, smax)
+    parts = _grid_pack(rng, n, n ** 3 if count is None else min(int(count), n ** 3), box / n, hs, smin, smax)
     half = box / 2
     wall = dict(allow=1, geom=[-half, -half, -half, half, half, half])
-    s = finish(parts, Rc, dt, wall=wall)
+    kn = None if count is None else stable_kn(kn_rule(Rc), GLASS["rho"], max(hs) ** 3, dt)
+    s = finish(parts, Rc, dt, wall=wall, kn=kn)
     s.meta["name"] = "crush512"
     return s, base_config(dt, steps, speed_wall_z_max=wall_speed)
 
 
-def crush512_4m(steps=10000):
+def crush512_4m(steps=10000, count=None):
     """Config 2 at the node count quoted beside it (~4 M nodes, ~3.5e8 directed bonds): the same
     512-particle packing with every lattice spacing scaled by 0.6 (h from {0.03, 0.045, 0.06}
     mm) and dt lowered to 3e-9 s, below the bond-based critical step delta*sqrt(rho/(18 K))
     of the finest lattice (4.8e-9 s at h = 0.03 mm)."""
-    s, cfg = crush512(steps=steps, dt=3e-9, hs=(0.03 * MM, 0.045 * MM, 0.06 * MM))
+    s, cfg = crush512(steps=steps, dt=3e-9, hs=(0.03 * MM, 0.045 * MM, 0.06 * MM), count=count)
     s.meta["name"] = "crush512_4m"
     return s, cfg
 
