@@ -648,19 +648,43 @@ void launch_bond_constants(const DevView &v, double *bxi, double *bxin, double *
   if (blocks) k_bond_constants<<<(unsigned)blocks, 128, 0, s>>>(v, bxi, bxin, brxin);
 }
 
-// AABBs of all particles before the loop (timeloop.h:389-393).
+// AABBs of all particles before the loop (timeloop.h:389-393). A warp whose nodes all belong to
+// one particle reduces its keys with shuffles first (min/max are exact, so the result does not
+// depend on how they are combined), which keeps the atomics on a particle's six keys few.
 __global__ void k_init_lrtb_acc(DevView v) {
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N) return;
-  const uint32_t k = v.pid[n];
-  D3 cur = ld3(v.pos, n, v.Ncap) + ld3(v.disp, n, v.Ncap);
-  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
-  atomicMin(&L[0], ord_key(cur.x));
-  atomicMin(&L[1], ord_key(cur.y));
-  atomicMin(&L[2], ord_key(cur.z));
-  atomicMax(&L[3], ord_key(cur.x));
-  atomicMax(&L[4], ord_key(cur.y));
-  atomicMax(&L[5], ord_key(cur.z));
+  const bool valid = n < v.N;
+  const uint32_t k = valid ? v.pid[n] : 0xFFFFFFFFu;
+  unsigned long long lo[3], hi[3];
+  if (valid) {
+    const D3 cur = ld3(v.pos, n, v.Ncap) + ld3(v.disp, n, v.Ncap);
+    lo[0] = hi[0] = ord_key(cur.x);
+    lo[1] = hi[1] = ord_key(cur.y);
+    lo[2] = hi[2] = ord_key(cur.z);
+  } else {
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = ord_key(INFINITY);
+      hi[c] = ord_key(-INFINITY);
+    }
+  }
+  const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+  if (__all_sync(0xffffffffu, !valid || k == k0)) {  // lanes past N carry the identity keys
+    if (k0 == 0xFFFFFFFFu) return;
+    for (int o = 16; o > 0; o >>= 1)
+      for (int c = 0; c < 3; ++c) {
+        lo[c] = min(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+        hi[c] = max(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+      }
+    if ((threadIdx.x & 31) != 0) return;
+  } else if (!valid) {
+    return;
+  }
+  const uint64_t kp = valid ? k : k0;
+  unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * kp;
+  for (int c = 0; c < 3; ++c) {
+    atomicMin(&L[c], lo[c]);
+    atomicMax(&L[3 + c], hi[c]);
+  }
 }
 __global__ void k_init_lrtb_fin(DevView v) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
