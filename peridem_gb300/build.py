@@ -29,6 +29,7 @@ UNITS = [
     ("pd_fp32c.cu", []),
     ("pd_noalloc.cu", []),
     ("pd_pairs.cu", ["-fmad=false"]),
+    ("pd_sell.cu", []),
     ("pd_engine.cu", ["-fmad=false"]),
     ("pd_capi.cpp", []),
     ("pd_batch.cpp", []),

@@ -195,7 +195,7 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   final_.assign(S_, std::vector<double>());
   {
     int64_t bad = -1;
-    order_nodes(sims_, file_of_, node_of_, deg_file_, &bad);
+    order_nodes(sims_, file_of_, node_of_, deg_file_, &bad, &conn_sorted_);
     if (bad >= 0) {
       err = "Connectivity index out of range in particle " + std::to_string(bad);
       return PD_EINVAL;
@@ -220,7 +220,8 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
 
 
 void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
-                         std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file, int64_t *bad) {
+                         std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file, int64_t *bad,
+                         bool *sorted) {
   // The SELL-32 layout pads every row of a slice to the slice's longest row. In file order a
   // slice mixes interior nodes (full neighbourhoods) with surface nodes (truncated ones);
   // sorting by bond count makes the rows of a slice nearly equal (crush512: padded entries
@@ -246,12 +247,15 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
   file_of.assign(N, 0);
   node_of.assign(N, 0);
   std::atomic<int64_t> bad_p(-1);
+  std::atomic<bool> all_sorted(true);
   parallel_items(parts.size(), [&](uint64_t x) {
     const HostSim &s = *parts[x].s;
     const uint32_t p = parts[x].p;
     const uint64_t g0 = parts[x].g0;
     const uint64_t nloc = s.node_offset[p + 1] - s.node_offset[p];
     uint32_t *dg = deg_file.data() + g0;
+    bool srt = true;  // pairs i < j in strictly increasing (i, j) order: every row ascending
+    uint64_t prev = 0;
     for (uint64_t l = s.conn_offset[p]; l < s.conn_offset[p + 1]; ++l) {
       const uint32_t i = s.conn[2 * l], j = s.conn[2 * l + 1];
       if (i < nloc && j < nloc) {
@@ -260,7 +264,11 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
       } else {
         bad_p = (int64_t)p;
       }
+      const uint64_t key = ((uint64_t)i << 32) | j;
+      srt = srt && i < j && (l == s.conn_offset[p] || key > prev);
+      prev = key;
     }
+    if (!srt) all_sorted = false;
     std::vector<uint32_t> idx(nloc);
     std::vector<uint32_t> hist;
     for (uint64_t w0 = 0; w0 < nloc; w0 += kOrderWindow) {
@@ -283,6 +291,7 @@ void Engine::order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t>
     }
   });
   if (bad) *bad = bad_p.load();
+  if (sorted) *sorted = all_sorted.load();
 }
 
 int Engine::build_bonds_host(SellHost &h) {
@@ -303,24 +312,14 @@ int Engine::build_bonds_host(SellHost &h) {
       gnode += s.node_offset[s.np];
     }
   }
-  // bond counts per engine node (counted by order_nodes, which also checked the indices)
-  std::vector<uint32_t> deg(Ncap_, 0);
-  for (uint64_t g = 0; g < N_; ++g) deg[node_of_[g]] = deg_file_[g];
-  uint32_t maxdeg = 0;
-  for (uint64_t n = 0; n < N_; ++n) maxdeg = std::max(maxdeg, deg[n]);
-  if (maxdeg > 65535) {
-    h.err = "node degree above 65535";
-    return PD_EINVAL;
+  std::vector<uint32_t> deg;
+  {
+    const int rc = bond_counts(deg, nullptr);
+    if (rc != PD_OK) {
+      h.err = "node degree above 65535";
+      return rc;
+    }
   }
-  h_deg_.assign(Ncap_, 0);
-  for (uint64_t n = 0; n < Ncap_; ++n) h_deg_[n] = (uint16_t)deg[n];
-  h_slice_ptr_.assign(nslices_ + 1, 0);
-  for (uint64_t s = 0; s < nslices_; ++s) {
-    uint32_t w = 0;
-    for (int l = 0; l < 32; ++l) w = std::max(w, deg[s * 32 + l]);
-    h_slice_ptr_[s + 1] = h_slice_ptr_[s] + 32ull * w;
-  }
-  E_ = h_slice_ptr_[nslices_];
   const uint64_t ncol = std::max<uint64_t>(E_, 1), nmask = std::max<uint64_t>(E_ / 32, 1);
   h.ncol = ncol;
   h.nmask = nmask;
@@ -363,13 +362,61 @@ int Engine::build_bonds_host(SellHost &h) {
       fill[b]++;
     }
   });
-  initial_bonds_ = 0;
-  for (uint64_t n = 0; n < N_; ++n) initial_bonds_ += deg[n];
   return PD_OK;
 }
 
-int Engine::upload_bonds(SellHost &h) {
-  const uint64_t ncol = h.ncol, nmask = h.nmask;
+int Engine::bond_counts(std::vector<uint32_t> &deg, std::vector<uint64_t> *rowptr) {
+  // bond counts per engine node (counted by order_nodes, which also checked the indices),
+  // slice widths, and the row starts of a row-contiguous layout when asked for
+  deg.assign(Ncap_, 0);
+  const uint64_t nchunk = (Ncap_ + 65535) / 65536;
+  std::vector<uint32_t> cmax(nchunk, 0);
+  std::vector<uint64_t> csum(nchunk + 1, 0);
+  parallel_items(nchunk, [&](uint64_t c) {
+    uint32_t m = 0;
+    for (uint64_t g = c * 65536; g < std::min<uint64_t>(N_, c * 65536 + 65536); ++g) {
+      deg[node_of_[g]] = deg_file_[g];
+      m = std::max(m, deg_file_[g]);
+    }
+    cmax[c] = m;
+  });
+  uint32_t maxdeg = 0;
+  for (uint32_t m : cmax) maxdeg = std::max(maxdeg, m);
+  if (maxdeg > 65535) return PD_EINVAL;
+  h_deg_.assign(Ncap_, 0);
+  if (rowptr) rowptr->assign(Ncap_ + 1, 0);
+  parallel_items(nchunk, [&](uint64_t c) {
+    uint64_t t = 0;
+    for (uint64_t n = c * 65536; n < std::min<uint64_t>(Ncap_, c * 65536 + 65536); ++n) {
+      h_deg_[n] = (uint16_t)deg[n];
+      if (rowptr) (*rowptr)[n] = t;  // offset inside the chunk for now
+      t += deg[n];
+    }
+    csum[c + 1] = t;
+  });
+  for (uint64_t c = 0; c < nchunk; ++c) csum[c + 1] += csum[c];
+  initial_bonds_ = csum[nchunk];
+  if (rowptr) {
+    parallel_items(nchunk, [&](uint64_t c) {
+      for (uint64_t n = c * 65536; n < std::min<uint64_t>(Ncap_, c * 65536 + 65536); ++n) (*rowptr)[n] += csum[c];
+    });
+    (*rowptr)[Ncap_] = csum[nchunk];
+  }
+  h_slice_ptr_.assign(nslices_ + 1, 0);
+  parallel_items((nslices_ + 4095) / 4096, [&](uint64_t c) {
+    for (uint64_t sl = c * 4096; sl < std::min<uint64_t>(nslices_, c * 4096 + 4096); ++sl) {
+      uint32_t w = 0;
+      for (int l = 0; l < 32; ++l) w = std::max(w, deg[sl * 32 + l]);
+      h_slice_ptr_[sl + 1] = 32ull * w;  // widths for now
+    }
+  });
+  for (uint64_t sl = 0; sl < nslices_; ++sl) h_slice_ptr_[sl + 1] += h_slice_ptr_[sl];
+  E_ = h_slice_ptr_[nslices_];
+  return PD_OK;
+}
+
+int Engine::alloc_bond_arrays() {
+  const uint64_t ncol = std::max<uint64_t>(E_, 1), nmask = std::max<uint64_t>(E_ / 32, 1);
   if (precision_ == PD_FP32C) {
     // record ranges of the staged bond kernel: computed on the device the first time a staged
     // variant is chosen (prepare_windows)
@@ -385,6 +432,96 @@ int Engine::upload_bonds(SellHost &h) {
   PD_TRY(dalloc(this, allocs_, &d_mask_, nmask, err));
   PD_TRY(cpy(d_slice_ptr_, h_slice_ptr_.data(), (nslices_ + 1) * 8, "upload slice_ptr"));
   PD_TRY(cpy(d_deg_, h_deg_.data(), Ncap_ * 2, "upload deg"));
+  return PD_OK;
+}
+
+int Engine::build_bonds_gpu(bool &fallback) {
+  fallback = false;
+  std::vector<uint32_t> deg;
+  std::vector<uint64_t> rowptr;
+  if (bond_counts(deg, &rowptr) != PD_OK) {
+    err = "node degree above 65535";
+    return PD_EINVAL;
+  }
+  // per-particle pair offsets and first nodes, particles of all simulations concatenated
+  std::vector<uint64_t> pair_off(1, 0), node0;
+  uint64_t gnode = 0;
+  for (auto &s : sims_) {
+    for (uint32_t p = 0; p < s.np; ++p) {
+      pair_off.push_back(pair_off.back() + (s.conn_offset[p + 1] - s.conn_offset[p]));
+      node0.push_back(gnode + s.node_offset[p]);
+    }
+    gnode += s.node_offset[s.np];
+  }
+  const uint64_t npairs = pair_off.back();
+  // scratch (not part of the handle's memory): freed before this returns
+  void *t_conn = nullptr, *t_off = nullptr, *t_node0 = nullptr, *t_rowptr = nullptr, *t_cursor = nullptr,
+       *t_rows = nullptr;
+  auto tfree = [&] {
+    for (void *q : {t_conn, t_off, t_node0, t_rowptr, t_cursor, t_rows})
+      if (q) cudaFreeAsync(q, stream_);
+  };
+  auto talloc = [&](void **q, size_t bytes) {
+    if (cudaMallocAsync(q, bytes ? bytes : 8, stream_) != cudaSuccess) {
+      cudaGetLastError();
+      *q = nullptr;
+      return false;
+    }
+    return true;
+  };
+  if (!talloc(&t_conn, npairs * 8) || !talloc(&t_off, pair_off.size() * 8) ||
+      !talloc(&t_node0, node0.size() * 8) || !talloc(&t_rowptr, rowptr.size() * 8) ||
+      !talloc(&t_cursor, Ncap_ * 4) || !talloc(&t_rows, initial_bonds_ * 4)) {
+    tfree();
+    fallback = true;  // no room for the scratch: the host builds the arrays
+    return PD_OK;
+  }
+  int rc = PD_OK;
+  {
+    uint64_t at = 0;
+    for (auto &s : sims_) {
+      const uint64_t m = s.conn_offset[s.np];
+      if (m && rc == PD_OK)
+        rc = check(cudaMemcpyAsync((char *)t_conn + at * 8, s.conn.data(), m * 8, cudaMemcpyHostToDevice,
+                                   stream_), "upload Connectivity");
+      at += m;
+    }
+  }
+  auto h2d = [&](void *dst, const void *src, size_t bytes, const char *what) {
+    if (rc == PD_OK) rc = check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream_), what);
+  };
+  h2d(t_off, pair_off.data(), pair_off.size() * 8, "upload pair offsets");
+  h2d(t_node0, node0.data(), node0.size() * 8, "upload node offsets");
+  h2d(t_rowptr, rowptr.data(), rowptr.size() * 8, "upload row starts");
+  if (rc == PD_OK) rc = check(cudaMemsetAsync(t_cursor, 0, Ncap_ * 4, stream_), "zero row cursors");
+  if (rc == PD_OK) rc = alloc_bond_arrays();
+  if (rc == PD_OK) {
+    SellBuild b;
+    b.conn = (const uint32_t *)t_conn;
+    b.npairs = npairs;
+    b.pair_off = (const uint64_t *)t_off;
+    b.node0 = (const uint64_t *)t_node0;
+    b.nparts = (uint32_t)node0.size();
+    b.node_of = d_node_of_;
+    b.rowptr = (const uint64_t *)t_rowptr;
+    b.cursor = (uint32_t *)t_cursor;
+    b.rows = (uint32_t *)t_rows;
+    b.n_nodes = N_;
+    b.slice_ptr = d_slice_ptr_;
+    b.nslices = nslices_;
+    b.col = d_col_;
+    b.mask = d_mask_;
+    launch_sell_build(b, stream_);
+    rc = check(cudaGetLastError(), "bond build kernels");
+  }
+  tfree();
+  if (rc == PD_OK) rc = check(cudaStreamSynchronize(stream_), "bond build");
+  return rc;
+}
+
+int Engine::upload_bonds(SellHost &h) {
+  const uint64_t ncol = h.ncol, nmask = h.nmask;
+  PD_TRY(alloc_bond_arrays());
   PD_TRY(cpy(d_col_, h.col.get(), ncol * 4, "upload col"));
   PD_TRY(cpy(d_mask_, h.mask.get(), nmask * 4, "upload mask"));
   return PD_OK;
@@ -392,17 +529,20 @@ int Engine::upload_bonds(SellHost &h) {
 
 int Engine::alloc_and_upload() {
   const uint64_t C = Ncap_;
-  // the bond layout is built on the host beside the node arrays' staging and upload
+  // The bond layout: built on the device from a sorted Connectivity (after the node arrays'
+  // upload, it needs node_of), else on the host beside the node arrays' staging and upload.
   SellHost sell;
   int sell_rc = PD_OK;
-  std::thread sell_thread([&] {
+  auto host_build = [&] {
     try {
       sell_rc = build_bonds_host(sell);
     } catch (const std::bad_alloc &) {  // an exception must not leave the thread
       sell.err = "host memory exhausted while building the bond lists";
       sell_rc = PD_ENOMEM;
     }
-  });
+  };
+  std::thread sell_thread;
+  if (!conn_sorted_) sell_thread = std::thread(host_build);
   struct Joiner {
     std::thread &t;
     ~Joiner() {
@@ -659,12 +799,24 @@ int Engine::alloc_and_upload() {
     PD_TRY(mset(d_afd_, 0, 3 * C * 8, "memset applied force density"));
   }
 
-  sell_thread.join();
-  if (sell_rc != PD_OK) {
-    err = sell.err;
-    return sell_rc;
+  bool host_bonds = !conn_sorted_;
+  if (conn_sorted_) {
+    bool fallback = false;
+    PD_TRY(build_bonds_gpu(fallback));
+    if (fallback) {  // no device room for the build's scratch
+      host_bonds = true;
+      host_build();
+    }
+  } else {
+    sell_thread.join();
   }
-  PD_TRY(upload_bonds(sell));
+  if (host_bonds) {
+    if (sell_rc != PD_OK) {
+      err = sell.err;
+      return sell_rc;
+    }
+    PD_TRY(upload_bonds(sell));
+  }
 
   if (precision_ == PD_FP64) {
     PD_TRY(dalloc(this, allocs_, &d_bxi_, 3 * std::max<uint64_t>(E_, 1), err));

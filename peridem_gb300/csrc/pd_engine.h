@@ -334,7 +334,8 @@ class Engine {
   // deg_file = bond count of each node in file order (indices out of range are not counted).
   static void order_nodes(const std::vector<HostSim> &sims, std::vector<uint32_t> &file_of,
                           std::vector<uint32_t> &node_of, std::vector<uint32_t> &deg_file,
-                          int64_t *bad = nullptr);  // bad: a particle with an index out of range, or -1
+                          int64_t *bad = nullptr,   // a particle with an index out of range, or -1
+                          bool *sorted = nullptr);  // every Connectivity strictly (i, j)-sorted, i < j
   int raw_alloc(void **p, size_t bytes);
   double step_bytes(uint64_t live_bonds) const;
   uint64_t initial_bonds() const { return initial_bonds_; }
@@ -361,6 +362,12 @@ class Engine {
   };
   int build_bonds_host(SellHost &h);
   int upload_bonds(SellHost &h);
+  // Bond counts per engine node (deg), h_deg_, h_slice_ptr_, E_, initial_bonds_, and the row
+  // starts of a row-contiguous layout when rowptr is given.
+  int bond_counts(std::vector<uint32_t> &deg, std::vector<uint64_t> *rowptr);
+  int alloc_bond_arrays();  // device SELL arrays (+ staged-kernel ranges), slice_ptr and deg uploaded
+  // Device build from a sorted Connectivity; fallback = true when its scratch does not fit.
+  int build_bonds_gpu(bool &fallback);
   int launch_step_seq(int cur, cudaStream_t s);
   int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
@@ -416,6 +423,7 @@ class Engine {
   // host mirrors used when reading results back
   std::vector<uint32_t> file_of_, node_of_;  // see order_nodes
   std::vector<uint32_t> deg_file_;           // bond counts in file order, while building
+  bool conn_sorted_ = false;                 // rows in push order are ascending (GPU bond build)
   std::vector<uint32_t> h_pid_;
   std::vector<uint64_t> h_slice_ptr_;
   std::vector<uint16_t> h_deg_;
@@ -460,6 +468,24 @@ class Engine {
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
   bool graphs_ok_ = false;
 };
+
+// Device build of the SELL-32 bond arrays from a strictly sorted Connectivity (pd_sell.cu).
+struct SellBuild {
+  const uint32_t *conn;      // [npairs][2] local pair indices, particles concatenated
+  uint64_t npairs;
+  const uint64_t *pair_off;  // [nparts+1] first pair of each particle
+  const uint64_t *node0;     // [nparts] first file-order node of each particle
+  uint32_t nparts;
+  const uint32_t *node_of;   // file index -> engine index
+  const uint64_t *rowptr;    // [n_nodes+1] row starts, engine order
+  uint32_t *cursor;          // [n_nodes], zeroed
+  uint32_t *rows;            // [rowptr[n_nodes]] scratch
+  uint64_t n_nodes;
+  const uint64_t *slice_ptr;
+  uint64_t nslices;
+  uint32_t *col, *mask;      // outputs
+};
+void launch_sell_build(const SellBuild &b, cudaStream_t s);
 
 // kernel launchers (pd_kernels.cu / pd_broadphase.cu)
 void launch_predict(const DevView &v, int tpb, cudaStream_t s);

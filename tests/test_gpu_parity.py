@@ -200,3 +200,24 @@ def test_fp32c_variants_identical_with_breaking():
         np.testing.assert_array_equal(c.state()["curpos"], ra["curpos"], err_msg=f"variant {v}")
         for p in range(s.n_particles):
             np.testing.assert_array_equal(c.connectivity(p), rc[p], err_msg=f"variant {v} conn {p}")
+
+
+def test_fp64_bitexact_with_unsorted_connectivity():
+    """A Connectivity in arbitrary order (pairs shuffled, some written (j, i)): rows keep the
+    reference's push order, so the FP64 form still matches the oracle bit for bit (the device
+    bond build covers sorted files; this one takes the host build)."""
+    s, cfg = cases.impact_walls(steps=20)
+    rng = np.random.default_rng(5)
+    conn = s.conn.copy()
+    for p in range(s.n_particles):
+        a, b = int(s.conn_offset[p]), int(s.conn_offset[p + 1])
+        blk = conn[a:b][rng.permutation(b - a)]
+        flip = rng.random(b - a) < 0.5
+        blk[flip] = blk[flip][:, ::-1]
+        conn[a:b] = blk
+    s.conn = np.ascontiguousarray(conn)
+    sim = Sim(s, cfg, "fp64")
+    orc = O.Oracle(s, cfg)
+    sim.step(20)
+    orc.step(20)
+    _compare_exact("unsorted", s, sim, orc, 20)
