@@ -220,9 +220,10 @@ int pd_close(pd_sim *sim);
 /* Tuning knobs: contact skin as a fraction of the contact radius (<= 0 keeps it), per-node
  * candidate capacity (0 keeps it, at most 64), threads per block (<= 0 keeps it), per-step
  * statistics on/off (< 0 keeps it; on adds the pair-count kernel), step launch mode
- * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the default, 2 the same
- * graph with the broad-phase rebuild kernels in a conditional node: fewer launches per step,
- * but the conditional node itself costs a few microseconds, which small handles feel). */
+ * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the default below 131,072
+ * nodes, 2 the same graph with the broad-phase rebuild kernels in a conditional node, the
+ * default above: fewer launches per step, but the conditional node itself costs a few
+ * microseconds, which small handles feel). */
 int pd_set_tuning(pd_sim *sim, double skin_frac, uint32_t cand_cap, int threads_per_block,
                   int stats, int use_graphs);
 /* Clears the device error word after the caller has handled it. */

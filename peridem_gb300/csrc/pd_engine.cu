@@ -184,6 +184,9 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   // handles are launch-latency bound and gain most from doing the non-bond work in the bond
   // kernel, one launch less per step)
   variant_ = N_ < 131072 ? 6 : 18;
+  // and the step graph: on large handles the broad phase's kernels are worth skipping in
+  // steps without a rebuild (a conditional node); small handles replay them, exiting at once
+  use_conditional_ = N_ >= 131072;
   sim_node0_.assign(S_ + 1, 0);
   sim_p0_.assign(S_ + 1, 0);
   for (uint32_t i = 0; i < S_; ++i) {

@@ -401,7 +401,8 @@ class Engine {
   bool torque_possible_ = false;
   bool stats_ = false;
   bool use_graphs_ = true;
-  bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning mode 2)
+  bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning
+                                  // mode 2); init() picks by size
   int variant_ = 18;  // FP32 bond-kernel variant; init() picks by size (the autotuner's usual choices)
   std::vector<std::pair<void *, size_t>> mutable_;  // device buffers that change while stepping
   void *backup_ = nullptr;

@@ -55,17 +55,25 @@ def test_fp64_bitexact(name):
     sim.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("name", ["impact_walls", "cubes_gravity"])
-def test_fp64_no_graph_same_as_graph(name):
+def test_launch_modes_give_the_same_results(name, mode, precision):
+    """Separate launches (0) and the step graph with the broad phase in a conditional node (2,
+    the default on large handles) against the plain step graph (1), rebuilds included."""
     s, cfg = cases.CASES[name]()
-    a = Sim(s, cfg, "fp64")
-    b = Sim(s, cfg, "fp64")
-    b.tune(graphs=0)
+    a = Sim(s, cfg, precision)
+    b = Sim(s, cfg, precision)
+    a.tune(graphs=1)
+    b.tune(graphs=mode)
     a.step(25)
     b.step(25)
+    if mode == 2:
+        assert b.graph_mode() in (1, 2)  # 1 where the conditional node is unsupported
     sa, sb = a.state(), b.state()
     for k in sa:
         np.testing.assert_array_equal(sa[k], sb[k])
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"] > 0
 
 
 @pytest.mark.parametrize("skin", [0.05, 0.2, 1.0])
