@@ -438,14 +438,8 @@ int Engine::alloc_bond_arrays() {
   return PD_OK;
 }
 
-int Engine::build_bonds_gpu(bool &fallback) {
+int Engine::build_bonds_gpu(const std::vector<uint64_t> &rowptr, bool &fallback) {
   fallback = false;
-  std::vector<uint32_t> deg;
-  std::vector<uint64_t> rowptr;
-  if (bond_counts(deg, &rowptr) != PD_OK) {
-    err = "node degree above 65535";
-    return PD_EINVAL;
-  }
   // per-particle pair offsets and first nodes, particles of all simulations concatenated
   std::vector<uint64_t> pair_off(1, 0), node0;
   uint64_t gnode = 0;
@@ -544,8 +538,20 @@ int Engine::alloc_and_upload() {
       sell_rc = PD_ENOMEM;
     }
   };
+  // device build: the bond counts and row starts are computed beside the node arrays' staging
+  std::vector<uint64_t> rowptr;
+  int counts_rc = PD_OK;
+  auto counts = [&] {
+    try {
+      std::vector<uint32_t> deg;
+      counts_rc = bond_counts(deg, &rowptr);
+    } catch (const std::bad_alloc &) {
+      counts_rc = PD_ENOMEM;
+    }
+  };
   std::thread sell_thread;
   if (!conn_sorted_) sell_thread = std::thread(host_build);
+  else sell_thread = std::thread(counts);
   struct Joiner {
     std::thread &t;
     ~Joiner() {
@@ -624,7 +630,6 @@ int Engine::alloc_and_upload() {
       }
       for (int c = 0; c < 3; ++c) P.anchor_pos[c] = pos[c * C + P.g0];
       h_g0_[gp] = P.g0;
-      for (uint32_t k = 0; k < P.n; ++k) h_pid_[P.g0 + k] = gp;
       if (!s.bdry_offset.empty())
         for (uint64_t l = s.bdry_offset[p]; l < s.bdry_offset[p + 1]; ++l) {
           if (s.bdry[l] >= P.n) {
@@ -740,6 +745,9 @@ int Engine::alloc_and_upload() {
   }
   half_skin_ = min_half_skin;
 
+  parallel_items(P_, [&](uint64_t gp) {  // particle of each node
+    for (uint32_t k = 0; k < parts[gp].n; ++k) h_pid_[parts[gp].g0 + k] = (uint32_t)gp;
+  });
   PD_TRY(dalloc(this, allocs_, &d_pos_, 3 * C, err));
   PD_TRY(dalloc(this, allocs_, &d_disp_, 3 * C, err));
   PD_TRY(dalloc(this, allocs_, &d_vel_[0], 3 * C, err));
@@ -804,8 +812,14 @@ int Engine::alloc_and_upload() {
 
   bool host_bonds = !conn_sorted_;
   if (conn_sorted_) {
+    sell_thread.join();
+    if (counts_rc != PD_OK) {
+      err = counts_rc == PD_ENOMEM ? "host memory exhausted while counting bonds"
+                                   : "node degree above 65535";
+      return counts_rc;
+    }
     bool fallback = false;
-    PD_TRY(build_bonds_gpu(fallback));
+    PD_TRY(build_bonds_gpu(rowptr, fallback));
     if (fallback) {  // no device room for the build's scratch
       host_bonds = true;
       host_build();

@@ -366,8 +366,9 @@ class Engine {
   // starts of a row-contiguous layout when rowptr is given.
   int bond_counts(std::vector<uint32_t> &deg, std::vector<uint64_t> *rowptr);
   int alloc_bond_arrays();  // device SELL arrays (+ staged-kernel ranges), slice_ptr and deg uploaded
-  // Device build from a sorted Connectivity; fallback = true when its scratch does not fit.
-  int build_bonds_gpu(bool &fallback);
+  // Device build from a sorted Connectivity, after bond_counts (rowptr: its row starts);
+  // fallback = true when its scratch does not fit.
+  int build_bonds_gpu(const std::vector<uint64_t> &rowptr, bool &fallback);
   int launch_step_seq(int cur, cudaStream_t s);
   int prepare_fused(int cur);  // FP32 form: predicted state for the next step from disp[cur^1]
   int capture_graphs();
