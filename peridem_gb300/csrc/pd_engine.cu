@@ -1129,6 +1129,39 @@ void Engine::rows_to_file(const double *src, uint64_t stride, uint64_t node0, ui
 
 int Engine::get_state(double *curpos, double *vel, double *acc, double *force, double *disp) {
   PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  // each array put in file order on the device, then copied straight to the caller
+  double *rows = nullptr;
+  if (cudaMallocAsync((void **)&rows, std::max<uint64_t>(3 * N_, 1) * 8, stream_) != cudaSuccess) {
+    cudaGetLastError();
+    return get_state_host(curpos, vel, acc, force, disp);  // no room for the scratch
+  }
+  const bool fused = precision_ == PD_FP32C;
+  const double *dcur = fused ? d_dispb_[cur_ ^ 1] : d_disp_;
+  const uint32_t *clist = n_clamped_ ? d_clamped_ + (P_ + 1) : nullptr;
+  int rc = PD_OK;
+  auto out = [&](const double *src, const double *add, int clamped_mode, double *dst) {
+    if (!dst || rc != PD_OK) return;
+    launch_rows_to_file(src, add, Ncap_, N_, d_file_of_, rows, stream_);
+    if (clamped_mode == 1) launch_clamped_rows(clist, n_clamped_, d_file_of_, nullptr, nullptr, Ncap_, rows, stream_);
+    if (clamped_mode == 2)
+      launch_clamped_rows(clist, n_clamped_, d_file_of_, d_pos_, d_clamped_disp_, Ncap_, rows, stream_);
+    rc = check(cudaGetLastError(), "read state");
+    if (rc == PD_OK) rc = check(cudaMemcpyAsync(dst, rows, 3 * N_ * 8, cudaMemcpyDeviceToHost, stream_), "read state");
+    if (rc == PD_OK) rc = check(cudaStreamSynchronize(stream_), "read state");
+  };
+  const bool stepped = steps_done_ > 0 && n_clamped_;
+  // clamped nodes end each step at zero (timeloop.h:767-774); the FP64 form's CurrPos keeps
+  // their predicted displacement (the FP32 form's displacement buffer already holds it)
+  out(dcur, nullptr, fused && stepped ? 1 : 0, disp);
+  out(dcur, d_pos_, !fused && stepped ? 2 : 0, curpos);
+  out(d_vel_[cur_], nullptr, 0, vel);
+  out(d_acc_, nullptr, 0, acc);
+  out(d_force_, nullptr, 0, force);
+  cudaFreeAsync(rows, stream_);
+  return rc;
+}
+
+int Engine::get_state_host(double *curpos, double *vel, double *acc, double *force, double *disp) {
   const uint64_t C = Ncap_;
   std::unique_ptr<double[]> buf(new double[3 * C]);  // staging, overwritten by each copy
   auto scatter = [&](double *dst) { rows_to_file(buf.get(), C, 0, N_, dst); };

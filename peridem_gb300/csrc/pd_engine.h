@@ -279,6 +279,8 @@ class Engine {
   int sync(int timeout_ms);
   int set_stream(cudaStream_t s);
   int get_state(double *curpos, double *vel, double *acc, double *force, double *disp);
+  // The same through host staging (when the device has no room for get_state's scratch).
+  int get_state_host(double *curpos, double *vel, double *acc, double *force, double *disp);
   int set_state(const double *disp, const double *vel, const double *acc);
   int get_connectivity(uint32_t particle, uint32_t *pairs, uint64_t cap, uint64_t *n);
   // Keeps exactly the listed bonds (local i<q pairs) of a particle alive (resume).
@@ -511,6 +513,10 @@ void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
 void launch_col_flags(const DevView &v, cudaStream_t s);
+void launch_rows_to_file(const double *src, const double *add, uint64_t Ncap, uint64_t N, const uint32_t *file_of,
+                         double *dst, cudaStream_t s);
+void launch_clamped_rows(const uint32_t *clamped, uint64_t n_clamped, const uint32_t *file_of, const double *pos,
+                         const double *cdisp, uint64_t Ncap, double *dst, cudaStream_t s);
 void launch_prescribed(const DevView &v, cudaStream_t s);
 void launch_reset_y(const DevView &v, cudaStream_t s);
 

@@ -729,6 +729,41 @@ void launch_init_lrtb(const DevView &v, cudaStream_t s) {
   k_init_lrtb_fin<<<(v.P + 127) / 128, 128, 0, s>>>(v);
 }
 
+// Readback in file order: a [3][Ncap] engine-order array (plus `add` of the same layout,
+// added as add + src, when given) -> N*3 rows in file order.
+__global__ void k_rows_to_file(const double *src, const double *add, uint64_t Ncap, uint64_t N,
+                               const uint32_t *file_of, double *dst) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const uint64_t f = file_of[n];
+  for (int c = 0; c < 3; ++c) {
+    const double x = src[c * Ncap + n];
+    dst[3 * f + c] = add ? add[c * Ncap + n] + x : x;
+  }
+}
+
+// The rows of the clamped nodes: zero (FP32 form's displacement after a step), or pos + the
+// predicted displacement kept for them (FP64 form's CurrPos, timeloop.h:767-774).
+__global__ void k_clamped_rows(const uint32_t *clamped, uint64_t n_clamped, const uint32_t *file_of,
+                               const double *pos, const double *cdisp, uint64_t Ncap, double *dst) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_clamped) return;
+  const uint64_t g = clamped[i], f = file_of[g];
+  for (int c = 0; c < 3; ++c) dst[3 * f + c] = cdisp ? pos[c * Ncap + g] + cdisp[3 * i + c] : 0.0;
+}
+
+void launch_rows_to_file(const double *src, const double *add, uint64_t Ncap, uint64_t N, const uint32_t *file_of,
+                         double *dst, cudaStream_t s) {
+  if (N) k_rows_to_file<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(src, add, Ncap, N, file_of, dst);
+}
+
+void launch_clamped_rows(const uint32_t *clamped, uint64_t n_clamped, const uint32_t *file_of, const double *pos,
+                         const double *cdisp, uint64_t Ncap, double *dst, cudaStream_t s) {
+  if (n_clamped)
+    k_clamped_rows<<<(unsigned)((n_clamped + 127) / 128), 128, 0, s>>>(clamped, n_clamped, file_of, pos, cdisp,
+                                                                       Ncap, dst);
+}
+
 // Number of particle pairs the pair loop evaluates (timeloop.h:641-649), for the
 // progress line's "#contacts" column.
 __global__ void k_pairwise(DevView v) {
