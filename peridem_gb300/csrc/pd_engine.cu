@@ -526,8 +526,10 @@ int Engine::upload_bonds(SellHost &h) {
 
 int Engine::alloc_and_upload() {
   const uint64_t C = Ncap_;
-  // The bond layout: built on the device from a sorted Connectivity (after the node arrays'
-  // upload, it needs node_of), else on the host beside the node arrays' staging and upload.
+  // The SELL-32 bond arrays: from a sorted Connectivity they are built on the device once the
+  // node arrays (node_of among them) are uploaded, the bond counts being computed on a host
+  // thread meanwhile; from any other Connectivity the whole build runs on a host thread beside
+  // the node arrays' staging and upload.
   SellHost sell;
   int sell_rc = PD_OK;
   auto host_build = [&] {
@@ -538,8 +540,7 @@ int Engine::alloc_and_upload() {
       sell_rc = PD_ENOMEM;
     }
   };
-  // device build: the bond counts and row starts are computed beside the node arrays' staging
-  std::vector<uint64_t> rowptr;
+  std::vector<uint64_t> rowptr;  // row starts for the device build
   int counts_rc = PD_OK;
   auto counts = [&] {
     try {
