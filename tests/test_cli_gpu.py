@@ -90,6 +90,40 @@ def test_cli_resume_equals_oracle_resume(tmp_path):
         np.testing.assert_array_equal(resumed["particles"][p]["Connectivity"], orc.connectivity(p))
 
 
+def test_cli_fp32c_resume_close_to_oracle_resume(tmp_path):
+    """The FP32-compensated form resumed from a frame with broken bonds: the saved Connectivity
+    sets the live bits and the FP32 kernels' broken flags, so the resumed run stays within the
+    form's tolerance of the oracle resumed from the same frame."""
+    g = load("impact_walls")
+    s, cfg = g["setup"], dict(g["config"])
+    out, _ = run_cli(tmp_path, s, cfg, precision="fp32c")
+    k = 2
+    fr = h5.read_frame(out, k, s.n_particles)
+    assert sum(len(p["Connectivity"]) for p in fr["particles"]) < len(s.conn), "the frame must have broken bonds"
+    rcfg = dict(cfg, do_resume=1, resume_ind=k, wall_resume=1, timesteps=cfg["modulo"])
+    O.write_conf(str(tmp_path / "main.conf"), rcfg)
+    r = subprocess.run([str(EXE), "-c", str(tmp_path / "main.conf"), "-i", str(tmp_path / "setup.h5"),
+                        "-o", str(out), "-p", "fp32c"], capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    resumed = h5.read_frame(out, k + 1, s.n_particles)
+    cur = np.concatenate([p["CurrPos"] for p in fr["particles"]])
+    w = fr["wall"]["wall_info"]
+    orc = O.Oracle(s, dict(rcfg, wall_x_min=w[0], wall_y_min=w[1], wall_z_min=w[2], wall_x_max=w[3],
+                           wall_y_max=w[4], wall_z_max=w[5]))
+    orc.set_state(disp=cur - s.pos, vel=np.concatenate([p["vel"] for p in fr["particles"]]),
+                  acc=np.concatenate([p["acc"] for p in fr["particles"]]))
+    for p in range(s.n_particles):
+        orc.set_connectivity(p, fr["particles"][p]["Connectivity"])
+    orc.step(cfg["modulo"])
+    st = orc.state()
+    got = np.concatenate([p["CurrPos"] for p in resumed["particles"]])
+    assert np.abs(got - st["curpos"]).max() <= 1e-5 * max(np.abs(st["disp"]).max(), 1e-300)
+    n_or = sum(len(orc.connectivity(p)) for p in range(s.n_particles))
+    mism = sum(len({tuple(x) for x in resumed["particles"][p]["Connectivity"]} ^
+                   {tuple(x) for x in orc.connectivity(p)}) for p in range(s.n_particles))
+    assert mism <= 1e-3 * max(1, n_or)
+
+
 def test_cli_fp32c_close_to_reference(tmp_path):
     g = load("cubes_gravity")
     s, cfg = g["setup"], g["config"]
