@@ -181,6 +181,12 @@ int pd_get_node_state(pd_sim *sim, double *curpos, double *vel, double *acc, dou
 /* applied_force_density (N*3): non-zero on the particle_w_fixed_velocity particle once the
  * velocity constraint is on (timeloop.h:760-764, saved at timeloop.h:844-848). */
 int pd_get_applied_force_density(pd_sim *sim, double *afd);
+/* Damage per node (N, file order), the field the reference's plotting derives from a saved
+ * frame (examples/3D-HPC-aggregate-particle-breakage/plot3d_timestep.py:95-105, 156-166):
+ * (bonds in the setup's Connectivity - bonds in the Connectivity pd_get_connectivity would
+ * return) / bonds in the setup's Connectivity, each pair counted at both of its nodes. A node
+ * without bonds in the setup gets NaN (0/0), as it does there. Computed on the device. */
+int pd_get_damage(pd_sim *sim, double *damage);
 /* Overwrites the kinematic state (resume from a frame, timeloop.h:262-312). */
 int pd_set_state(pd_sim *sim, const double *disp, const double *vel, const double *acc);
 /* Connectivity (local i<q pairs of live bonds) of one particle, as NbdArr2conn

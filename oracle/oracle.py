@@ -143,6 +143,28 @@ class Oracle:
         return out
 
 
+def total_neighbors(conn: np.ndarray, n: int) -> np.ndarray:
+    """Bonds per node of an (m, 2) Connectivity, each pair counted at both ends, as float64
+    (examples/3D-HPC-aggregate-particle-breakage/plot3d_timestep.py:95-105)."""
+    deg = np.zeros(n)
+    np.add.at(deg, np.asarray(conn, dtype=np.int64).ravel(), 1.0)
+    return deg
+
+
+def damage(setup, conns) -> np.ndarray:
+    """Per-node damage of all particles in file order from their current Connectivity
+    (conns[p], local pairs): (orig - now) / orig with orig from the setup's Connectivity
+    (plot3d_timestep.py:108-117 and 156-166; 0/0 gives NaN as numpy does there)."""
+    out = []
+    for p in range(setup.n_particles):
+        n = int(setup.node_offset[p + 1] - setup.node_offset[p])
+        orig = total_neighbors(setup.conn[int(setup.conn_offset[p]):int(setup.conn_offset[p + 1])], n)
+        now = total_neighbors(conns[p], n)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            out.append((orig - now) / orig)
+    return np.concatenate(out) if out else np.zeros(0)
+
+
 # ------------------------------------------------------------------------------------------
 # PeriDEM's own code (oracle/_ref), driven through its main() with an in-memory file store
 

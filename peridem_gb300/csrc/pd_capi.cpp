@@ -178,6 +178,11 @@ int pd_get_applied_force_density(pd_sim *s, double *afd) {
   return s->eng.get_afd(afd);
 }
 
+int pd_get_damage(pd_sim *s, double *damage) {
+  if (!s || !damage) return fail_global(PD_EINVAL, "null argument");
+  return s->eng.get_damage(damage);
+}
+
 int pd_get_disp(pd_sim *s, double *disp) {
   if (!s) return fail_global(PD_EINVAL, "null handle");
   return s->eng.get_state(nullptr, nullptr, nullptr, nullptr, disp);

@@ -306,6 +306,9 @@ class Engine {
   int count_live_bonds(uint64_t *live);
   // applied_force_density (N*3, file order); zeros when no particle has a prescribed velocity.
   int get_afd(double *afd);
+  // Damage per node (N, file order) as plot3d_timestep.py:156-166 derives it from a saved
+  // Connectivity: (setup bonds - live bonds) / setup bonds, NaN for a node without bonds.
+  int get_damage(double *damage);
   // ---- output frames off the critical path (pd_frames.cpp) ----
   int frame_alloc(HostFrame &f);
   void frame_free(HostFrame &f);
@@ -511,6 +514,8 @@ void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s, cudaGr
 void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
+// k_damage_count + k_damage_out: now[N] (file order) must be zeroed; out[N] in file order.
+void launch_damage(const DevView &v, uint32_t *now, double *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
 void launch_col_flags(const DevView &v, cudaStream_t s);
 void launch_rows_to_file(const double *src, const double *add, uint64_t Ncap, uint64_t N, const uint32_t *file_of,

@@ -819,4 +819,44 @@ void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s
   if (blocks) k_count_live<<<(unsigned)blocks, 256, 0, s>>>(v, out);
 }
 
+// Bonds of each node as a saved Connectivity counts them: NbdArr2conn (timeloop.h:20-44)
+// keeps the live pair (i, q) for i < q only, and total_neighbors (plot3d_timestep.py:95-105)
+// counts each kept pair at both ends. So row n adds every live partner above it in file
+// order to both n and that partner. now[] is indexed by file order and starts at zero.
+__global__ void k_damage_count(DevView v, uint32_t *now) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint64_t e0 = v.slice_ptr[n >> 5];
+  const uint32_t lane = (uint32_t)(n & 31);
+  const uint32_t fn = v.file_of[n];
+  const int dg = v.deg[n];
+  uint32_t own = 0;
+  for (int j = 0; j < dg; ++j) {
+    if (!((v.mask[(e0 >> 5) + j] >> lane) & 1u)) continue;
+    const uint32_t fq = v.file_of[v.col[e0 + 32 * (uint64_t)j + lane] & kColIndex];
+    if (fq > fn) {
+      ++own;
+      atomicAdd(&now[fq], 1u);
+    }
+  }
+  if (own) atomicAdd(&now[fn], own);
+}
+
+// damage = (orig - now) / orig per node (plot3d_timestep.py:156-166), orig being the node's
+// bond count in the setup's Connectivity (its row length); 0/0 gives NaN as it does there.
+__global__ void k_damage_out(DevView v, const uint32_t *now, double *out) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.N) return;
+  const uint32_t fn = v.file_of[n];
+  const double orig = (double)v.deg[n];
+  out[fn] = (orig - (double)now[fn]) / orig;
+}
+
+void launch_damage(const DevView &v, uint32_t *now, double *out, cudaStream_t s) {
+  const uint64_t blocks = (v.N + 255) / 256;
+  if (!blocks) return;
+  k_damage_count<<<(unsigned)blocks, 256, 0, s>>>(v, now);
+  k_damage_out<<<(unsigned)blocks, 256, 0, s>>>(v, now, out);
+}
+
 }  // namespace pdg

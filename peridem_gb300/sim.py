@@ -92,6 +92,13 @@ class Sim:
         self._ck(lib().pd_get_applied_force_density(self.h, ptr(out)))
         return out
 
+    def damage(self) -> np.ndarray:
+        """Per-node damage (N,), file order: the field plot3d_timestep.py:156-166 derives
+        from a saved Connectivity (NaN for a node without bonds in the setup)."""
+        out = np.empty(self.N)
+        self._ck(lib().pd_get_damage(self.h, ptr(out)))
+        return out
+
     def set_state(self, disp=None, vel=None, acc=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (disp, vel, acc)]
         self._ck(lib().pd_set_state(self.h, *(ptr(a) for a in arrs)))

@@ -229,3 +229,30 @@ def test_fp64_bitexact_with_unsorted_connectivity():
     sim.step(20)
     orc.step(20)
     _compare_exact("unsorted", s, sim, orc, 20)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_damage_field(precision):
+    """pd_get_damage (computed on the device) equals the plotting script's damage of the
+    Connectivity the handle returns, bit for bit; in the FP64 form that Connectivity is the
+    oracle's. Node 0 of particle 0 has every setup pair removed, so its damage is NaN (0/0)."""
+    s, cfg = cases.impact_walls(steps=40)
+    a, b = int(s.conn_offset[0]), int(s.conn_offset[1])
+    keep = np.ones(len(s.conn), dtype=bool)
+    keep[a:b] = (s.conn[a:b] != 0).all(axis=1)
+    s.conn = np.ascontiguousarray(s.conn[keep])
+    s.conn_offset = s.conn_offset - np.concatenate([[0], np.full(s.n_particles, b - a - keep[a:b].sum())]).astype(
+        s.conn_offset.dtype)
+    sim = Sim(s, cfg, precision)
+    d0 = sim.damage()
+    assert np.isnan(d0[0]) and np.isnan(d0).sum() == 1
+    np.testing.assert_array_equal(d0[1:], 0.0)
+    sim.step(40)
+    d = sim.damage()
+    conns = [sim.connectivity(p) for p in range(s.n_particles)]
+    np.testing.assert_array_equal(d, O.damage(s, conns))
+    assert np.nanmax(d) > 0, "the case must break bonds"
+    if precision == "fp64":
+        orc = O.Oracle(s, cfg)
+        orc.step(40)
+        np.testing.assert_array_equal(d, O.damage(s, [orc.connectivity(p) for p in range(s.n_particles)]))
