@@ -278,7 +278,9 @@ int pd_count_live_bonds_noalloc(pd_sim *sim, uint64_t *live);
  * particle indices). Errors of these calls are reported by pd_global_error(). */
 int pd_create_batch(const pd_setup_arrays *setups, const pd_config *cfgs, uint32_t n_sims,
                     int precision, pd_sim **out);
-/* Device bytes pd_create_batch would allocate for these setups (no device work). */
+/* Device bytes pd_create_batch would allocate for these setups (host work only: it runs
+ * without a GPU). PD_EINVAL where pd_create_batch would refuse a Connectivity index out of
+ * range. */
 int pd_estimate_bytes(const pd_setup_arrays *setups, uint32_t n_sims, int precision,
                       uint64_t *bytes);
 /* Device bytes a handle holds; free and total memory of the current device. */

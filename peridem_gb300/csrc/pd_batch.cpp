@@ -34,7 +34,7 @@ inline uint64_t atleast1(uint64_t x) { return x ? x : 1; }
 
 // Mirrors every allocation of Engine::init (alloc_and_upload, upload_bonds,
 // alloc_candidates) for the same setups, without touching the device.
-uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap) {
+uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap, int64_t *bad) {
   uint64_t N = 0, P = 0, S = sims.size(), ncl = 0;
   for (auto &s : sims) {
     N += s.node_offset[s.np];
@@ -43,7 +43,7 @@ uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision,
   }
   const uint64_t C = up32(N), nsl = C / 32;
   std::vector<uint32_t> file_of, node_of, deg_file;
-  order_nodes(sims, file_of, node_of, deg_file);
+  order_nodes(sims, file_of, node_of, deg_file, bad);
   std::vector<uint32_t> deg(C, 0);
   for (uint64_t n = 0; n < N; ++n) deg[n] = deg_file[file_of[n]];
   uint64_t E = 0;
@@ -210,7 +210,10 @@ int pd_estimate_bytes(const pd_setup_arrays *setups, uint32_t n_sims, int precis
     int rc = pdg::host_sim_from_arrays(&setups[i], &cfg, sims[i], err);
     if (rc != PD_OK) return fail(rc, "simulation " + std::to_string(i) + ": " + err);
   }
-  *bytes = pdg::Engine::estimate_bytes(sims, precision, 0);
+  int64_t bad = -1;
+  const uint64_t b = pdg::Engine::estimate_bytes(sims, precision, 0, &bad);
+  if (bad >= 0) return fail(PD_EINVAL, "Connectivity index out of range in particle " + std::to_string(bad));
+  *bytes = b;
   return PD_OK;
 }
 

@@ -333,7 +333,10 @@ class Engine {
   // Bytes of device memory this engine holds, and the same figure computed from a setup
   // before anything is allocated.
   uint64_t device_bytes() const { return device_bytes_; }
-  static uint64_t estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap);
+  // *bad (if given): a particle whose Connectivity has an index out of range, or -1 (the
+  // setups pd_create_batch would refuse).
+  static uint64_t estimate_bytes(const std::vector<HostSim> &sims, int precision, uint32_t cand_cap,
+                                 int64_t *bad = nullptr);
   // Engine node order: inside each window of kOrderWindow nodes of a particle, nodes by
   // descending bond count (stable: equal counts keep their file order). file_of[engine index] = file index, node_of = its inverse,
   // deg_file = bond count of each node in file order (indices out of range are not counted).

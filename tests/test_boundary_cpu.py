@@ -144,3 +144,23 @@ def test_h5_rejects_non_hdf5(tmp_path):
     f.write_bytes(b"not an hdf5 file at all" * 10)
     with pytest.raises(OSError):
         h5.Reader(f)
+
+
+def test_estimate_bytes_runs_on_the_host_and_checks_indices():
+    """pd_estimate_bytes is host work only (admission control calls it before any device
+    work): it sizes both forms, grows with the batch, and refuses a Connectivity index out of
+    range as pd_create_batch does."""
+    L = _capi.lib()
+    s, _ = cases.impact_walls(steps=10)
+    st, keep = _capi.setup_struct(s)
+    pair = (_capi.PdSetupArrays * 2)(st, st)
+    b1, b2 = C.c_uint64(), C.c_uint64()
+    for prec in (0, 1):
+        assert L.pd_estimate_bytes(C.byref(st), 1, prec, C.byref(b1)) == 0
+        assert L.pd_estimate_bytes(pair, 2, prec, C.byref(b2)) == 0
+        assert 0 < b1.value < b2.value
+    s.conn = s.conn.copy()
+    s.conn[5, 1] = s.n_nodes + 7
+    bad, keep2 = _capi.setup_struct(s)
+    assert L.pd_estimate_bytes(C.byref(bad), 1, 1, C.byref(b1)) == _capi.PD_EINVAL
+    assert b"out of range" in L.pd_global_error()
