@@ -300,6 +300,8 @@ int pd_get_sim_state(pd_sim *sim, uint32_t i, double *curpos, double *vel, doubl
                      double *force);
 int pd_get_sim_disp(pd_sim *sim, uint32_t i, double *disp);
 int pd_get_sim_wall(pd_sim *sim, uint32_t i, double *wall_info, double *reaction);
+/* Damage of simulation i alone (N_i, its own node order; pd_get_damage's definition). */
+int pd_get_sim_damage(pd_sim *sim, uint32_t i, double *damage);
 
 /* ---- bond lists on the GPU (setup generation) -----------------------------------------
  * For each particle p (nodes [node_offset[p], node_offset[p+1]) of pos, N*3), every node pair

@@ -102,6 +102,7 @@ SIGNATURES = [
     ("pd_get_node_state", C.c_int, [_P, _P, _P, _P, _P, _P]),
     ("pd_get_applied_force_density", C.c_int, [_P, _P]),
     ("pd_get_damage", C.c_int, [_P, _P]),
+    ("pd_get_sim_damage", C.c_int, [_P, _u32, _P]),
     ("pd_set_state", C.c_int, [_P, _P, _P, _P]),
     ("pd_get_connectivity", C.c_int, [_P, _u32, _P, _u64, C.POINTER(_u64)]),
     ("pd_get_wall", C.c_int, [_P, _P, _P]),

@@ -267,6 +267,14 @@ int pd_get_sim_disp(pd_sim *s, uint32_t sim, double *disp) {
   return s->eng.get_sim_state(sim, nullptr, nullptr, nullptr, nullptr, disp);
 }
 
+int pd_get_sim_damage(pd_sim *s, uint32_t sim, double *damage) {
+  if (!s || !damage) return fail(PD_EINVAL, "null argument");
+  uint64_t n0 = 0, nn = 0;
+  uint32_t p0 = 0, np = 0;
+  if (s->eng.sim_range(sim, &n0, &nn, &p0, &np) != PD_OK) return fail(PD_EINVAL, "simulation index out of range");
+  return s->eng.get_damage(damage, n0, nn);
+}
+
 int pd_get_sim_wall(pd_sim *s, uint32_t sim, double *wall_info, double *reaction) {
   if (!s) return fail(PD_EINVAL, "null handle");
   if (sim >= s->eng.num_sims()) return fail(PD_EINVAL, "simulation index out of range");

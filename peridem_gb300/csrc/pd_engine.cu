@@ -1455,23 +1455,28 @@ int Engine::count_live_bonds(uint64_t *live) {
   return PD_OK;
 }
 
-int Engine::get_damage(double *damage) {
-  if (!N_) return PD_OK;
+int Engine::get_damage(double *damage, uint64_t n0, uint64_t nn) {
+  if (nn == UINT64_MAX) nn = N_ - n0;
+  if (n0 > N_ || nn > N_ - n0) {
+    err = "get_damage: node range out of bounds";
+    return PD_EINVAL;
+  }
+  if (!nn) return PD_OK;
   // scratch: the file-ordered bond counts (4 B/node, padded to 8 B) and the damage field
-  const uint64_t bytes = 4 * (N_ + (N_ & 1)) + 8 * N_;
+  const uint64_t bytes = 4 * (nn + (nn & 1)) + 8 * nn;
   uint32_t *now = nullptr;
   if (cudaMallocAsync((void **)&now, bytes, stream_) != cudaSuccess) {
     cudaGetLastError();
     err = "get_damage: no device room for " + std::to_string(bytes) + " bytes of scratch";
     return PD_ENOMEM;
   }
-  double *out = reinterpret_cast<double *>(now + N_ + (N_ & 1));  // 8-byte aligned
-  cudaError_t e = cudaMemsetAsync(now, 0, 4 * N_, stream_);
+  double *out = reinterpret_cast<double *>(now + nn + (nn & 1));  // 8-byte aligned
+  cudaError_t e = cudaMemsetAsync(now, 0, 4 * nn, stream_);
   if (e == cudaSuccess) {
-    launch_damage(view(cur_), now, out, stream_);
+    launch_damage(view(cur_), n0, nn, now, out, stream_);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(damage, out, 8 * N_, cudaMemcpyDeviceToHost, stream_);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(damage, out, 8 * nn, cudaMemcpyDeviceToHost, stream_);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
   cudaFreeAsync(now, stream_);
   PD_TRY(check(e, "read damage"));

@@ -308,7 +308,8 @@ class Engine {
   int get_afd(double *afd);
   // Damage per node (N, file order) as plot3d_timestep.py:156-166 derives it from a saved
   // Connectivity: (setup bonds - live bonds) / setup bonds, NaN for a node without bonds.
-  int get_damage(double *damage);
+  // Nodes [n0, n0 + nn) only when nn is given (whole simulations of a batch).
+  int get_damage(double *damage, uint64_t n0 = 0, uint64_t nn = UINT64_MAX);
   // ---- output frames off the critical path (pd_frames.cpp) ----
   int frame_alloc(HostFrame &f);
   void frame_free(HostFrame &f);
@@ -517,8 +518,9 @@ void launch_bp_decide(const DevView &v, double half_skin, cudaStream_t s, cudaGr
 void launch_pairwise_count(const DevView &v, cudaStream_t s);
 void launch_init_lrtb(const DevView &v, cudaStream_t s);
 void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s);
-// k_damage_count + k_damage_out: now[N] (file order) must be zeroed; out[N] in file order.
-void launch_damage(const DevView &v, uint32_t *now, double *out, cudaStream_t s);
+// k_damage_count + k_damage_out over nodes [n0, n0 + nn) (whole particles): now[nn] (file
+// order - n0) must be zeroed; out[nn] in file order - n0.
+void launch_damage(const DevView &v, uint64_t n0, uint64_t nn, uint32_t *now, double *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
 void launch_col_flags(const DevView &v, cudaStream_t s);
 void launch_rows_to_file(const double *src, const double *add, uint64_t Ncap, uint64_t N, const uint32_t *file_of,

@@ -822,10 +822,12 @@ void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s
 // Bonds of each node as a saved Connectivity counts them: NbdArr2conn (timeloop.h:20-44)
 // keeps the live pair (i, q) for i < q only, and total_neighbors (plot3d_timestep.py:95-105)
 // counts each kept pair at both ends. So row n adds every live partner above it in file
-// order to both n and that partner. now[] is indexed by file order and starts at zero.
-__global__ void k_damage_count(DevView v, uint32_t *now) {
-  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N) return;
+// order to both n and that partner. Nodes [n0, n0 + nn) are whole particles (the same range
+// in engine and file order); now[] is indexed by file order - n0 and starts at zero.
+__global__ void k_damage_count(DevView v, uint64_t n0, uint64_t nn, uint32_t *now) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nn) return;
+  const uint64_t n = n0 + k;
   const uint64_t e0 = v.slice_ptr[n >> 5];
   const uint32_t lane = (uint32_t)(n & 31);
   const uint32_t fn = v.file_of[n];
@@ -836,27 +838,28 @@ __global__ void k_damage_count(DevView v, uint32_t *now) {
     const uint32_t fq = v.file_of[v.col[e0 + 32 * (uint64_t)j + lane] & kColIndex];
     if (fq > fn) {
       ++own;
-      atomicAdd(&now[fq], 1u);
+      atomicAdd(&now[fq - n0], 1u);
     }
   }
-  if (own) atomicAdd(&now[fn], own);
+  if (own) atomicAdd(&now[fn - n0], own);
 }
 
 // damage = (orig - now) / orig per node (plot3d_timestep.py:156-166), orig being the node's
 // bond count in the setup's Connectivity (its row length); 0/0 gives NaN as it does there.
-__global__ void k_damage_out(DevView v, const uint32_t *now, double *out) {
-  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N) return;
-  const uint32_t fn = v.file_of[n];
+__global__ void k_damage_out(DevView v, uint64_t n0, uint64_t nn, const uint32_t *now, double *out) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nn) return;
+  const uint64_t n = n0 + k;
+  const uint64_t f = v.file_of[n] - n0;
   const double orig = (double)v.deg[n];
-  out[fn] = (orig - (double)now[fn]) / orig;
+  out[f] = (orig - (double)now[f]) / orig;
 }
 
-void launch_damage(const DevView &v, uint32_t *now, double *out, cudaStream_t s) {
-  const uint64_t blocks = (v.N + 255) / 256;
+void launch_damage(const DevView &v, uint64_t n0, uint64_t nn, uint32_t *now, double *out, cudaStream_t s) {
+  const uint64_t blocks = (nn + 255) / 256;
   if (!blocks) return;
-  k_damage_count<<<(unsigned)blocks, 256, 0, s>>>(v, now);
-  k_damage_out<<<(unsigned)blocks, 256, 0, s>>>(v, now, out);
+  k_damage_count<<<(unsigned)blocks, 256, 0, s>>>(v, n0, nn, now);
+  k_damage_out<<<(unsigned)blocks, 256, 0, s>>>(v, n0, nn, now, out);
 }
 
 }  // namespace pdg

@@ -245,6 +245,11 @@ class Batch(Sim):
         self._ck(lib().pd_get_sim_disp(self.h, i, ptr(out["disp"])))
         return out
 
+    def sim_damage(self, i: int) -> np.ndarray:
+        out = np.empty(self.sim_range(i)[1])
+        self._ck(lib().pd_get_sim_damage(self.h, i, ptr(out)))
+        return out
+
     def sim_wall(self, i: int) -> tuple[np.ndarray, np.ndarray]:
         w = np.empty(6)
         r = np.empty((6, 3))

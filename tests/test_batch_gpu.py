@@ -1,5 +1,5 @@
 """Batches of independent simulations and the serving loop, through the C-ABI batch entry
-points (pd_create_batch, pd_finish_sim, pd_get_sim_state, ...).
+points (pd_create_batch, pd_finish_sim, pd_get_sim_state, pd_get_sim_damage, ...).
 
 A simulation inside a batch must compute exactly what it computes alone: every quantity is
 compared bit for bit with a handle of its own, in both precision forms. The serving loop
@@ -20,13 +20,13 @@ def _alone(name, precision, steps):
     s, cfg = cases.CASES[name]()
     sim = Sim(s, cfg, precision)
     sim.step(steps)
-    out = sim.state(), sim.wall(), [sim.connectivity(p) for p in range(s.n_particles)]
+    out = sim.state(), sim.wall(), [sim.connectivity(p) for p in range(s.n_particles)], sim.damage()
     sim.close()
     return out
 
 
 def _check_same(b, i, ref, name):
-    st, (w, r), conn = ref
+    st, (w, r), conn, dmg = ref
     a = b.sim_state(i)
     for k in ("curpos", "vel", "acc", "force", "disp"):
         np.testing.assert_array_equal(a[k], st[k], err_msg=f"{name} {k}")
@@ -35,6 +35,7 @@ def _check_same(b, i, ref, name):
     np.testing.assert_array_equal(rb, r)
     for p, c in enumerate(conn):
         np.testing.assert_array_equal(b.sim_connectivity(i, p), c, err_msg=f"{name} conn {p}")
+    np.testing.assert_array_equal(b.sim_damage(i), dmg, err_msg=f"{name} damage")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
@@ -86,7 +87,7 @@ def test_server_results_equal_alone():
     assert srv.used == 0 and not srv.cohorts
     for r, n, k in zip(res, names, steps):
         assert r.error is None and r.steps == k
-        st, wall, _ = _alone(n, "fp32c", k)
+        st, wall, _, _ = _alone(n, "fp32c", k)
         for key in ("curpos", "vel", "acc", "force"):
             np.testing.assert_array_equal(r.state[key], st[key], err_msg=f"request {r.rid} {key}")
         np.testing.assert_array_equal(r.wall[0], wall[0])
