@@ -55,6 +55,7 @@ class Result:
     n_nodes: int
     bonds: int          # directed bonds of the setup (the bond-update count of one step)
     error: str | None = None
+    damage: np.ndarray | None = None  # per-node damage at the last step (keep_damage)
 
     @property
     def ttc(self) -> float:
@@ -80,12 +81,14 @@ class Server:
     """Continuous-batching server over batch handles.
 
     make_batch(setups, configs, precision) -> handle with step(n, sync=False), poll(),
-    finish(i), sim_state(i), sim_wall(i), device_bytes(), close(); the default is
+    finish(i), sim_state(i), sim_wall(i), device_bytes(), close() (and sim_damage(i) with
+    keep_damage); the default is
     peridem_gb300.sim.Batch. estimate(setups, precision) -> bytes (default
     peridem_gb300.sim.estimate_bytes)."""
 
     def __init__(self, precision: str = "fp32c", capacity_bytes: int | None = None, chunk_steps: int = 500,
-                 max_batch: int = 32, keep_state: bool = True, make_batch=None, estimate=None, tune=None):
+                 max_batch: int = 32, keep_state: bool = True, make_batch=None, estimate=None, tune=None,
+                 keep_damage: bool = False):
         if make_batch is None or estimate is None:
             from . import sim as _sim
             make_batch = make_batch or _sim.Batch
@@ -100,6 +103,7 @@ class Server:
         self.chunk = int(chunk_steps)
         self.max_batch = int(max_batch)
         self.keep_state = keep_state
+        self.keep_damage = keep_damage
         self.make_batch = make_batch
         self.estimate = estimate
         self.tune = tune or {}
@@ -213,10 +217,11 @@ class Server:
                         c.batch.finish(i)
                         st = c.batch.sim_state(i) if self.keep_state else None
                         wl = c.batch.sim_wall(i) if self.keep_state else None
+                        dm = c.batch.sim_damage(i) if self.keep_damage else None
                         c.finished.append(i)
                         self.finish_s += time.perf_counter() - tf
                         results[r.rid] = Result(r.rid, st, wl, r.arrival if realtime else 0.0, c.admitted, now(),
-                                                r.steps, len(r.setup.pos), directed_bonds(r.setup))
+                                                r.steps, len(r.setup.pos), directed_bonds(r.setup), damage=dm)
                         self.log.append((tdone, "done", r.rid))
                         busy = True
                 live = [k for k in c.remaining if k > 0]

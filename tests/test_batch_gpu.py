@@ -82,12 +82,13 @@ def test_server_results_equal_alone():
     for rid, (n, k, t) in enumerate(zip(names, steps, arrivals)):
         s, cfg = cases.CASES[n]()
         reqs.append(serve.Request(rid, s, cfg, k, t))
-    srv = serve.Server("fp32c", chunk_steps=7, max_batch=3)
+    srv = serve.Server("fp32c", chunk_steps=7, max_batch=3, keep_damage=True)
     res = srv.run(reqs)
     assert srv.used == 0 and not srv.cohorts
     for r, n, k in zip(res, names, steps):
         assert r.error is None and r.steps == k
-        st, wall, _, _ = _alone(n, "fp32c", k)
+        st, wall, _, dmg = _alone(n, "fp32c", k)
+        np.testing.assert_array_equal(r.damage, dmg, err_msg=f"request {r.rid} damage")
         for key in ("curpos", "vel", "acc", "force"):
             np.testing.assert_array_equal(r.state[key], st[key], err_msg=f"request {r.rid} {key}")
         np.testing.assert_array_equal(r.wall[0], wall[0])

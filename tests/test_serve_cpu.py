@@ -39,6 +39,9 @@ class FakeBatch:
     def sim_wall(self, i):
         return (np.zeros(6), np.zeros((6, 3)))
 
+    def sim_damage(self, i):
+        return np.full(3, float(self.steps[i]))
+
     def device_bytes(self):
         return self.nb
 
@@ -127,3 +130,14 @@ def test_failed_cohort_is_retried_one_by_one():
     res = srv.run(reqs, realtime=False)
     assert all(r.error is None and r.state["steps"] == 10 for r in res)
     assert srv.max_batch == 4  # only the failed requests were retried alone
+
+
+def test_damage_is_read_only_when_asked():
+    for keep in (False, True):
+        srv = _server(10 ** 9, chunk_steps=4, keep_damage=keep)
+        res = srv.run([_req(0, 10, 9), _req(1, 20, 5)])
+        for r in res:
+            if keep:
+                np.testing.assert_array_equal(r.damage, np.full(3, float(r.steps)))
+            else:
+                assert r.damage is None
