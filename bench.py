@@ -18,7 +18,8 @@ Printed (one JSON line, rank 0):
   cpu_baseline  the CPU oracle (restatement of the reference's serial/MPI-round-robin path)
               on a bounded sample (the first 32 particles of the same packing)
   accuracy    FP32-compensated vs FP64 after the same number of steps
---impl reference times that CPU path alone on the same sample.
+--impl reference times that CPU path on the whole workload (same config; whole steps, as many
+as fit in --ref-budget seconds), with its setup built on the host cores.
 """
 from __future__ import annotations
 
@@ -388,21 +389,65 @@ def serving_run(args):
     return summ
 
 
+def workload_config(name: str, s, cfg) -> dict:
+    """The workload description both arms print as `config` (the same dict)."""
+    return {"workload": name, "particles": s.n_particles, "nodes": s.n_nodes,
+            "directed_bonds": s.n_bonds_directed, "dt": cfg["dt"],
+            "l2": f"inputs larger than L2 ({(s.n_bonds_directed * 4.125 + s.n_nodes * 224) / 1e9:.2f} GB "
+                  f"touched per step vs 0.13 GB L2)"}
+
+
 def reference_arm(args):
+    """The reference's CPU path on the same workload: the oracle (the restatement of PeriDEM's
+    step, its OpenMP threads dealt particles and particle pairs round-robin like the
+    reference's MPI ranks) on all host cores. The setup is built on the host (scipy's
+    query_pairs, the reference's own call), so this arm maps no engine library. Each timed step
+    is one whole step of the workload; a full step of the 4 M-node packing takes tens of
+    seconds, so the arm times as many of the K steps as fit in --ref-budget seconds (at least
+    one) after min(W, 1) warm-up steps and reports the rate of those."""
     r, w, _ = rank_info()
     if r != 0:
         return 0
-    s, cfg = load_workload(args.workload, particles=CPU_SAMPLE_PARTICLES)
+    from oracle import oracle as O
+    from peridem_gb300 import gen
+    gen.set_bond_builder("cpu")
+    t0 = time.perf_counter()
+    s, cfg = gen.WORKLOADS[args.workload]()
+    t_gen = time.perf_counter() - t0
     threads = os.cpu_count() or 1
-    rate, done, sub = cpu_sample_rate(s, cfg, threads, args.steps, args.warmup, budget_s=args.cpu_budget)
-    sample = (f"first {sub.n_particles} particles of {args.workload} ({sub.n_nodes} nodes, "
-              f"{sub.n_bonds_directed} directed bonds), {done} timed steps after {args.warmup} warm-up")
+    t0 = time.perf_counter()
+    orc = O.Oracle(s, cfg, threads=threads)
+    t_create = time.perf_counter() - t0
+    warm = min(args.warmup, 1)
+    if warm:
+        orc.step(warm)
+    done = bonds = 0
+    step_s = []
+    t0 = time.perf_counter()
+    while done < args.steps:
+        ts = time.perf_counter()
+        orc.step(1)
+        step_s.append(time.perf_counter() - ts)
+        bonds += orc.counts()["live_bonds"]
+        done += 1
+        if time.perf_counter() - t0 > args.ref_budget:
+            break
+    dt = time.perf_counter() - t0
+    orc.close()
+    rate = bonds / dt
+    sample = (f"the whole {args.workload} ({s.n_nodes} nodes, {s.n_bonds_directed} directed bonds): "
+              f"{done} of the {args.steps} requested steps timed after {warm} warm-up step(s), "
+              f"{dt / max(done, 1):.1f} s per step on {threads} threads"
+              + ("" if done == args.steps else f" (stopped at the {args.ref_budget:.0f} s budget; "
+                                               "the rate is per timed step)"))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": w, "steps": done,
-        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "warmup": warm, "ms_per_step": 1e3 * dt / max(done, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "sample": sample},
-        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "config": workload_config(args.workload, s, cfg),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "setup_s": {"generate": t_gen, "create": t_create},
+                         "step_s": [round(x, 3) for x in step_s]},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -542,11 +587,8 @@ def ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 bonds / f64 state", "data": "synthetic",
-        "config": {"workload": args.workload, "particles": s.n_particles, "nodes": s.n_nodes,
-                   "directed_bonds": s.n_bonds_directed, "precision": "fp32c", "dt": cfg["dt"],
-                   "l2": f"inputs larger than L2 ({(s.n_bonds_directed * 4.125 + s.n_nodes * 224) / 1e9:.2f} GB "
-                         f"touched per step vs 0.13 GB L2)",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": workload_config(args.workload, s, cfg), "precision": "fp32c",
+        "parallelism": "replicas" if world > 1 else "1 GPU",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "kernel": f"k_extra32 + k_bond32 (variant {variant})", "kernel_ms": ph[2],
@@ -574,6 +616,8 @@ def main():
     ap.add_argument("--workload", default="crush512_4m")
     ap.add_argument("--fp64-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="seconds of timed steps in --impl reference (whole steps; at least one)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -21,6 +21,8 @@ _u32, _u64 = C.c_uint32, C.c_uint64
 
 
 def _capi():
+    """The ctypes structure layouts of include/peridem_gb300.h (pure Python: importing them maps
+    no library; the oracle never loads the engine library)."""
     from peridem_gb300 import _capi
     return _capi
 
@@ -35,6 +37,7 @@ def oracle_lib() -> C.CDLL:
             raise RuntimeError(f"{ORACLE_LIB} missing: run `make -C oracle`")
         L = C.CDLL(str(ORACLE_LIB))
         capi = _capi()
+        L.or_config_default.argtypes = [C.POINTER(capi.PdConfig)]
         L.or_create.restype = _P
         L.or_create.argtypes = [C.POINTER(capi.PdSetupArrays), C.POINTER(capi.PdConfig)]
         L.or_set_threads.argtypes = [_P, C.c_int]
@@ -59,13 +62,25 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
+def default_config(**over):
+    """pd_config with ConfigVal's defaults (from the oracle library) and the given fields set."""
+    capi = _capi()
+    cfg = capi.PdConfig()
+    oracle_lib().or_config_default(C.byref(cfg))
+    for k, v in over.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, v.encode() if isinstance(v, str) else v)
+    return cfg
+
+
 class Oracle:
     """The CPU restatement, one simulation (threads=1 is the exact, serial path)."""
 
     def __init__(self, setup, config=None, threads: int = 1):
         capi = _capi()
         self.setup = setup
-        self.cfg = config if isinstance(config, capi.PdConfig) else capi.default_config(**(config or {}))
+        self.cfg = config if isinstance(config, capi.PdConfig) else default_config(**(config or {}))
         st, keep = capi.setup_struct(setup)
         L = oracle_lib()
         self.h = L.or_create(C.byref(st), C.byref(self.cfg))

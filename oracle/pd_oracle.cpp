@@ -574,6 +574,52 @@ void step_once(or_sim &S) {
 
 extern "C" {
 
+// ConfigVal's defaults: the in-class initialisers (read_config.h:36-99) and the constructor
+// (read_config.h:102-167). The oracle keeps its own copy so that its callers never need the
+// engine library.
+int or_config_default(pd_config *c) {
+  if (!c) return PD_EINVAL;
+  std::memset(c, 0, sizeof(*c));
+  c->timesteps = 8000;
+  c->modulo = 100;
+  c->dt = 0.02 / 1e5;
+  c->is_parallel = 1;
+  c->resume_ind = 50;
+  c->save_file = 1;
+  c->allow_damping = 1;
+  c->allow_friction = 1;
+  c->self_contact = 1;
+  c->self_contact_rad = -1;
+  c->cohesion_scaling = 1;
+  c->set_torque_timestep = -1;
+  c->set_fracture_timestep = -1;
+  c->set_self_contact_timestep = -1;
+  c->set_zero_wall_speed_timestep = -1;
+  c->set_damping_timestep = -1;
+  c->set_movable_index = -1;
+  c->set_movable_timestep = -1;
+  c->set_stoppable_index = -1;
+  c->set_stoppable_timestep = -1;
+  c->particle_w_fixed_velocity = -1;
+  c->set_fix_velocity_timestep = -1;
+  c->prescribed_angular_vel = -999;
+  c->prescribed_velocity_mean_x = -999;
+  c->normal_stiffness = -1;
+  c->damping_ratio = -1;
+  c->friction_coefficient = -1;
+  c->new_snot = -1;
+  c->wall_left = c->wall_right = c->wall_top = c->wall_bottom = -999;
+  c->wall_x_min = c->wall_y_min = c->wall_z_min = -999;
+  c->wall_x_max = c->wall_y_max = c->wall_z_max = -999;
+  c->brazil_reset_wall_bottom_freq = -1;
+  c->brazil_nonzero_wall_bottom_speed_freq = -1;
+  c->brazil_reset_wall_bottom_y = -999;
+  c->forcefield_scaling = 1e9;
+  std::strncpy(c->setup_filename, "data/hdf5/all.h5", sizeof(c->setup_filename) - 1);
+  std::strncpy(c->output_dir, "output/hdf5/", sizeof(c->output_dir) - 1);
+  return PD_OK;
+}
+
 or_sim *or_create(const pd_setup_arrays *su, const pd_config *cfg) {
   if (!su || !cfg || su->n_particles == 0) return nullptr;
   or_sim *S = new or_sim();

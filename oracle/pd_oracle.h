@@ -20,6 +20,8 @@ extern "C" {
 
 typedef struct or_sim or_sim;
 
+/* ConfigVal's defaults (read_config.h:36-167), the same values pd_config_default gives. */
+int or_config_default(pd_config *cfg);
 or_sim *or_create(const pd_setup_arrays *setup, const pd_config *cfg);
 void or_set_threads(or_sim *s, int threads);
 /* Runs steps t = t0+1 .. t0+nsteps (t0 = steps already taken). */

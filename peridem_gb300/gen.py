@@ -147,7 +147,9 @@ def make_particle(local: np.ndarray, h: float, mat: dict, delta_factor: float, r
     P = P + np.asarray(center, dtype=np.float64)
     delta = delta_factor * h
     m = material_3d(mat, delta)
-    conn = bonds(P, delta)
+    # without a boundary-node pass nothing here needs the bonds yet: finish() builds the
+    # pending ones of all particles at once (on all host cores with the CPU builder)
+    conn = bonds(P, delta) if Rc is not None else _PendingBonds(P, delta)
     n = len(P)
     part = dict(pos=P, vol=np.full(n, h ** 3), conn=conn, vel=np.tile(np.asarray(vel, float), (n, 1)), **m)
     part["h"] = h
@@ -157,7 +159,34 @@ def make_particle(local: np.ndarray, h: float, mat: dict, delta_factor: float, r
     return part
 
 
+class _PendingBonds:
+    """Bonds of one particle, built later by resolve_bonds."""
+
+    def __init__(self, pos: np.ndarray, delta: float):
+        self.pos, self.delta = pos, delta
+
+
+def resolve_bonds(parts: list) -> None:
+    """Builds every pending bond list of `parts` in place. The CPU builder runs the particles on
+    a thread pool (cKDTree releases the GIL while it queries); the GPU builder takes all of
+    them in one pd_query_pairs call. The pairs are those bonds() gives one particle at a time."""
+    idx = [i for i, p in enumerate(parts) if isinstance(p.get("conn"), _PendingBonds)]
+    if not idx:
+        return
+    jobs = [parts[i]["conn"] for i in idx]
+    if _BOND_BUILDER == "gpu":
+        out = bonds_gpu([j.pos for j in jobs], [j.delta for j in jobs])
+    else:
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=max(1, min(32, os.cpu_count() or 1))) as ex:
+            out = list(ex.map(lambda j: bonds(j.pos, j.delta), jobs))
+    for i, c in zip(idx, out):
+        parts[i]["conn"] = c
+
+
 def finish(parts, Rc, dt, zeta=0.8, mu=0.3, wall=None, kn=None) -> Setup:
+    resolve_bonds(parts)
     vol_max = max(float(np.max(p["vol"])) for p in parts)
     rho_min = min(p["rho"] for p in parts)
     Kn = kn if kn is not None else stable_kn(kn_rule(Rc), rho_min, vol_max, dt)
