@@ -18,7 +18,10 @@ How it works:
   * completion: at a chunk boundary the members that reached their step count are finished
     (state read back, kept for the caller, their nodes skipped from then on); a cohort whose
     members are all finished is closed and its memory returns to the budget, which admits
-    the next waiting requests.
+    the next waiting requests;
+  * failures: a cohort whose handle reports an error (a device error word, a failed read) is
+    closed and its memory returned; its unfinished members are queued again, each alone, and a
+    member that fails alone gets the error as its result. Other cohorts are not affected.
 Each result is what the same simulation computes alone: nothing in a step couples two
 simulations of a batch (the tests check this bit for bit).
 """
@@ -112,7 +115,7 @@ class Server:
         self.cohorts: list[_Cohort] = []
         self.log: list[tuple] = []   # (time, event, detail)
         self.create_s: list[float] = []  # host+device time to build each cohort's handle
-        self._solo: set = set()          # requests to admit alone (their cohort failed to build)
+        self._solo: set = set()          # requests to admit alone (their cohort failed)
         self.finish_s = 0.0              # time spent reading finished simulations back
 
     # -- admission ------------------------------------------------------------------------
@@ -143,6 +146,62 @@ class Server:
         except Exception as e:  # reported per request
             out["error"] = str(e)
         out["create_s"] = time.perf_counter() - t0
+
+    # -- one cohort -----------------------------------------------------------------------
+    def _advance(self, c: _Cohort, results: dict, now, realtime: bool) -> bool:
+        """Reads back the members that reached their step count, closes the cohort when none is
+        left, else enqueues its next chunk. Returns whether anything happened."""
+        if not c.batch.poll():
+            return False
+        tdone = now()
+        for i, r in enumerate(c.members):
+            if c.remaining[i] == 0 and i not in c.finished:
+                tf = time.perf_counter()
+                c.batch.finish(i)
+                st = c.batch.sim_state(i) if self.keep_state else None
+                wl = c.batch.sim_wall(i) if self.keep_state else None
+                dm = c.batch.sim_damage(i) if self.keep_damage else None
+                c.finished.append(i)
+                self.finish_s += time.perf_counter() - tf
+                results[r.rid] = Result(r.rid, st, wl, r.arrival if realtime else 0.0, c.admitted, now(),
+                                        r.steps, len(r.setup.pos), directed_bonds(r.setup), damage=dm)
+                self.log.append((tdone, "done", r.rid))
+        live = [k for k in c.remaining if k > 0]
+        if not live:
+            c.batch.close()
+            self.used -= c.nbytes
+            self.cohorts.remove(c)
+            self.log.append((now(), "close", [r.rid for r in c.members]))
+            return True
+        k = min(self.chunk, min(live))
+        c.batch.step(k, sync=False)
+        c.remaining = [max(0, x - k) if x > 0 else 0 for x in c.remaining]
+        return True
+
+    def _fail(self, c: _Cohort, err: Exception, waiting: deque, results: dict, now, realtime: bool) -> None:
+        """A cohort whose handle reported an error (the device error word is per handle, so the
+        member that raised it is unknown): the handle is closed and its bytes returned; each
+        unfinished member runs again alone from its setup, and one that was already alone gets
+        the error as its result. The other cohorts go on."""
+        try:
+            c.batch.close()
+        except Exception:
+            pass
+        self.used -= c.nbytes
+        self.cohorts.remove(c)
+        self.log.append((now(), "fail", [r.rid for r in c.members], str(err)))
+        again = []
+        for i, r in enumerate(c.members):
+            if i in c.finished or r.rid in results:
+                continue
+            if len(c.members) == 1 or r.rid in self._solo:
+                results[r.rid] = Result(r.rid, None, None, r.arrival if realtime else 0.0, c.admitted, now(), 0,
+                                        len(r.setup.pos), directed_bonds(r.setup), error=str(err))
+            else:
+                self._solo.add(r.rid)
+                again.append(r)
+        for r in reversed(again):
+            waiting.appendleft(r)
 
     # -- main loop ------------------------------------------------------------------------
     def run(self, requests: list[Request], realtime: bool = True, idle_sleep: float = 2e-4) -> list[Result]:
@@ -208,34 +267,11 @@ class Server:
                     busy = True
             # advance cohorts
             for c in list(self.cohorts):
-                if not c.batch.poll():
-                    continue
-                tdone = now()
-                for i, r in enumerate(c.members):
-                    if c.remaining[i] == 0 and i not in c.finished:
-                        tf = time.perf_counter()
-                        c.batch.finish(i)
-                        st = c.batch.sim_state(i) if self.keep_state else None
-                        wl = c.batch.sim_wall(i) if self.keep_state else None
-                        dm = c.batch.sim_damage(i) if self.keep_damage else None
-                        c.finished.append(i)
-                        self.finish_s += time.perf_counter() - tf
-                        results[r.rid] = Result(r.rid, st, wl, r.arrival if realtime else 0.0, c.admitted, now(),
-                                                r.steps, len(r.setup.pos), directed_bonds(r.setup), damage=dm)
-                        self.log.append((tdone, "done", r.rid))
-                        busy = True
-                live = [k for k in c.remaining if k > 0]
-                if not live:
-                    c.batch.close()
-                    self.used -= c.nbytes
-                    self.cohorts.remove(c)
-                    self.log.append((now(), "close", [r.rid for r in c.members]))
+                try:
+                    busy |= self._advance(c, results, now, realtime)
+                except Exception as e:  # a device error of this handle (PdError), a failed read
+                    self._fail(c, e, waiting, results, now, realtime)
                     busy = True
-                    continue
-                k = min(self.chunk, min(live))
-                c.batch.step(k, sync=False)
-                c.remaining = [max(0, x - k) if x > 0 else 0 for x in c.remaining]
-                busy = True
             if not busy:
                 if realtime and not waiting and not self.cohorts and admit is None and nxt < len(reqs):
                     time.sleep(max(0.0, min(reqs[nxt].arrival - now(), 0.01)))

@@ -141,3 +141,63 @@ def test_damage_is_read_only_when_asked():
                 np.testing.assert_array_equal(r.damage, np.full(3, float(r.steps)))
             else:
                 assert r.damage is None
+
+
+class FailingBatch(FakeBatch):
+    """A fake handle whose device error word is raised by poll() once any member listed in
+    `bad` is in it and `after` chunks have run (as Batch.poll raises PdError on PD_EDEVICE)."""
+    bad: set = set()
+    after = 1
+
+    def __init__(self, setups, configs, precision):
+        super().__init__(setups, configs, precision)
+        self.rids = [c["rid"] for c in configs]
+        self.chunks = 0
+
+    def step(self, k, sync=True):
+        super().step(k, sync)
+        self.chunks += 1
+
+    def poll(self):
+        if self.chunks >= FailingBatch.after and FailingBatch.bad & set(self.rids):
+            raise RuntimeError("[-6] device error word: non-finite force density")
+        return True
+
+
+def _failing_server(capacity, bad, **kw):
+    FakeBatch.instances.clear()
+    FailingBatch.bad = set(bad)
+    return serve.Server("fp32c", capacity_bytes=capacity, make_batch=FailingBatch, estimate=fake_estimate, **kw)
+
+
+def _req_rid(rid, nodes, steps, arrival=0.0):
+    r = _req(rid, nodes, steps, arrival)
+    r.config = dict(r.config, rid=rid)
+    return r
+
+
+def test_a_failing_cohort_does_not_stop_the_others():
+    """Member 2 makes its handle raise: its cohort is closed and its bytes returned; the other
+    members of that cohort run again alone and complete; only member 2 gets the error; the
+    other cohort is not affected."""
+    reqs = [_req_rid(i, 100, 120) for i in range(6)]
+    srv = _failing_server(10 ** 9, bad={2}, chunk_steps=50, max_batch=3)
+    res = srv.run(reqs, realtime=False)
+    errs = {r.rid: r.error for r in res}
+    assert errs[2] is not None and "non-finite" in errs[2]
+    for i in (0, 1, 3, 4, 5):
+        assert errs[i] is None, (i, errs[i])
+        assert res[i].state["steps"] == 120
+    assert srv.used == 0
+    assert all(b.closed for b in FakeBatch.instances)
+    fails = [e for e in srv.log if e[1] == "fail"]
+    assert len(fails) == 2  # the cohort of three, then member 2 alone
+    assert sorted(fails[0][2]) == [0, 1, 2] and fails[1][2] == [2]
+
+
+def test_a_failing_request_alone_reports_its_error():
+    reqs = [_req_rid(0, 100, 80)]
+    srv = _failing_server(10 ** 9, bad={0}, chunk_steps=50, max_batch=4)
+    res = srv.run(reqs, realtime=False)
+    assert res[0].error is not None and res[0].state is None
+    assert srv.used == 0 and not srv.cohorts
