@@ -622,7 +622,6 @@ int Engine::alloc_and_upload() {
       P.stoppable = s.stoppable[p];
       P.break_bonds = 1;  // simulate3d.cpp:137-139
       P.has_ext = part_ext[gp];
-      P.cnot32 = (float)P.cnot;
       P.snot_lo32 = (float)(P.snot * (1.0 - 1e-4));
       P.snot_hi32 = (float)(P.snot * (1.0 + 1e-4));
       if (P.n == 0) {
@@ -848,8 +847,10 @@ int Engine::alloc_and_upload() {
         r.u = make_float4(0.f, 0.f, 0.f, 0.f);
         if (g < N_) {
           const DevPart &P = parts[h_pid_[g]];
+          // the bond kernels' force coefficient of this node as a partner: cnot * volume (a
+          // bond's partner is in the same particle)
           r.p = make_float4((float)(pos[g] - P.anchor_pos[0]), (float)(pos[C + g] - P.anchor_pos[1]),
-                            (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)vol[g]);
+                            (float)(pos[2 * C + g] - P.anchor_pos[2]), (float)(P.cnot * vol[g]));
         } else {
           r.p = make_float4(0.f, 0.f, 0.f, 0.f);
         }

@@ -22,7 +22,7 @@
 //   * FP64 form only: per-entry constants xi = pos[q]-pos[i] (3 doubles), |xi| and the
 //     correctly rounded reciprocal of |xi| (gen_xi, particle2.h:241-257);
 //   * FP32-compensated form only: a 32-byte record per node, float4 (local position,
-//     volume) + float4 (local displacement), double-buffered; local = relative to the
+//     cnot * volume) + float4 (local displacement), double-buffered; local = relative to the
 //     particle's anchor node;
 //   * contact broad phase: hashed cell list (counting sort) rebuilt only when the nodes may
 //     have moved more than half the skin since the last build; per-node candidate lists
@@ -77,7 +77,7 @@ struct DevPart {
   int32_t movable, breakable, stoppable, break_bonds;
   double anchor_pos[3];  // FP32 form: position of the anchor node
   int32_t has_ext;       // any non-zero extforce in this particle
-  float cnot32, snot_lo32, snot_hi32;  // FP32 form: cnot and the band around snot
+  float snot_lo32, snot_hi32;  // FP32 form: the band around snot
 };
 
 // Per-simulation constants (Contact, RectWall and Timeloop fields after apply_config).
@@ -130,7 +130,8 @@ struct DevCounters {
 };
 
 // FP32 form: one 32-byte record per node, so that a bond gathers its partner with a single
-// 256-bit load: p = (anchor-relative position, volume), u = (anchor-relative displacement, 0).
+// 256-bit load: p = (anchor-relative position, cnot * volume), u = (anchor-relative
+// displacement, 0).
 struct __align__(32) Rec32 {
   float4 p, u;
 };

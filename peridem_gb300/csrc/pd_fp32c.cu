@@ -228,10 +228,44 @@ __device__ __noinline__ void band_check(const DevView &v, uint64_t n, uint32_t q
   }
 }
 
-// One bond in FP32: cancellation-free stretch and Kahan-compensated accumulation.
+// A column entry: read once per step, so it is not allocated in L1, which is left to the
+// partner records (the bond kernel's working set).
+__device__ __forceinline__ uint32_t ld_col(const uint32_t *p) {
+  uint32_t r;
+  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
+  return r;
+}
+
+// A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector.
+template <int W>
+__device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
+  if (W) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(u.x), "=f"(u.y), "=f"(u.z), "=f"(u.w)
+        : "l"(r));
+  } else {
+    p = __ldg(&r->p);
+    u = __ldg(&r->u);
+  }
+}
+
+// Kahan-compensated FP32 accumulator of a node's bond force density.
 struct Acc32 {
   float sx, sy, sz, cx, cy, cz;
 };
+
+// Approximate reciprocal square root and reciprocal (one special-function instruction each;
+// subnormal inputs flush to zero, which never occurs for squared bond lengths).
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 // The terms of one bond in FP32: cancellation-free stretch and the force coefficient g, so
 // that the bond adds g * (xi + eta) to the node's force density.
@@ -239,8 +273,13 @@ struct BondTerms {
   float g, yx, yy, yz, str;
 };
 
+// xi = pq - pi (reference positions), eta = uq - ui (displacements), y = xi + eta. The stretch
+// (particle2.h:139-149) s = (|y| - |xi|) / |xi| is formed as (|y|^2 - |xi|^2) / ((|y| + |xi|) |xi|)
+// with |y|^2 - |xi|^2 = 2 xi.eta + eta.eta = eta.(xi + y), which has no cancellation; the force
+// density term is cnot V_q s y / |y| (particle2.h:151-157), and the record's fourth float holds
+// cnot V_q.
 __device__ __forceinline__ BondTerms bond32_terms(const float4 &pi, const float4 &ui, const float4 &pq,
-                                                  const float4 &uq, float cn) {
+                                                  const float4 &uq) {
   const float xx = pq.x - pi.x, xy = pq.y - pi.y, xz = pq.z - pi.z;
   const float ex = uq.x - ui.x, ey = uq.y - ui.y, ez = uq.z - ui.z;
   BondTerms b;
@@ -249,14 +288,10 @@ __device__ __forceinline__ BondTerms bond32_terms(const float4 &pi, const float4
   b.yz = xz + ez;
   const float x2 = fmaf(xx, xx, fmaf(xy, xy, xz * xz));
   const float y2 = fmaf(b.yx, b.yx, fmaf(b.yy, b.yy, b.yz * b.yz));
-  // |xi| and |xi+eta| from the hardware reciprocal square root (relative error ~1e-7; the
-  // breaking decision near snot is re-taken in FP64)
-  const float rx = rsqrtf(x2), ry = rsqrtf(y2);
-  const float xin = x2 * rx, yn = y2 * ry;
-  const float xe = fmaf(xx, ex, fmaf(xy, ey, xz * ez));
-  const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-  b.str = __fdividef(fmaf(2.f, xe, ee), (yn + xin) * xin);
-  b.g = cn * b.str * pq.w * ry;
+  const float num = fmaf(ex, xx + b.yx, fmaf(ey, xy + b.yy, ez * (xz + b.yz)));
+  const float rx = rsqrt_approx(x2), ry = rsqrt_approx(y2);
+  b.str = (num * rx) * rcp_approx(fmaf(x2, rx, y2 * ry));
+  b.g = (b.str * ry) * pq.w;
   return b;
 }
 
@@ -268,11 +303,46 @@ __device__ __forceinline__ void kahan_add(Acc32 &a, float g, float yx, float yy,
   y = fmaf(g, yz, -a.cz); t = a.sz + y; a.cz = (t - a.sz) - y; a.sz = t;
 }
 
-__device__ __forceinline__ float bond32(const float4 &pi, const float4 &ui, const float4 &pq, const float4 &uq,
-                                        float cn, Acc32 &a) {
-  const BondTerms b = bond32_terms(pi, ui, pq, uq, cn);
-  kahan_add(a, b.g, b.yx, b.yy, b.yz);
-  return b.str;
+// One load group of U positions of a node's row: the partner records are gathered, every
+// position's terms evaluated (a broken or missing bond's are discarded), the live ones summed in
+// position order, and -- once per group, only when some live stretch exceeds the lower edge of
+// the band around snot -- the breaking decisions taken (FP32 above the band, FP64 inside it).
+template <int U, int W>
+__device__ __forceinline__ void bond_group(const DevView &v, uint64_t nn, const Rec32 *__restrict__ rec,
+                                           const float4 &pi4, const float4 &ui4, const uint32_t (&q)[U], Acc32 &a,
+                                           bool brk, float slo, float shi, double snot, uint32_t *maskp,
+                                           uint32_t *colw, uint32_t lane) {
+  float4 pq[U], uq[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
+  BondTerms bt[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u]);
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (!(q[u] & kColBroken)) kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
+  if (brk) {
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < U; ++u) any |= !(q[u] & kColBroken) && bt[u].str > slo;
+    if (any) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!(q[u] & kColBroken) && bt[u].str > slo) {
+          if (bt[u].str > shi) cut_bond(&maskp[u], lane, colw + 32 * u, q[u]);
+          else band_check(v, nn, q[u], &maskp[u], lane, snot, colw + 32 * u);
+        }
+      }
+    }
+  }
+}
+
+// Live bonds of a row at the start of the step (statistics only: a second read of the row's
+// column entries, outside the bond loop).
+__device__ __noinline__ uint32_t row_live(const uint32_t *colp, int dg) {
+  uint32_t live = 0;
+  for (int j = 0; j < dg; ++j) live += !(colp[32 * j] & kColBroken);
+  return live;
 }
 
 // Per-node end of the FP32-form step, given the total force density f: force store,
@@ -353,27 +423,6 @@ __device__ __forceinline__ void verlet_tail(const DevView &v, uint64_t nn, uint3
   }
 }
 
-// A column entry: read once per step, so it is not allocated in L1, which is left to the
-// partner records (the bond kernel's working set).
-__device__ __forceinline__ uint32_t ld_col(const uint32_t *p) {
-  uint32_t r;
-  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
-  return r;
-}
-
-// A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector.
-template <int W>
-__device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
-  if (W) {
-    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(u.x), "=f"(u.y), "=f"(u.z), "=f"(u.w)
-        : "l"(r));
-  } else {
-    p = __ldg(&r->p);
-    u = __ldg(&r->u);
-  }
-}
-
 // U: positions whose loads are issued together; MINB: minimum resident blocks per SM (register
 // cap); W: 256-bit record loads; PF: the column entries (index + broken flag) of the next PF
 // groups are loaded ahead of this group's partner records, so that the column stream's latency
@@ -401,8 +450,9 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     uint32_t *maskp = v.mask + (sbase >> 5);
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
-    const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
+    const float slo = P.snot_lo32, shi = P.snot_hi32;
     const Rec32 *__restrict__ rec = v.rec;
+    if (v.stats) live = row_live(colp, dg);
     int j = 0;
     // column entries (index + broken flag) of the next PF groups, loaded ahead (static
     // indices only, so that the ring stays in registers)
@@ -432,47 +482,13 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
 #pragma unroll
         for (int u = 0; u < U; ++u) q[u] = ld_col(colp + 32 * (j + u));
       }
-      float4 pq[U], uq[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
-      // the group's bond terms are evaluated unconditionally (a broken bond's are discarded),
-      // so that the independent bonds' arithmetic interleaves; the sums take live ones in order
-      BondTerms bt[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (!(q[u] & kColBroken)) {
-          ++live;
-          kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
-          if (brk && bt[u].str > slo) {
-            if (bt[u].str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
-            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
-          }
-        }
-      }
+      bond_group<U, W>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
     }
     if (j < dg) {  // the row's last dg - j < U positions as one group; missing ones count as broken
       uint32_t q[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? ld_col(colp + 32 * (j + u)) : kColBroken;
-      float4 pq[U], uq[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
-      BondTerms bt[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (!(q[u] & kColBroken)) {
-          ++live;
-          kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
-          if (brk && bt[u].str > slo) {
-            if (bt[u].str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
-            else band_check(v, nn, q[u], &maskp[j + u], lane, P.snot, colw + 32 * (j + u));
-          }
-        }
-      }
+      bond_group<U, W>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
     }
   }
   D3 f = d3(0.0, 0.0, 0.0);
@@ -557,8 +573,9 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
     uint32_t *maskp = v.mask + (sbase >> 5);
     const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
-    const float cn = P.cnot32, slo = P.snot_lo32, shi = P.snot_hi32;
+    const float slo = P.snot_lo32, shi = P.snot_hi32;
     const Rec32 *__restrict__ rec = v.rec;
+    if (v.stats) live = row_live(colp, dg);
     // partner record: shared memory when staged (and inside the staged range), else global
     auto partner = [&](uint32_t q, float4 &p, float4 &u) {
       const uint32_t o = q - wlo;
@@ -596,11 +613,10 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
       for (int u = 0; u < U; ++u) partner(q[u] & kColIndex, pq[u], uq[u]);
       BondTerms bt[U];  // as in bond_node: terms unconditionally, live ones summed in order
 #pragma unroll
-      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u], cn);
+      for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (!(q[u] & kColBroken)) {
-          ++live;
           kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
           if (brk && bt[u].str > slo) {
             if (bt[u].str > shi) cut_bond(&maskp[j + u], lane, colw + 32 * (j + u), q[u]);
@@ -612,10 +628,11 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
     for (; j < dg; ++j) {
       const uint32_t q = __ldg(colp + 32 * j);
       if (q & kColBroken) continue;
-      ++live;
       float4 pq, uq;
       partner(q, pq, uq);
-      const float str = bond32(pi4, ui4, pq, uq, cn, a);
+      const BondTerms b = bond32_terms(pi4, ui4, pq, uq);
+      kahan_add(a, b.g, b.yx, b.yy, b.yz);
+      const float str = b.str;
       if (brk && str > slo) {
         if (str > shi) cut_bond(&maskp[j], lane, colw + 32 * j, q);
         else band_check(v, nn, q, &maskp[j], lane, P.snot, colw + 32 * j);
