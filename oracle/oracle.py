@@ -41,6 +41,7 @@ def oracle_lib() -> C.CDLL:
         L.or_create.restype = _P
         L.or_create.argtypes = [C.POINTER(capi.PdSetupArrays), C.POINTER(capi.PdConfig)]
         L.or_set_threads.argtypes = [_P, C.c_int]
+        L.or_set_cell_search.argtypes = [_P, C.c_int]
         L.or_step.argtypes = [_P, _u32]
         L.or_get_state.argtypes = [_P, _P, _P, _P, _P]
         L.or_get_disp.argtypes = [_P, _P]
@@ -75,9 +76,11 @@ def default_config(**over):
 
 
 class Oracle:
-    """The CPU restatement, one simulation (threads=1 is the exact, serial path)."""
+    """The CPU restatement, one simulation (threads=1 is the exact, serial path). cell_search:
+    contact visits only the node pairs within reach, in the reference's order (the same sums,
+    bit for bit; for large cases, whose brute-force contact loops would take minutes)."""
 
-    def __init__(self, setup, config=None, threads: int = 1):
+    def __init__(self, setup, config=None, threads: int = 1, cell_search: bool = False):
         capi = _capi()
         self.setup = setup
         self.cfg = config if isinstance(config, capi.PdConfig) else default_config(**(config or {}))
@@ -91,6 +94,8 @@ class Oracle:
         self.P = setup.n_particles
         if threads != 1:
             L.or_set_threads(self.h, int(threads))
+        if cell_search:
+            L.or_set_cell_search(self.h, 1)
 
     def close(self):
         if getattr(self, "h", None):

@@ -58,6 +58,7 @@ struct Part {
 struct Contact {
   double Rc, Kn, zeta, mu;
   int allow_damping, allow_friction, nl_bdry_only, self_contact, compute_wall_reaction;
+  int cell_search = 0;  // visit only node pairs in neighbouring cells (see contact_force)
 };
 
 struct Wall {
@@ -193,78 +194,126 @@ void remove_bonds(Part &p) {
   }
 }
 
-// update_contact_force_by_boundary<3> (contact.h:744-942).
+// update_contact_force_by_boundary<3> (contact.h:744-942). `pair` is the loop body for node
+// i of C and node j of N; the reference visits every (i, j), i outer, both ascending in the
+// iteration lists. With cn.cell_search the same pairs are visited in the same order, but only
+// those whose current positions lie in neighbouring cells of edge > Rc: every other pair fails
+// the first test (|dir| <= Rc), so the sums are bit-identical and the cost follows the pairs in
+// reach instead of nC * nN (the checker of large cases; timing runs use the plain loops).
 uint64_t contact_force(const Part &C, const Part &N, const Contact &cn, double dt,
                        std::vector<V3> &gf, bool self) {
   uint64_t contacts = 0;
   uint32_t tn_i = cn.nl_bdry_only ? (uint32_t)C.bdry.size() : C.n;
   uint32_t tn_j = cn.nl_bdry_only ? (uint32_t)N.bdry.size() : N.n;
-  for (uint32_t pp = 0; pp < tn_i; ++pp) {
-    uint32_t i = cn.nl_bdry_only ? C.bdry[pp] : pp;
-    for (uint32_t qq = 0; qq < tn_j; ++qq) {
-      uint32_t j = cn.nl_bdry_only ? N.bdry[qq] : qq;
-      V3 xi_ij = vsub(N.pos[j], C.pos[i]);
-      V3 dir = vadd(vsub(N.disp[j], C.disp[i]), xi_ij);
-      double dn = vnorm(dir);
-      if (!(dn <= cn.Rc)) continue;
-      bool do_compute = true;
-      double xin = vnorm(xi_ij);
-      double len_ref = cn.Rc;
-      double sc = cn.Kn * cn.Rc;
-      if (self) {
-        if (i == j) {
-          do_compute = false;
-        } else if (std::find(C.nbr[i].begin(), C.nbr[i].end(), j) != C.nbr[i].end()) {
-          do_compute = false;
-        } else if (xin < cn.Rc) {
-          len_ref = xin;
-          sc = N.cnot;
-        } else {
-          len_ref = cn.Rc;
-        }
+  auto pair = [&](uint32_t i, uint32_t j) {
+    V3 xi_ij = vsub(N.pos[j], C.pos[i]);
+    V3 dir = vadd(vsub(N.disp[j], C.disp[i]), xi_ij);
+    double dn = vnorm(dir);
+    if (!(dn <= cn.Rc)) return;
+    bool do_compute = true;
+    double xin = vnorm(xi_ij);
+    double len_ref = cn.Rc;
+    double sc = cn.Kn * cn.Rc;
+    if (self) {
+      if (i == j) {
+        do_compute = false;
+      } else if (std::find(C.nbr[i].begin(), C.nbr[i].end(), j) != C.nbr[i].end()) {
+        do_compute = false;
+      } else if (xin < cn.Rc) {
+        len_ref = xin;
+        sc = N.cnot;
+      } else {
+        len_ref = cn.Rc;
       }
-      if (!(do_compute && (dn < len_ref))) continue;
-      ++contacts;
-      double N_vol = N.vol[j];
-      V3 unit = vdiv(dir, dn);
-      double s = (dn - len_ref) / len_ref;
-      double fmag = (sc * s) * N_vol;
-      V3 fc = vscale(fmag, unit);
-      double fcn = vnorm(fc);
-      uint32_t gi = C.g0 + i, gj = N.g0 + j;
-      if (C.stoppable) vacc(gf[gi], fc);
+    }
+    if (!(do_compute && (dn < len_ref))) return;
+    ++contacts;
+    double N_vol = N.vol[j];
+    V3 unit = vdiv(dir, dn);
+    double s = (dn - len_ref) / len_ref;
+    double fmag = (sc * s) * N_vol;
+    V3 fc = vscale(fmag, unit);
+    double fcn = vnorm(fc);
+    uint32_t gi = C.g0 + i, gj = N.g0 + j;
+    if (C.stoppable) vacc(gf[gi], fc);
+    if (!self && N.stoppable) {
+      double cv = C.vol[i];
+      for (int k = 0; k < 3; ++k) gf[gj].c[k] -= (fc.c[k] / N_vol) * cv;
+    }
+    if (cn.allow_damping) {
+      V3 rel = vsub(C.vel[i], N.vel[j]);
+      double rvp = vdot(rel, unit);
+      V3 rvn = vscale(rvp, unit);
+      double dc = ((2.0 * cn.zeta) * std::sqrt(sc * C.rho)) * std::sqrt(N_vol);
+      V3 fd = vscale(-dc, rvn);
+      if (C.stoppable) vacc(gf[gi], fd);
       if (!self && N.stoppable) {
-        double cv = C.vol[i];
-        for (int k = 0; k < 3; ++k) gf[gj].c[k] -= (fc.c[k] / N_vol) * cv;
+        double sn = std::sqrt(N_vol), sv = std::sqrt(C.vol[i]);
+        for (int k = 0; k < 3; ++k) gf[gj].c[k] -= (fd.c[k] / sn) * sv;
       }
-      if (cn.allow_damping) {
-        V3 rel = vsub(C.vel[i], N.vel[j]);
-        double rvp = vdot(rel, unit);
-        V3 rvn = vscale(rvp, unit);
-        double dc = ((2.0 * cn.zeta) * std::sqrt(sc * C.rho)) * std::sqrt(N_vol);
-        V3 fd = vscale(-dc, rvn);
-        if (C.stoppable) vacc(gf[gi], fd);
+    }
+    if (cn.allow_friction) {
+      V3 rel = vsub(C.vel[i], N.vel[j]);
+      double rd = vdot(rel, unit);
+      V3 rvt = vsub(rel, vscale(rd, unit));
+      double rvtn = vnorm(rvt);
+      if (rvtn > 0) {
+        V3 tu = vdiv(rvt, vnorm(rvt));
+        V3 ff = vscale((-cn.mu) * fcn, tu);
+        if (rvtn < ((cn.mu * fcn) * dt) / C.rho) ff = vscale(((-rvtn) / C.rho) / dt, tu);
+        if (C.stoppable) vacc(gf[gi], ff);
         if (!self && N.stoppable) {
-          double sn = std::sqrt(N_vol), sv = std::sqrt(C.vol[i]);
-          for (int k = 0; k < 3; ++k) gf[gj].c[k] -= (fd.c[k] / sn) * sv;
-        }
-      }
-      if (cn.allow_friction) {
-        V3 rel = vsub(C.vel[i], N.vel[j]);
-        double rd = vdot(rel, unit);
-        V3 rvt = vsub(rel, vscale(rd, unit));
-        double rvtn = vnorm(rvt);
-        if (rvtn > 0) {
-          V3 tu = vdiv(rvt, vnorm(rvt));
-          V3 ff = vscale((-cn.mu) * fcn, tu);
-          if (rvtn < ((cn.mu * fcn) * dt) / C.rho) ff = vscale(((-rvtn) / C.rho) / dt, tu);
-          if (C.stoppable) vacc(gf[gi], ff);
-          if (!self && N.stoppable) {
-            for (int k = 0; k < 3; ++k) gf[gj].c[k] -= ff.c[k];
-          }
+          for (int k = 0; k < 3; ++k) gf[gj].c[k] -= ff.c[k];
         }
       }
     }
+  };
+  if (!cn.cell_search || (uint64_t)tn_i * tn_j <= 4096) {
+    for (uint32_t pp = 0; pp < tn_i; ++pp) {
+      uint32_t i = cn.nl_bdry_only ? C.bdry[pp] : pp;
+      for (uint32_t qq = 0; qq < tn_j; ++qq) pair(i, cn.nl_bdry_only ? N.bdry[qq] : qq);
+    }
+    return contacts;
+  }
+  // cells of edge h > Rc over N's iterated nodes (current positions pos + disp); a pair with
+  // |dir| <= Rc has |cur_j - cur_i| <= Rc up to rounding (1e-15 relative), so it lies in
+  // neighbouring cells
+  const double h = cn.Rc * 1.001;
+  double lo[3] = {INFINITY, INFINITY, INFINITY};
+  for (uint32_t qq = 0; qq < tn_j; ++qq) {
+    const V3 &x = N.cur[cn.nl_bdry_only ? N.bdry[qq] : qq];
+    for (int c = 0; c < 3; ++c) lo[c] = std::min(lo[c], x.c[c]);
+  }
+  auto cell = [&](const V3 &x, int64_t *k) {
+    for (int c = 0; c < 3; ++c) k[c] = (int64_t)std::floor((x.c[c] - lo[c]) / h);
+  };
+  auto key = [](int64_t a, int64_t b, int64_t c) {
+    return ((uint64_t)(a + (1 << 20)) << 42) | ((uint64_t)(b + (1 << 20)) << 21) | (uint64_t)(c + (1 << 20));
+  };
+  std::vector<std::pair<uint64_t, uint32_t>> grid(tn_j);
+  for (uint32_t qq = 0; qq < tn_j; ++qq) {
+    int64_t k[3];
+    cell(N.cur[cn.nl_bdry_only ? N.bdry[qq] : qq], k);
+    grid[qq] = {key(k[0], k[1], k[2]), qq};
+  }
+  std::sort(grid.begin(), grid.end());
+  std::vector<uint32_t> cand;
+  for (uint32_t pp = 0; pp < tn_i; ++pp) {
+    uint32_t i = cn.nl_bdry_only ? C.bdry[pp] : pp;
+    int64_t k[3];
+    cell(C.cur[i], k);
+    if (k[0] < -2 || k[1] < -2 || k[2] < -2 || k[0] > (1 << 19) || k[1] > (1 << 19) || k[2] > (1 << 19)) continue;
+    cand.clear();
+    for (int64_t a = k[0] - 1; a <= k[0] + 1; ++a)
+      for (int64_t b2 = k[1] - 1; b2 <= k[1] + 1; ++b2)
+        for (int64_t c = k[2] - 1; c <= k[2] + 1; ++c) {
+          if (a < -1 || b2 < -1 || c < -1) continue;
+          const uint64_t kk = key(a, b2, c);
+          auto it = std::lower_bound(grid.begin(), grid.end(), std::make_pair(kk, 0u));
+          for (; it != grid.end() && it->first == kk; ++it) cand.push_back(it->second);
+        }
+    std::sort(cand.begin(), cand.end());
+    for (uint32_t qq : cand) pair(i, cn.nl_bdry_only ? N.bdry[qq] : qq);
   }
   return contacts;
 }
@@ -730,6 +779,8 @@ or_sim *or_create(const pd_setup_arrays *su, const pd_config *cfg) {
   or_set_threads(S, 1);
   return S;
 }
+
+void or_set_cell_search(or_sim *S, int on) { S->cn.cell_search = on ? 1 : 0; }
 
 void or_set_threads(or_sim *S, int threads) {
   if (threads < 1) threads = 1;

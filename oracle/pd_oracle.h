@@ -24,6 +24,10 @@ typedef struct or_sim or_sim;
 int or_config_default(pd_config *cfg);
 or_sim *or_create(const pd_setup_arrays *setup, const pd_config *cfg);
 void or_set_threads(or_sim *s, int threads);
+/* Node-node and self-contact visit only the node pairs whose current positions lie in
+ * neighbouring cells of edge just above the contact radius, in the reference's order: the
+ * same sums, bit for bit, at a cost that follows the pairs in reach (large test cases). */
+void or_set_cell_search(or_sim *s, int on);
 /* Runs steps t = t0+1 .. t0+nsteps (t0 = steps already taken). */
 int or_step(or_sim *s, uint32_t nsteps);
 int or_get_state(or_sim *s, double *curpos, double *vel, double *acc, double *force);

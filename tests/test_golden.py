@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 from tests.golden.make_golden import load
+from oracle import oracle as O
 from tests import cases
 
 NAMES = sorted(cases.CASES)
@@ -61,3 +62,46 @@ def test_gpu_fp64_matches_reference_golden(name):
         _check(name, g, t, counter, st["curpos"], st["vel"], st["acc"], st["force"], sim.connectivity, w, r,
                sim.applied_force_density())
     sim.close()
+
+
+def test_oracle_cell_search_equals_brute_force():
+    """The oracle's cell-search contact (used to check large cases) gives the brute-force loops'
+    results bit for bit on every small case, contacts and self-contact included."""
+    from tests import cases
+    for name in sorted(cases.CASES):
+        s, cfg = cases.CASES[name]()
+        a = O.Oracle(s, cfg)
+        b = O.Oracle(s, cfg, cell_search=True)
+        for _ in range(3):
+            k = max(1, cfg["timesteps"] // 3)
+            a.step(k)
+            b.step(k)
+            sa, sb = a.state(), b.state()
+            for key in sa:
+                np.testing.assert_array_equal(sa[key], sb[key], err_msg=f"{name} {key}")
+            assert a.counts() == b.counts(), name
+            for p in range(s.n_particles):
+                np.testing.assert_array_equal(a.connectivity(p), b.connectivity(p))
+            np.testing.assert_array_equal(a.wall()[1], b.wall()[1])
+
+
+def test_oracle_cell_search_equals_brute_force_on_a_packing_in_contact():
+    """Eight overlapping particles pressed by the top wall (inter-particle and self-contact,
+    breaking): 10 steps by both contact loops, bit for bit."""
+    from peridem_gb300 import gen
+    MM = 1e-3
+    s, cfg = gen.crush512(n=2, box=2.2 * MM, steps=10, dt=5e-9, hs=(0.075 * MM, 0.1 * MM), smin=1.2 * MM,
+                          smax=1.4 * MM)
+    cfg.update(wall_z_max=float(s.pos[:, 2].max()) + 0.02 * MM, speed_wall_z_max=-20.0, compute_wall_reaction=1)
+    a = O.Oracle(s, cfg)
+    b = O.Oracle(s, cfg, cell_search=True)
+    a.step(10)
+    b.step(10)
+    sa, sb = a.state(), b.state()
+    for key in sa:
+        np.testing.assert_array_equal(sa[key], sb[key], err_msg=key)
+    assert a.counts() == b.counts()
+    broken = len(s.conn) - sum(len(a.connectivity(p)) for p in range(s.n_particles))
+    assert broken > 0
+    for p in range(s.n_particles):
+        np.testing.assert_array_equal(a.connectivity(p), b.connectivity(p))
