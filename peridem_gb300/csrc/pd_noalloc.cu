@@ -18,8 +18,9 @@
 //
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current and remembers it for that device. That
-// first call should come before any stream capture. Call it with the simulation's device
-// current (the device the simulation was created on).
+// first call should come before any stream capture. Every call runs on the simulation's own
+// device (the device of its stream): when another device is current, the call makes the
+// simulation's device current for its duration and restores the caller's device afterwards.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -80,6 +81,10 @@ __global__ void k_live_total(unsigned long long *part, uint32_t nblocks) {
 }  // namespace
 }  // namespace pdg
 
+namespace {
+int count_on_device(pd_sim *s, cudaStream_t st, int dev, uint64_t N, uint64_t *live);
+}
+
 extern "C" int pd_count_live_bonds_noalloc(pd_sim *s, uint64_t *live) {
   using namespace pdg;
   if (!s || !live) return PD_EINVAL;
@@ -89,12 +94,32 @@ extern "C" int pd_count_live_bonds_noalloc(pd_sim *s, uint64_t *live) {
                  std::to_string(kNoAllocMaxNodes) + " nodes";
     return PD_EINVAL;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  if (N == 0) {  // nothing to count (and no zero-block launch)
+    *live = 0;
+    return PD_OK;
+  }
+  cudaStream_t st = s->eng.stream();
+  int dev = 0, caller_dev = 0;
+  cudaError_t e = cudaStreamGetDevice(st, &dev);
+  if (e == cudaSuccess) e = cudaGetDevice(&caller_dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    s->eng.err = "pd_count_live_bonds_noalloc: no usable current device";
+    s->eng.err = "pd_count_live_bonds_noalloc: no usable device for the simulation's stream";
     return PD_ECUDA;
   }
+  if (caller_dev != dev && cudaSetDevice(dev) != cudaSuccess) {
+    s->eng.err = "pd_count_live_bonds_noalloc: cannot make the simulation's device current";
+    return PD_ECUDA;
+  }
+  const int rc = count_on_device(s, st, dev, N, live);
+  if (caller_dev != dev) cudaSetDevice(caller_dev);
+  return rc;
+}
+
+namespace {
+// The count itself, with the simulation's device current.
+int count_on_device(pd_sim *s, cudaStream_t st, int dev, uint64_t N, uint64_t *live) {
+  using namespace pdg;
+  cudaError_t e = cudaSuccess;
   unsigned long long *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -110,7 +135,6 @@ extern "C" int pd_count_live_bonds_noalloc(pd_sim *s, uint64_t *live) {
     scratch = g_scratch_addr[dev];
   }
   const uint32_t nblocks = (uint32_t)((N + kNoAllocThreads - 1) / kNoAllocThreads);
-  cudaStream_t st = s->eng.stream();
   k_live_partials<<<nblocks, kNoAllocThreads, 0, st>>>(s->eng.current_view(), scratch);
   k_live_total<<<1, kNoAllocThreads, 0, st>>>(scratch, nblocks);
   e = cudaGetLastError();
@@ -128,3 +152,4 @@ extern "C" int pd_count_live_bonds_noalloc(pd_sim *s, uint64_t *live) {
   *live = h;
   return PD_OK;
 }
+}  // namespace

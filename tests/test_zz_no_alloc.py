@@ -50,3 +50,29 @@ def test_noalloc_fp32c_handle():
     assert _noalloc(sim) == sim.live_bonds()
     assert _noalloc(sim) == sim.live_bonds()
     sim.close()
+
+
+def test_noalloc_refuses_handles_above_its_limit():
+    """A handle of more nodes than the static scratch holds (1,048,576) gets PD_EINVAL and a
+    message naming the limit; the allocating entry point still counts it."""
+    import numpy as np
+
+    from peridem_gb300.setupdata import concat
+    n = 102
+    ax = np.arange(n) * 1e-3  # nodes 1 mm apart, horizon 0.1 mm: no bonds, no contacts
+    X, Y, Z = np.meshgrid(ax, ax, ax[:101], indexing="ij")
+    pos = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    assert len(pos) > 1 << 20
+    part = dict(pos=pos, vol=np.full(len(pos), 1e-12), conn=np.zeros((0, 2), np.uint32),
+                rho=2440.0, delta=1e-4, cnot=1.0, snot=1e-3)
+    s = concat([part], dict(contact_radius=1e-5, normal_stiffness=1.0, damping_ratio=0.8,
+                            friction_coefficient=0.3), None)
+    sim = Sim(s, dict(dt=1e-9, timesteps=1, enable_fracture=0), "fp64")
+    n_out = C.c_uint64(12345)
+    rc = _capi.lib().pd_count_live_bonds_noalloc(sim.h, C.byref(n_out))
+    assert rc == _capi.PD_EINVAL
+    msg = _capi.lib().pd_last_error(sim.h).decode()
+    assert "1048576" in msg and str(len(pos)) in msg, msg
+    assert n_out.value == 12345  # nothing written on refusal
+    assert sim.live_bonds() == 0
+    sim.close()
