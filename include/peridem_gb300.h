@@ -43,7 +43,9 @@ extern "C" {
 
 /* ---- device error word bits (pd_device_errors) ----------------------------------- */
 #define PD_DERR_NONFINITE 1u      /* a NaN/Inf force density was produced             */
-#define PD_DERR_CAND_OVERFLOW 2u  /* per-node contact candidate list overflowed       */
+#define PD_DERR_CAND_OVERFLOW 2u  /* not raised: a node with more contact candidates than
+                                     its list holds takes them from the cell list (same
+                                     results) and the lists grow at the next pd_step      */
 #define PD_DERR_CONTACT_OVERFLOW 4u /* more in-range contacts than the per-node cap   */
 #define PD_DERR_STAGE_TIMEOUT 8u    /* a shared-memory staging copy missed its wait limit
                                        (the block used global loads; results unaffected) */
@@ -224,7 +226,9 @@ const char *pd_global_error(void);
 int pd_close(pd_sim *sim);
 
 /* Tuning knobs: contact skin as a fraction of the contact radius (<= 0 keeps it), per-node
- * candidate capacity (0 keeps it, at most 64), threads per block (<= 0 keeps it), per-step
+ * candidate capacity (0 keeps it, at most 64; capacity never changes results: a node with more
+ * candidates walks the broad phase's cell list instead, and after a pd_sync that saw one the
+ * next pd_step doubles the capacity, up to 64), threads per block (<= 0 keeps it), per-step
  * statistics on/off (< 0 keeps it; on adds the pair-count kernel), step launch mode
  * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the default below 131,072
  * nodes, 2 the same graph with the broad-phase rebuild kernels in a conditional node, the
@@ -302,6 +306,23 @@ int pd_get_sim_disp(pd_sim *sim, uint32_t i, double *disp);
 int pd_get_sim_wall(pd_sim *sim, uint32_t i, double *wall_info, double *reaction);
 /* Damage of simulation i alone (N_i, its own node order; pd_get_damage's definition). */
 int pd_get_sim_damage(pd_sim *sim, uint32_t i, double *damage);
+/* Eviction and re-admission. pd_save_sim writes a checkpoint of simulation i at the current
+ * step boundary into host memory: everything stepping changes (displacement, velocity,
+ * acceleration, force, each particle's live bonds as its Connectivity, walls and their
+ * reactions, step counter, scheduled toggles, the FP32 form's records and predicted step).
+ * *bytes receives its size; with buf == NULL only the size is returned, else cap must hold it.
+ * It extends the reference's resume (timeloop.h:262-312, which reloads CurrPos, vel, acc,
+ * Connectivity and the wall from a frame) to an exact continuation: the displacement is saved
+ * as such (not as CurrPos - pos) together with the rest of the state. A finished simulation
+ * (pd_finish_sim) cannot be saved (PD_ESTATE). The handle may be closed afterwards: its device
+ * memory returns at pd_close. */
+int pd_save_sim(pd_sim *sim, uint32_t i, void *buf, uint64_t cap, uint64_t *bytes);
+/* Loads such a checkpoint into simulation i of a handle (a batch or single handle) whose
+ * simulation i was created from the same setup and config in the same precision form
+ * (PD_EINVAL otherwise), at a step boundary of that handle. From then on simulation i computes
+ * exactly what the saved simulation would have computed had it stepped on; the other
+ * simulations of the handle are not touched. */
+int pd_load_sim(pd_sim *sim, uint32_t i, const void *buf, uint64_t bytes);
 
 /* ---- bond lists on the GPU (setup generation) -----------------------------------------
  * For each particle p (nodes [node_offset[p], node_offset[p+1]) of pos, N*3), every node pair

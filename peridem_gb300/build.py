@@ -117,7 +117,8 @@ def build_oracle(verbose: bool = False) -> None:
     r = subprocess.run(["make", "-C", str(odir)], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref = Path(os.environ.get("PD_REFERENCE_DIR", "/root/reference"))
+    # PeriDEM's sources: PD_REFERENCE_DIR, else a checkout named `reference` beside this repository
+    ref = Path(os.environ.get("PD_REFERENCE_DIR") or (ROOT.parent / "reference"))
     if (ref / "run" / "simulate3d.cpp").exists():
         r = subprocess.run(["make", "-C", str(odir), "ref", f"REF={ref}"], capture_output=True, text=True)
         if r.returncode != 0:

@@ -3,7 +3,9 @@
 // within contact radius + skin. The reference tests every node pair of every particle
 // pair whose AABBs intersect (timeloop.h:637-651, contact.h:754-769); the exact distance
 // test of the reference is still made for every candidate in every step (pd_kernels.cu),
-// so the lists only need to be a superset of the pairs within the contact radius.
+// so the lists only need to be a superset of the pairs within the contact radius. A node with
+// more candidates than a list holds is marked to walk the cell list instead (CandWalk,
+// pd_device.cuh): the same partners in the same order, so capacity never changes results.
 //
 // The lists are rebuilt only when the accumulated bound on node movement since the last
 // build could exceed half the skin: every kernel here first reads the rebuild flag set by
@@ -12,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "pd_device.cuh"
 #include "pd_engine.h"
 #include "pd_math.cuh"
 
@@ -22,20 +25,8 @@ namespace {
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
 constexpr int kScanBlock = kScanThreads * kScanPer;
-constexpr int kMaxCand = 64;
+constexpr int kMaxCand = (int)kMaxCandCap;
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;  // node not in the cell list
-
-__device__ __forceinline__ uint32_t cell_hash(long long cx, long long cy, long long cz, uint32_t sim,
-                                              uint32_t mask) {
-  unsigned long long h = (unsigned long long)cx * 0x9E3779B97F4A7C15ull;
-  h ^= (unsigned long long)cy * 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
-  h ^= (unsigned long long)cz * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
-  h ^= (unsigned long long)sim * 0x27D4EB2F165667C5ull;
-  h ^= h >> 31;
-  h *= 0x7FB5D329728EA185ull;
-  h ^= h >> 27;
-  return (uint32_t)h & mask;
-}
 
 __device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double cell, long long &cx,
                                           long long &cy, long long &cz, double &x, double &y, double &z) {
@@ -198,18 +189,24 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
           if (pos > 0 && list[pos - 1] == fm) continue;
           if (cnt >= (int)cap) {
             overflow = true;
-            continue;
+            break;
           }
           for (int q = cnt; q > pos; --q) list[q] = list[q - 1];
           list[pos] = fm;
           ++cnt;
         }
       }
-  uint32_t *out = cand + n * cap;
-  for (int i = 0; i < cnt; ++i) out[i] = v.node_of[list[i]];
-  cand_n[n] = (uint16_t)cnt;
+  if (overflow) {
+    // more partners than the list holds: the consumers walk the cell list for this node instead
+    // (CandWalk), which gives the same partners in the same order; the host grows the lists
+    cand_n[n] = kCandCells;
+    atomicAdd(&v.cnt->cand_cells, 1u);
+  } else {
+    uint32_t *out = cand + n * cap;
+    for (int i = 0; i < cnt; ++i) out[i] = v.node_of[list[i]];
+    cand_n[n] = (uint16_t)cnt;
+  }
   if (cnt && v.xnodes) v.xnodes[atomicAdd(&v.xcount[0], 1u)] = (uint32_t)n;  // FP32 form: work list
-  if (overflow) atomicOr(&v.cnt->err, PD_DERR_CAND_OVERFLOW);
 }
 
 }  // namespace

@@ -139,6 +139,94 @@ __device__ __forceinline__ void wall_face(double dist, int dir, D3 vel, double v
   }
 }
 
+// Bucket of a broad-phase cell (hashed cell list: cells of every simulation share one table).
+__device__ __forceinline__ uint32_t cell_hash(long long cx, long long cy, long long cz, uint32_t sim,
+                                              uint32_t mask) {
+  unsigned long long h = (unsigned long long)cx * 0x9E3779B97F4A7C15ull;
+  h ^= (unsigned long long)cy * 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
+  h ^= (unsigned long long)cz * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
+  h ^= (unsigned long long)sim * 0x27D4EB2F165667C5ull;
+  h ^= h >> 31;
+  h *= 0x7FB5D329728EA185ull;
+  h ^= h >> 27;
+  return (uint32_t)h & mask;
+}
+
+// The contact partners of node n in ascending file-order index (the order in which the
+// reference visits them): its candidate list, or, for a node whose list overflowed at the last
+// rebuild, the nodes of the same simulation in the 27 cells around its current position that
+// lie within the candidate radius now, taken one at a time by selection. Both are supersets of
+// the partners within the contact radius (a node moves less than half the skin between
+// rebuilds and cells are wider than the candidate radius), and every consumer makes the exact
+// distance test, so the two give the same sums; the cell walk costs a scan of the 27 cells per
+// partner, which only nodes in unusually dense contact pay.
+struct CandWalk {
+  const DevView &v;
+  uint64_t n;
+  const uint32_t *cl;
+  int nc, c;
+  bool cells;
+  long long cx, cy, cz;
+  double x, y, z, r2;
+  uint32_t sim;
+  long long last;  // file index of the partner returned last (-1: none yet)
+
+  __device__ __forceinline__ CandWalk(const DevView &view, uint64_t node) : v(view), n(node), c(0), last(-1) {
+    const uint16_t k = v.cand_n[n];
+    cells = k == kCandCells;
+    nc = cells ? 0 : (int)k;
+    cl = v.cand + n * v.cand_cap;
+    if (cells) {
+      sim = v.parts[v.pid[n]].sim;
+      const DevSimParams &sp = v.sp[sim];
+      x = v.pos[n] + v.disp[n];
+      y = v.pos[n + v.Ncap] + v.disp[n + v.Ncap];
+      z = v.pos[n + 2 * v.Ncap] + v.disp[n + 2 * v.Ncap];
+      cx = (long long)floor(x / sp.cell);
+      cy = (long long)floor(y / sp.cell);
+      cz = (long long)floor(z / sp.cell);
+      r2 = sp.cand_r2;
+    }
+  }
+
+  __device__ __noinline__ bool next_cell(uint32_t &m) {
+    uint32_t best = 0, best_m = 0;
+    bool found = false;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const uint32_t kk = cell_hash(cx + dx, cy + dy, cz + dz, sim, v.cell_mask);
+          const uint32_t b = v.cell_start[kk], e = b + v.cell_count[kk];
+          for (uint32_t it = b; it < e; ++it) {
+            const uint32_t q = v.cell_sorted[it];
+            if (q == n || v.parts[v.pid[q]].sim != sim) continue;
+            const uint32_t fq = v.file_of[q];
+            if ((long long)fq <= last || (found && fq >= best)) continue;
+            const double ddx = (v.pos[q] + v.disp[q]) - x;
+            const double ddy = (v.pos[q + v.Ncap] + v.disp[q + v.Ncap]) - y;
+            const double ddz = (v.pos[q + 2 * v.Ncap] + v.disp[q + 2 * v.Ncap]) - z;
+            if (ddx * ddx + ddy * ddy + ddz * ddz > r2) continue;
+            best = fq;
+            best_m = q;
+            found = true;
+          }
+        }
+    if (!found) return false;
+    last = best;
+    m = best_m;
+    return true;
+  }
+
+  __device__ __forceinline__ bool next(uint32_t &m) {
+    if (!cells) {
+      if (c >= nc) return false;
+      m = cl[c++];
+      return true;
+    }
+    return next_cell(m);
+  }
+};
+
 // Does row n hold a live bond to global node m? (std::find over NbdArr, contact.h:783)
 __device__ __forceinline__ bool row_has_live(const DevView &v, uint64_t n, uint32_t m) {
   const uint64_t s = n >> 5;
@@ -164,6 +252,38 @@ __device__ __forceinline__ bool nonfinite(double x) {
   return ((__double2hiint(x) >> 20) & 0x7FF) == 0x7FF;
 }
 
+// FP32 form: the band [snot (1 - w), snot (1 + w)] in which a bond's breaking decision is
+// re-taken in FP64 (outside it the FP32 stretch decides), wide enough that the FP32 stretch can
+// never be on the other side of snot outside it. With eps = 2^-24 and s <= 2 snot near the band:
+//  * reference positions are stored as floats relative to the anchor, |component| <= ext_p, so
+//    xi is off by at most a = 2 sqrt(3) eps ext_p; displacements likewise, |component| <= u_max,
+//    so eta is off by at most b = 2 sqrt(3) eps u_max. The stretch s = |xi + eta| / |xi| - 1
+//    moves by at most (|b| + |y^ - (1 + s) xi^| |a|) / |xi| <= (b + (2 + s) a) / xi_min to first
+//    order, whatever the rotation of the bond;
+//  * the numerator eta.(xi + y) is a dot product of vectors up to (2 + s)|xi| and (4 + s)|xi| long
+//    (a rotated bond): its rounding moves s by at most 4 eps (2 + s)(4 + s); the approximate
+//    reciprocal square roots and reciprocal (relative error below 2^-22 each) and the remaining
+//    roundings add at most 3 * 2^-22 s.
+// w is 1.25 times that bound over snot (the band is set from this step's extent and used in the
+// next), and at least 1e-4. xi_min is the particle's shortest setup bond: reference positions do
+// not change, so no bond gets shorter.
+__device__ __forceinline__ void set_break_band(DevPart &P, double u_max) {
+  const double eps = 5.9604644775390625e-08, two_sqrt3 = 3.4641016151377544;
+  const double s = 2.0 * P.snot;
+  const double a = two_sqrt3 * eps * P.ext_p, b = two_sqrt3 * eps * u_max;
+  const double ds = (b + (2.0 + s) * a) / P.xi_min + 4.0 * eps * (2.0 + s) * (4.0 + s) + 3.0 * 4.0 * eps * s;
+  double w = 1.25 * ds / P.snot;
+  if (!(w >= 1e-4)) w = 1e-4;  // also for a particle without bonds (xi_min infinite: ds finite)
+  P.snot_lo32 = __double2float_rd(P.snot * (1.0 - w));
+  P.snot_hi32 = __double2float_ru(P.snot * (1.0 + w));
+}
+
+// Largest |component| of a particle's anchor-relative displacement, bounded from the box of its
+// current anchor-relative positions p + u (|u| <= |p + u| + |p|).
+__device__ __forceinline__ double u_extent(const DevPart &P, double box_extent) {
+  return box_extent + P.ext_p;
+}
+
 // Per-particle inputs of the FP32 form's end of step that depend only on the particle index,
 // loaded together before the kernel's branches (the kernel is a short chain of dependent loads).
 struct EndPre {
@@ -181,7 +301,7 @@ __device__ __forceinline__ void end_pre_fp32c(const DevView &v, uint32_t k, uint
   for (int c = 0; c < 3; ++c) {
     e.an[c] = v.anchor[3 * (uint64_t)k + c];
     e.ann[c] = v.anchor_next[3 * (uint64_t)k + c];
-    e.dn[c] = v.disp_next[g0 + c * v.Ncap];
+    e.dn[c] = v.disp_next[P.anchor + c * v.Ncap];
     e.apos[c] = P.anchor_pos[c];
   }
   e.movable = P.movable;
@@ -196,13 +316,16 @@ __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k,
   double *ann = v.anchor_next + 3 * (uint64_t)k;
   unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
   if (e.movable) {
+    double ext = 0.0;
     for (int c = 0; c < 3; ++c) {
       const float lo = fval(e.L[c]), hi = fval(e.L[3 + c]);
       const double base = e.apos[c] + e.an[c];
       const double w = 8.0 * (double)FLT_EPSILON * fmax(fabs((double)lo), fabs((double)hi)) + 1e-30;
       v.lrtb[6 * (uint64_t)k + c] = base + (double)lo - w;
       v.lrtb[6 * (uint64_t)k + 3 + c] = base + (double)hi + w;
+      ext = fmax(ext, fmax(fabs((double)lo), fabs((double)hi)) + w);
     }
+    set_break_band(v.parts[k], u_extent(v.parts[k], ext));
   }
   for (int c = 0; c < 3; ++c) {
     L[c] = fkey(INFINITY);

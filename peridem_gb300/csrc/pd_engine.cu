@@ -132,6 +132,10 @@ DevView Engine::view(int cur) const {
   v.cand = bp_.cand;
   v.cand_n = bp_.cand_n;
   v.cand_cap = bp_.cand_cap;
+  v.cell_count = bp_.count;
+  v.cell_start = bp_.start;
+  v.cell_sorted = bp_.sorted;
+  v.cell_mask = bp_.table_bits ? (uint32_t)((1ull << bp_.table_bits) - 1) : 0u;
   v.centroid = d_centroid_;
   v.afd = d_afd_;
   if (n_clamped_) {
@@ -622,13 +626,10 @@ int Engine::alloc_and_upload() {
       P.stoppable = s.stoppable[p];
       P.break_bonds = 1;  // simulate3d.cpp:137-139
       P.has_ext = part_ext[gp];
-      P.snot_lo32 = (float)(P.snot * (1.0 - 1e-4));
-      P.snot_hi32 = (float)(P.snot * (1.0 + 1e-4));
       if (P.n == 0) {
         err = "particle " + std::to_string(p) + " has no nodes";
         return PD_EINVAL;
       }
-      for (int c = 0; c < 3; ++c) P.anchor_pos[c] = pos[c * C + P.g0];
       h_g0_[gp] = P.g0;
       if (!s.bdry_offset.empty())
         for (uint64_t l = s.bdry_offset[p]; l < s.bdry_offset[p + 1]; ++l) {
@@ -767,6 +768,41 @@ int Engine::alloc_and_upload() {
   PD_TRY(dalloc(this, allocs_, &d_sp_, S_, err));
   PD_TRY(dalloc(this, allocs_, &d_ss_, S_, err));
   PD_TRY(dalloc(this, allocs_, &d_cnt_, 1, err));
+  // FP32 form: each particle's records are relative to an anchor node, the node nearest the
+  // centre of the particle's box (the FP32 rounding of a record grows with its distance from the
+  // anchor); ext_p bounds the reference positions' rounding (set_break_band). xi_min is measured
+  // on the device once the bonds are built.
+  parallel_items(P_, [&](uint64_t k) {
+    DevPart &P = parts[k];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint64_t g = P.g0; g < (uint64_t)P.g0 + P.n; ++g)
+      for (int c = 0; c < 3; ++c) {
+        lo[c] = std::min(lo[c], pos[c * C + g]);
+        hi[c] = std::max(hi[c], pos[c * C + g]);
+      }
+    double best = INFINITY;
+    uint32_t a = P.g0;
+    for (uint64_t g = P.g0; g < (uint64_t)P.g0 + P.n; ++g) {
+      double d2 = 0;
+      for (int c = 0; c < 3; ++c) {
+        const double d = pos[c * C + g] - 0.5 * (lo[c] + hi[c]);
+        d2 += d * d;
+      }
+      if (d2 < best) {
+        best = d2;
+        a = (uint32_t)g;
+      }
+    }
+    P.anchor = a;
+    double ep = 0;
+    for (int c = 0; c < 3; ++c) P.anchor_pos[c] = pos[c * C + a];
+    for (uint64_t g = P.g0; g < (uint64_t)P.g0 + P.n; ++g)
+      for (int c = 0; c < 3; ++c) ep = std::max(ep, std::fabs(pos[c * C + g] - P.anchor_pos[c]));
+    P.ext_p = ep;
+    P.xi_min = INFINITY;
+    P.snot_lo32 = (float)P.snot;
+    P.snot_hi32 = (float)P.snot;
+  });
   auto up = [&](void *d, const void *h, size_t b, const char *w) { return cpy(d, h, b, w); };
   PD_TRY(up(d_pos_, pos.get(), 3 * C * 8, "upload pos"));
   PD_TRY(up(d_disp_, disp.get(), 3 * C * 8, "upload disp"));
@@ -911,6 +947,16 @@ int Engine::alloc_and_upload() {
     launch_init_lrtb(v, stream_);
     PD_TRY(check(cudaGetLastError(), "init kernels"));
   } else {
+    // each particle's shortest bond, for the breaking band that prepare_fused sets
+    unsigned long long *d2min = nullptr;
+    PD_TRY(check(cudaMallocAsync((void **)&d2min, 8ull * std::max<uint32_t>(P_, 1), stream_), "xi_min scratch"));
+    int rc = check(cudaMemsetAsync(d2min, 0xFF, 8ull * P_, stream_), "xi_min scratch");
+    if (rc == PD_OK) {
+      launch_xi_min(view(0), d2min, stream_);
+      rc = check(cudaGetLastError(), "xi_min");
+    }
+    cudaFreeAsync(d2min, stream_);
+    PD_TRY(rc);
     cur_ = 1;
     PD_TRY(prepare_fused(cur_));
   }
@@ -1065,6 +1111,13 @@ int Engine::capture_graphs() {
 }
 
 int Engine::step(uint32_t nsteps) {
+  if (grow_cand_) {  // some node walked the cell list since the last grow: longer lists from now on
+    grow_cand_ = false;
+    const uint32_t cap = std::min<uint32_t>(kMaxCandCap, 2 * bp_.cand_cap);
+    if (cap > bp_.cand_cap) PD_TRY(set_tuning(0.0, cap, 0, -1, -1));
+    uint32_t z = 0;
+    PD_TRY(cpy(&d_cnt_->cand_cells, &z, 4, "reset cell-walk count"));
+  }
   if (!graphs_ok_ && use_graphs_) PD_TRY(capture_graphs());
   for (uint32_t i = 0; i < nsteps; ++i) {
     if (use_graphs_) {
@@ -1101,10 +1154,10 @@ int Engine::sync(int timeout_ms) {
   }
   DevCounters c;
   PD_TRY(cpy(&c, d_cnt_, sizeof(c), "read counters"));
+  if (c.cand_cells && bp_.cand_cap < kMaxCandCap) grow_cand_ = true;
   if (c.err) {
     err = "device error word 0x" + std::to_string(c.err);
     if (c.err & PD_DERR_NONFINITE) err += " (non-finite force density)";
-    if (c.err & PD_DERR_CAND_OVERFLOW) err += " (contact candidate list overflow: raise cand_cap)";
     return PD_EDEVICE;
   }
   return PD_OK;
@@ -1353,8 +1406,8 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
     relaunch = true;
   }
   if (cand_cap > 0 && cand_cap != bp_.cand_cap) {
-    if (cand_cap > 64) {
-      err = "cand_cap above 64";
+    if (cand_cap > kMaxCandCap) {
+      err = "cand_cap above " + std::to_string(kMaxCandCap);
       return PD_EINVAL;
     }
     bp_.cand_cap = cand_cap;
@@ -1595,10 +1648,9 @@ int Engine::snapshot() {
     reg(d_extra_flag_, C);
     reg(d_f_extra_, 3 * C * 8);
   }
-  reg(bp_.cand, (size_t)C * bp_.cand_cap * 4);
-  reg(bp_.cand_n, (size_t)C * 2);
+  // the contact candidate lists, the cell list and the FP32 form's contact-node list are
+  // derived from the positions: restore() has the next step rebuild them instead
   if (bp_.xcount) {
-    reg(bp_.xnodes, (size_t)C * 4);
     reg(bp_.xparts, (size_t)P_ * 4);
     reg(bp_.xcount, 8);
   }
@@ -1643,6 +1695,13 @@ int Engine::restore() {
   }
   if (precision_ == PD_FP32C) launch_col_flags(view(cur_), stream_);  // broken flags from the masks
   PD_TRY(check(cudaGetLastError(), "restore"));
+  {  // the next step rebuilds the broad phase from the restored positions (results do not depend
+     // on when it is rebuilt); the FP32 non-bond kernel visits every node once meanwhile
+    const double big = 1e300;
+    const uint32_t one = 1;
+    PD_TRY(check(cudaMemcpyAsync(&d_cnt_->moved, &big, 8, cudaMemcpyHostToDevice, stream_), "restore"));
+    PD_TRY(check(cudaMemcpyAsync(&d_cnt_->xall, &one, 4, cudaMemcpyHostToDevice, stream_), "restore"));
+  }
   cur_ = backup_cur_;
   steps_done_ = backup_steps_;
   sim_steps_ = backup_sim_steps_;

@@ -66,6 +66,8 @@ constexpr int kSlice = 32;
 constexpr int kStageNodes = 512;          // nodes per block of the staged bond kernel
 constexpr uint32_t kStageMaxRecords = 6400;  // 200 KB of 32-byte records per block
 constexpr uint32_t kNoCol = 0xFFFFFFFFu;
+constexpr uint16_t kCandCells = 0xFFFFu;  // cand_n of a node whose contact partners come from the cell list
+constexpr uint32_t kMaxCandCap = 64;      // largest per-node candidate list
 constexpr uint32_t kColBroken = 0x80000000u;  // FP32 form: broken flag in a column entry
 constexpr uint32_t kColIndex = 0x7FFFFFFFu;   // the partner index in a column entry
 constexpr uint64_t kOrderWindow = 1024;     // nodes per window of the bond-count sort (order_nodes)
@@ -77,7 +79,10 @@ struct DevPart {
   int32_t movable, breakable, stoppable, break_bonds;
   double anchor_pos[3];  // FP32 form: position of the anchor node
   int32_t has_ext;       // any non-zero extforce in this particle
-  float snot_lo32, snot_hi32;  // FP32 form: the band around snot
+  uint32_t anchor;       // FP32 form: the anchor node (the node nearest the particle's box centre)
+  double ext_p;          // FP32 form: largest |component| of a node's position relative to the anchor
+  double xi_min;         // FP32 form: shortest bond of the particle's setup (reference positions)
+  float snot_lo32, snot_hi32;  // FP32 form: the band around snot where FP64 decides (set_break_band)
 };
 
 // Per-simulation constants (Contact, RectWall and Timeloop fields after apply_config).
@@ -127,6 +132,7 @@ struct DevCounters {
   double last_stepmax;              // movement bound of the step that just ended
   uint32_t end_blocks;              // blocks of k_end_step done (the last one advances the sims)
   uint32_t xall;                    // FP32 form: k_extra32 visits every node this step (no lists)
+  uint32_t cand_cells;              // nodes whose candidate list overflowed (they walk the cells)
 };
 
 // FP32 form: one 32-byte record per node, so that a bond gathers its partner with a single
@@ -185,8 +191,11 @@ struct DevView {
   DevSimState *ss;
   // contact
   const uint32_t *cand;  // [N][cap]
-  const uint16_t *cand_n;
+  const uint16_t *cand_n;  // list length, or kCandCells: walk the cell list (the list overflowed)
   uint32_t cand_cap;
+  // the broad phase's hashed cell list (valid from one rebuild to the next)
+  const uint32_t *cell_count, *cell_start, *cell_sorted;
+  uint32_t cell_mask;
   // torque centroids [P][3]
   const double *centroid;
   DevCounters *cnt;
@@ -332,6 +341,12 @@ class Engine {
   bool sim_finished(uint32_t sim) const { return sim < S_ && finished_[sim]; }
   // N*3 arrays of one simulation (its own node order); any pointer may be NULL.
   int get_sim_state(uint32_t sim, double *curpos, double *vel, double *acc, double *force, double *disp);
+  // Checkpoint of one simulation at a step boundary (everything stepping changes, in a form that
+  // does not depend on the handle's layout), and its load into simulation `sim` of a handle
+  // created from the same setup and config: stepping on from the load computes what stepping on
+  // from the save would have. A finished simulation cannot be saved (its device state is gone).
+  int save_sim(uint32_t sim, std::vector<uint8_t> &out);
+  int load_sim(uint32_t sim, const uint8_t *buf, uint64_t n);
   // Bytes of device memory this engine holds, and the same figure computed from a setup
   // before anything is allocated.
   uint64_t device_bytes() const { return device_bytes_; }
@@ -412,6 +427,7 @@ class Engine {
   bool torque_possible_ = false;
   bool stats_ = false;
   bool use_graphs_ = true;
+  bool grow_cand_ = false;  // a sync saw nodes walking the cell list: double the lists at the next step
   bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning
                                   // mode 2); init() picks by size
   int variant_ = 18;  // FP32 bond-kernel variant; init() picks by size (the autotuner's usual choices)
@@ -523,6 +539,9 @@ void launch_count_live(const DevView &v, unsigned long long *out, cudaStream_t s
 // order - n0) must be zeroed; out[nn] in file order - n0.
 void launch_damage(const DevView &v, uint64_t n0, uint64_t nn, uint32_t *now, double *out, cudaStream_t s);
 void launch_anchor_next(const DevView &v, cudaStream_t s);
+// FP32 form: each particle's shortest setup bond into DevPart::xi_min (d2min: [P] scratch set to
+// all ones).
+void launch_xi_min(const DevView &v, unsigned long long *d2min, cudaStream_t s);
 void launch_col_flags(const DevView &v, cudaStream_t s);
 void launch_rows_to_file(const double *src, const double *add, uint64_t Ncap, uint64_t N, const uint32_t *file_of,
                          double *dst, cudaStream_t s);

@@ -50,7 +50,7 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
   const DevPart &P = v.parts[k];
   const DevSimParams &sp = v.sp[P.sim];
   DevSimState &st = v.ss[P.sim];
-  const int nc = v.cand_n[n];
+  const bool nc = v.cand_n[n] != 0;  // contact candidates (a list, or the cell walk)
   const bool mov = P.movable != 0;
   bool wall_near = false;
   if (mov && P.stoppable && sp.allow_wall) {
@@ -69,9 +69,9 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
   D3 f = d3(0.0, 0.0, 0.0);
   if (mov) {
     if (nc && st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || bdry_i)) {
-      const uint32_t *cl = v.cand + n * v.cand_cap;
-      for (int c = 0; c < nc; ++c) {
-        const uint32_t m = cl[c];
+      CandWalk walk(v, n);
+      uint32_t m;
+      while (walk.next(m)) {
         if (m < P.g0) continue;
         if (m >= P.g0 + P.n) break;
         if (sp.nl_bdry_only && !v.bdry[m]) continue;
@@ -132,9 +132,9 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
     f = f + (r_inv * P.tval) * perp;
   }
   if (nc && P.stoppable && (!sp.nl_bdry_only || bdry_i)) {
-    const uint32_t *cl = v.cand + n * v.cand_cap;
-    for (int c = 0; c < nc; ++c) {
-      const uint32_t m = cl[c];
+    CandWalk walk(v, n);
+    uint32_t m;
+    while (walk.next(m)) {
       if (m >= P.g0 && m < P.g0 + P.n) continue;
       const uint32_t km = v.pid[m];
       const uint32_t a = km < k ? km : k, b = km < k ? k : km;
@@ -731,8 +731,51 @@ void launch_col_flags(const DevView &v, cudaStream_t s) {
 __global__ void k_anchor_next(DevView v) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= v.P) return;
-  const uint32_t g0 = v.parts[k].g0;
-  for (int c = 0; c < 3; ++c) v.anchor_next[3 * (uint64_t)k + c] = v.disp[g0 + c * v.Ncap];
+  const uint32_t a = v.parts[k].anchor;
+  for (int c = 0; c < 3; ++c) v.anchor_next[3 * (uint64_t)k + c] = v.disp[a + c * v.Ncap];
+}
+
+// Shortest setup bond of every particle (FP64 reference positions), for the breaking band:
+// the squared length's bits (a non-negative double orders like its bits) min-reduced per
+// particle into d2min[P], which must start at all ones.
+__global__ void k_xi_min(const __grid_constant__ DevView v, unsigned long long *d2min) {
+  const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  unsigned long long m = ~0ull;
+  if (valid) {
+    const uint32_t lane = (uint32_t)(nn & 31);
+    const uint32_t *colp = v.col + v.slice_ptr[nn >> 5] + lane;
+    const int dg = v.deg[nn];
+    const D3 pi = ld3(v.pos, nn, v.Ncap);
+    for (int j = 0; j < dg; ++j) {
+      const uint32_t q = colp[32 * j] & kColIndex;
+      const D3 d = ld3(v.pos, q, v.Ncap) - pi;
+      const double d2 = (d.x * d.x + d.y * d.y) + d.z * d.z;
+      m = min(m, (unsigned long long)__double_as_longlong(d2));
+    }
+  }
+  const uint32_t k = v.pid[nn];
+  const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+  if (__all_sync(0xffffffffu, k == k0)) {
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m != ~0ull) atomicMin(&d2min[k0], m);
+  } else if (valid && m != ~0ull) {
+    atomicMin(&d2min[k], m);
+  }
+}
+
+__global__ void k_set_xi_min(DevView v, const unsigned long long *d2min) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= v.P) return;
+  const unsigned long long m = d2min[k];
+  // rounded down a little: a lower bound of every bond length of the particle
+  v.parts[k].xi_min = m == ~0ull ? INFINITY : sqrt(__longlong_as_double((long long)m)) * (1.0 - 1e-12);
+}
+
+void launch_xi_min(const DevView &v, unsigned long long *d2min, cudaStream_t s) {
+  if (v.N) k_xi_min<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v, d2min);
+  if (v.P) k_set_xi_min<<<(v.P + 127) / 128, 128, 0, s>>>(v, d2min);
 }
 
 void launch_anchor_next(const DevView &v, cudaStream_t s) {

@@ -114,10 +114,9 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
 
     // ---- self-contact (timeloop.h:554-557, contact.h:779-796), C side only
     if (st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || bdry_i)) {
-      const uint32_t *cl = v.cand + nn * v.cand_cap;
-      const int nc = v.cand_n[nn];
-      for (int c = 0; c < nc; ++c) {
-        const uint32_t m = cl[c];
+      CandWalk walk(v, nn);
+      uint32_t m;
+      while (walk.next(m)) {
         if (m < P.g0) continue;
         if (m >= P.g0 + P.n) break;
         if (sp.nl_bdry_only && !v.bdry[m]) continue;
@@ -187,10 +186,9 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
   // partners in ascending file-order global index; a partner in a lower particle index acts as
   // the "C" node of the pair (reaction form), a partner in a higher index as the "N" node.
   if (run && P.stoppable && (!sp.nl_bdry_only || bdry_i)) {
-    const uint32_t *cl = v.cand + nn * v.cand_cap;
-    const int nc = v.cand_n[nn];
-    for (int c = 0; c < nc; ++c) {
-      const uint32_t m = cl[c];
+    CandWalk walk(v, nn);
+    uint32_t m;
+    while (walk.next(m)) {
       if (m >= P.g0 && m < P.g0 + P.n) continue;
       const uint32_t km = v.pid[m];
       const uint32_t a = km < k ? km : k, b = km < k ? k : km;
@@ -322,7 +320,7 @@ __global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_
     DevPart &P = v.parts[k];
     const uint32_t sim = P.sim;
     EndPre pre;
-    if (v.rec) end_pre_fp32c(v, k, P.g0, P, pre);
+    if (v.rec) end_pre_fp32c(v, k, P.anchor, P, pre);
     const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);  // this step's bound
     const DevSimState &st = v.ss[sim];
     const DevSimParams &sp = v.sp[sim];
@@ -699,9 +697,16 @@ __global__ void k_init_lrtb_fin(DevView v) {
     const DevPart &P = v.parts[k];
     const DevSimState &st = v.ss[P.sim];
     double *an = const_cast<double *>(v.anchor) + 3 * (uint64_t)k;
-    an[0] = v.disp[P.g0];
-    an[1] = v.disp[P.g0 + v.Ncap];
-    an[2] = v.disp[P.g0 + 2 * v.Ncap];
+    an[0] = v.disp[P.anchor];
+    an[1] = v.disp[P.anchor + v.Ncap];
+    an[2] = v.disp[P.anchor + 2 * v.Ncap];
+    // the breaking band from the anchor-relative extent of the current positions
+    double ext = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      const double A = P.anchor_pos[c] + an[c];
+      ext = fmax(ext, fmax(fabs(v.lrtb[6 * (uint64_t)k + c] - A), fabs(v.lrtb[6 * (uint64_t)k + 3 + c] - A)));
+    }
+    set_break_band(v.parts[k], u_extent(P, ext * (1.0 + 1e-6)));
     unsigned int *Lf = v.lrtb_local_next + 6 * (uint64_t)k;
     float *wl = v.wall_local + 6 * (uint64_t)k;
     for (int c = 0; c < 3; ++c) {
