@@ -146,6 +146,8 @@ SIGNATURES = [
     ("pd_get_sim_state", C.c_int, [_P, _u32, _P, _P, _P, _P]),
     ("pd_get_sim_disp", C.c_int, [_P, _u32, _P]),
     ("pd_get_sim_wall", C.c_int, [_P, _u32, _P, _P]),
+    ("pd_save_sim", C.c_int, [_P, _u32, _P, _u64, C.POINTER(_u64)]),
+    ("pd_load_sim", C.c_int, [_P, _u32, _P, _u64]),
     ("pd_query_pairs", C.c_int, [_P, _P, _P, _u32, _P, _u64, _P]),
     ("pd_pairs_error", C.c_char_p, []),
 ]

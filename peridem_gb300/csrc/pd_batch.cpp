@@ -43,7 +43,7 @@ uint64_t Engine::estimate_bytes(const std::vector<HostSim> &sims, int precision,
   }
   const uint64_t C = up32(N), nsl = C / 32;
   std::vector<uint32_t> file_of, node_of, deg_file;
-  order_nodes(sims, file_of, node_of, deg_file, bad);
+  order_nodes(sims, file_of, node_of, deg_file, bad, nullptr, order_bin(precision));
   std::vector<uint32_t> deg(C, 0);
   for (uint64_t n = 0; n < N; ++n) deg[n] = deg_file[file_of[n]];
   uint64_t E = 0;
@@ -168,6 +168,274 @@ int Engine::finish_sim(uint32_t sim) {
   return PD_OK;
 }
 
+// ---- per-simulation checkpoints (eviction and re-admission) ----------------------------
+//
+// A simulation's nodes occupy one contiguous engine range whose internal order depends only on
+// its own setup (order_nodes sorts inside each particle), and its particles one contiguous
+// range; so the simulation's slices of every per-node and per-particle array are copied as
+// they are. What depends on the handle -- global node indices in the bond columns and the
+// SELL slices' live masks, the contact lists, the cell list, the work lists -- is not copied:
+// the live bonds travel as each particle's Connectivity and the rest is rebuilt by the next
+// step. The FP32 form's two displacement buffers, records and velocity buffer are saved by
+// role (completed step, predicted next step), since the two handles' buffer parity may differ.
+namespace {
+constexpr uint32_t kCkptMagic = 0x4B434450u;  // "PDCK"
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptHeader {
+  uint32_t magic, version;
+  int32_t precision, flags;  // flags: 1 pos saved (reset_partzero_y), 2 afd saved, 4 clamped disp
+  uint64_t nn, np, ncl, steps;
+  DevSimParams sp;           // the target's constants must be equal (layout fields zeroed)
+};
+
+// Mutable fields of a particle (toggles, the moving reference frame and the breaking band).
+struct CkptPart {
+  int32_t movable, breakable, stoppable, break_bonds;
+  double anchor_pos[3];
+  float snot_lo32, snot_hi32;
+  uint64_t n_nodes, n_pairs;  // the particle's size and its live pairs that follow the fixed part
+};
+
+struct Writer {
+  std::vector<uint8_t> &b;
+  void put(const void *p, size_t n) {
+    const uint8_t *c = static_cast<const uint8_t *>(p);
+    b.insert(b.end(), c, c + n);
+  }
+};
+struct Reader {
+  const uint8_t *p;
+  uint64_t n, off = 0;
+  bool get(void *dst, size_t k) {
+    if (off + k > n) return false;
+    std::memcpy(dst, p + off, k);
+    off += k;
+    return true;
+  }
+};
+
+// The simulation's constants without what depends on the handle: its place in the layout and
+// the broad phase's cell size (the contact skin, which does not change results).
+DevSimParams layout_free(DevSimParams sp) {
+  sp.p0 = 0;
+  sp.np = 0;
+  sp.node0 = 0;
+  sp.nnodes = 0;
+  sp.cell = 0;
+  sp.cand_r2 = 0;
+  return sp;
+}
+
+// Optional sections, from the simulation's own config: 1 reference positions (reset_partzero_y
+// moves them), 2 applied_force_density (a prescribed-velocity particle), 4 the FP64 form's
+// predicted displacement of clamped nodes.
+int ckpt_flags(const DevSimParams &sp, bool fused, uint64_t ncl) {
+  return (sp.reset_y ? 1 : 0) | (sp.pv_particle >= 0 ? 2 : 0) | (!fused && ncl ? 4 : 0);
+}
+}  // namespace
+
+int Engine::save_sim(uint32_t sim, std::vector<uint8_t> &out) {
+  if (sim >= S_) {
+    err = "simulation index out of range";
+    return PD_EINVAL;
+  }
+  if (finished_[sim]) {
+    err = "simulation " + std::to_string(sim) + " is finished: its device state is gone";
+    return PD_ESTATE;
+  }
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t n0 = sim_node0_[sim], nn = sim_node0_[sim + 1] - n0;
+  const uint32_t p0 = sim_p0_[sim], np = sim_p0_[sim + 1] - p0;
+  const bool fused = precision_ == PD_FP32C;
+  uint64_t c0 = 0, ncl = 0;  // the simulation's entries of the clamped list
+  for (uint64_t i = 0; i < h_clamped_.size(); ++i)
+    if (h_clamped_[i] >= n0 && h_clamped_[i] < n0 + nn) {
+      if (!ncl) c0 = i;
+      ++ncl;
+    }
+  CkptHeader h;
+  std::memset(&h, 0, sizeof(h));
+  h.magic = kCkptMagic;
+  h.version = kCkptVersion;
+  h.precision = precision_;
+  h.nn = nn;
+  h.np = np;
+  h.ncl = ncl;
+  h.steps = sim_steps_[sim];
+  PD_TRY(cpy(&h.sp, d_sp_ + sim, sizeof(DevSimParams), "read params"));
+  h.flags = ckpt_flags(h.sp, fused, ncl);
+  h.sp = layout_free(h.sp);
+  out.clear();
+  Writer w{out};
+  w.put(&h, sizeof(h));
+  std::vector<double> buf(3 * nn);
+  auto node3 = [&](const double *d) -> int {  // [3][Ncap] slice, engine order
+    for (int c = 0; c < 3; ++c)
+      PD_TRY(check(cudaMemcpyAsync(buf.data() + c * nn, d + c * Ncap_ + n0, nn * 8, cudaMemcpyDeviceToHost, stream_),
+                   "save"));
+    PD_TRY(check(cudaStreamSynchronize(stream_), "save"));
+    w.put(buf.data(), 3 * nn * 8);
+    return PD_OK;
+  };
+  PD_TRY(node3(fused ? d_dispb_[cur_ ^ 1] : d_disp_));  // the completed step
+  if (fused) PD_TRY(node3(d_dispb_[cur_]));              // the next step's prediction
+  PD_TRY(node3(d_vel_[cur_]));
+  PD_TRY(node3(d_acc_));
+  PD_TRY(node3(d_force_));
+  if (h.flags & 1) PD_TRY(node3(d_pos_));
+  if (h.flags & 2) PD_TRY(node3(d_afd_));
+  if (fused) {
+    std::vector<Rec32> r(nn);
+    PD_TRY(cpy(r.data(), d_rec_[cur_] + n0, nn * sizeof(Rec32), "save records"));
+    w.put(r.data(), nn * sizeof(Rec32));
+  }
+  std::vector<DevPart> parts(np);
+  PD_TRY(cpy(parts.data(), d_parts_ + p0, np * sizeof(DevPart), "save particles"));
+  std::vector<double> lrtb(6 * np);
+  PD_TRY(cpy(lrtb.data(), d_lrtb_ + 6ull * p0, 6 * np * 8, "save boxes"));
+  w.put(lrtb.data(), 6 * np * 8);
+  if (fused) {
+    std::vector<double> an(3 * np), ann(3 * np);
+    std::vector<float> wl(6 * np);
+    PD_TRY(cpy(an.data(), d_anchor_ + 3ull * p0, 3 * np * 8, "save anchors"));
+    PD_TRY(cpy(ann.data(), d_anchor_next_ + 3ull * p0, 3 * np * 8, "save anchors"));
+    PD_TRY(cpy(wl.data(), d_wall_local_ + 6ull * p0, 6 * np * 4, "save walls"));
+    w.put(an.data(), 3 * np * 8);
+    w.put(ann.data(), 3 * np * 8);
+    w.put(wl.data(), 6 * np * 4);
+  }
+  DevSimState ss;
+  PD_TRY(cpy(&ss, d_ss_ + sim, sizeof(ss), "save sim state"));
+  w.put(&ss, sizeof(ss));
+  if (h.flags & 4) {
+    std::vector<double> cd(3 * ncl);
+    PD_TRY(cpy(cd.data(), d_clamped_disp_ + 3 * c0, 3 * ncl * 8, "save clamped"));
+    w.put(cd.data(), 3 * ncl * 8);
+  }
+  std::vector<uint32_t> pairs;
+  for (uint32_t k = 0; k < np; ++k) {
+    uint64_t npairs = 0;
+    PD_TRY(get_connectivity(p0 + k, nullptr, 0, &npairs));
+    pairs.resize(2 * std::max<uint64_t>(npairs, 1));
+    PD_TRY(get_connectivity(p0 + k, pairs.data(), npairs, &npairs));
+    const DevPart &P = parts[k];
+    CkptPart cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.movable = P.movable;
+    cp.breakable = P.breakable;
+    cp.stoppable = P.stoppable;
+    cp.break_bonds = P.break_bonds;
+    for (int c = 0; c < 3; ++c) cp.anchor_pos[c] = P.anchor_pos[c];
+    cp.snot_lo32 = P.snot_lo32;
+    cp.snot_hi32 = P.snot_hi32;
+    cp.n_nodes = P.n;
+    cp.n_pairs = npairs;
+    w.put(&cp, sizeof(cp));
+    w.put(pairs.data(), 2 * npairs * 4);
+  }
+  return PD_OK;
+}
+
+int Engine::load_sim(uint32_t sim, const uint8_t *buf, uint64_t n) {
+  if (sim >= S_) {
+    err = "simulation index out of range";
+    return PD_EINVAL;
+  }
+  Reader r{buf, n};
+  CkptHeader h;
+  if (!r.get(&h, sizeof(h)) || h.magic != kCkptMagic || h.version != kCkptVersion) {
+    err = "not a simulation checkpoint of this library";
+    return PD_EINVAL;
+  }
+  PD_TRY(check(cudaStreamSynchronize(stream_), "sync"));
+  const uint64_t n0 = sim_node0_[sim], nn = sim_node0_[sim + 1] - n0;
+  const uint32_t p0 = sim_p0_[sim], np = sim_p0_[sim + 1] - p0;
+  const bool fused = precision_ == PD_FP32C;
+  uint64_t c0 = 0, ncl = 0;
+  for (uint64_t i = 0; i < h_clamped_.size(); ++i)
+    if (h_clamped_[i] >= n0 && h_clamped_[i] < n0 + nn) {
+      if (!ncl) c0 = i;
+      ++ncl;
+    }
+  DevSimParams sp;
+  PD_TRY(cpy(&sp, d_sp_ + sim, sizeof(sp), "read params"));
+  const int flags = ckpt_flags(sp, fused, ncl);
+  sp = layout_free(sp);
+  if (h.precision != precision_ || h.nn != nn || h.np != np || h.ncl != ncl || h.flags != flags ||
+      std::memcmp(&sp, &h.sp, sizeof(sp)) != 0) {
+    err = "checkpoint of another setup, config or precision form than simulation " + std::to_string(sim);
+    return PD_EINVAL;
+  }
+  std::vector<double> nodebuf(3 * nn);
+  auto node3 = [&](double *d) -> int {
+    if (!r.get(nodebuf.data(), 3 * nn * 8)) return PD_EINVAL;
+    for (int c = 0; c < 3; ++c)
+      PD_TRY(check(cudaMemcpyAsync(d + c * Ncap_ + n0, nodebuf.data() + c * nn, nn * 8, cudaMemcpyHostToDevice,
+                                   stream_), "load"));
+    return check(cudaStreamSynchronize(stream_), "load");
+  };
+  auto take = [&](void *dst_dev, size_t bytes, const char *what) -> int {
+    std::vector<uint8_t> tmp(bytes);
+    if (!r.get(tmp.data(), bytes)) return PD_EINVAL;
+    return cpy(dst_dev, tmp.data(), bytes, what);
+  };
+  int rc = PD_OK;
+  auto bad = [&]() {
+    err = "truncated or corrupt simulation checkpoint";
+    return PD_EINVAL;
+  };
+  if ((rc = node3(fused ? d_dispb_[cur_ ^ 1] : d_disp_)) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if (fused && (rc = node3(d_dispb_[cur_])) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if ((rc = node3(d_vel_[cur_])) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if ((rc = node3(d_acc_)) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if ((rc = node3(d_force_)) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if ((h.flags & 1) && (rc = node3(d_pos_)) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if ((h.flags & 2) && (rc = node3(d_afd_)) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if (fused && (rc = take(d_rec_[cur_] + n0, nn * sizeof(Rec32), "load records")) != PD_OK)
+    return rc == PD_EINVAL ? bad() : rc;
+  if ((rc = take(d_lrtb_ + 6ull * p0, 6 * np * 8, "load boxes")) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if (fused) {
+    if ((rc = take(d_anchor_ + 3ull * p0, 3 * np * 8, "load anchors")) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+    if ((rc = take(d_anchor_next_ + 3ull * p0, 3 * np * 8, "load anchors")) != PD_OK)
+      return rc == PD_EINVAL ? bad() : rc;
+    if ((rc = take(d_wall_local_ + 6ull * p0, 6 * np * 4, "load walls")) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  }
+  if ((rc = take(d_ss_ + sim, sizeof(DevSimState), "load sim state")) != PD_OK) return rc == PD_EINVAL ? bad() : rc;
+  if ((h.flags & 4) && (rc = take(d_clamped_disp_ + 3 * c0, 3 * ncl * 8, "load clamped")) != PD_OK)
+    return rc == PD_EINVAL ? bad() : rc;
+  std::vector<DevPart> parts(np);
+  PD_TRY(cpy(parts.data(), d_parts_ + p0, np * sizeof(DevPart), "read particles"));
+  std::vector<uint32_t> pairs;
+  for (uint32_t k = 0; k < np; ++k) {
+    CkptPart cp;
+    if (!r.get(&cp, sizeof(cp)) || cp.n_nodes != parts[k].n) return bad();
+    pairs.resize(2 * std::max<uint64_t>(cp.n_pairs, 1));
+    if (!r.get(pairs.data(), 2 * cp.n_pairs * 4)) return bad();
+    DevPart &P = parts[k];
+    P.movable = cp.movable;
+    P.breakable = cp.breakable;
+    P.stoppable = cp.stoppable;
+    P.break_bonds = cp.break_bonds;
+    for (int c = 0; c < 3; ++c) P.anchor_pos[c] = cp.anchor_pos[c];
+    P.snot_lo32 = cp.snot_lo32;
+    P.snot_hi32 = cp.snot_hi32;
+    PD_TRY(set_connectivity(p0 + k, pairs.data(), cp.n_pairs));
+  }
+  PD_TRY(cpy(d_parts_ + p0, parts.data(), np * sizeof(DevPart), "load particles"));
+  // contact lists, cell list and work lists follow from the loaded positions at the next step
+  const double big = 1e300;
+  PD_TRY(cpy(&d_cnt_->moved, &big, 8, "force rebuild"));
+  if (fused) {
+    const uint32_t one = 1;
+    PD_TRY(cpy(&d_cnt_->xall, &one, 4, "work lists"));
+  }
+  sim_steps_[sim] = h.steps;
+  finished_[sim] = 0;
+  final_[sim].clear();
+  return PD_OK;
+}
+
 }  // namespace pdg
 
 namespace {
@@ -273,6 +541,24 @@ int pd_get_sim_damage(pd_sim *s, uint32_t sim, double *damage) {
   uint32_t p0 = 0, np = 0;
   if (s->eng.sim_range(sim, &n0, &nn, &p0, &np) != PD_OK) return fail(PD_EINVAL, "simulation index out of range");
   return s->eng.get_damage(damage, n0, nn);
+}
+
+int pd_save_sim(pd_sim *s, uint32_t sim, void *buf, uint64_t cap, uint64_t *bytes) {
+  if (!s || !bytes) return fail(PD_EINVAL, "null argument");
+  std::vector<uint8_t> out;
+  int rc = s->eng.save_sim(sim, out);
+  if (rc != PD_OK) return fail(rc, s->eng.err);
+  *bytes = out.size();
+  if (!buf) return PD_OK;
+  if (cap < out.size()) return fail(PD_EINVAL, "checkpoint buffer too small");
+  std::memcpy(buf, out.data(), out.size());
+  return PD_OK;
+}
+
+int pd_load_sim(pd_sim *s, uint32_t sim, const void *buf, uint64_t bytes) {
+  if (!s || !buf) return fail(PD_EINVAL, "null argument");
+  int rc = s->eng.load_sim(sim, static_cast<const uint8_t *>(buf), bytes);
+  return rc == PD_OK ? rc : fail(rc, s->eng.err);
 }
 
 int pd_get_sim_wall(pd_sim *s, uint32_t sim, double *wall_info, double *reaction) {

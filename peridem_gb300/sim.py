@@ -158,6 +158,27 @@ class Sim:
     def restore(self):
         self._ck(lib().pd_restore(self.h))
 
+    def save_sim(self, i: int = 0) -> bytes:
+        """Checkpoint of simulation i at the current step boundary (pd_save_sim): host bytes
+        that pd_load_sim turns back into the same simulation, in this or another handle."""
+        n = C.c_uint64()
+        L = lib()
+        rc = L.pd_save_sim(self.h, i, None, 0, C.byref(n))
+        if rc != 0:
+            raise PdError(rc, L.pd_global_error().decode())
+        buf = C.create_string_buffer(n.value)
+        rc = L.pd_save_sim(self.h, i, buf, n.value, C.byref(n))
+        if rc != 0:
+            raise PdError(rc, L.pd_global_error().decode())
+        return buf.raw[:n.value]
+
+    def load_sim(self, blob: bytes, i: int = 0):
+        """Continues simulation i from a checkpoint of the same setup and config."""
+        L = lib()
+        rc = L.pd_load_sim(self.h, i, blob, len(blob))
+        if rc != 0:
+            raise PdError(rc, L.pd_global_error().decode())
+
     def live_bonds(self) -> int:
         n = C.c_uint64()
         self._ck(lib().pd_count_live_bonds(self.h, C.byref(n)))
