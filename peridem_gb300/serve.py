@@ -19,6 +19,12 @@ How it works:
     (state read back, kept for the caller, their nodes skipped from then on); a cohort whose
     members are all finished is closed and its memory returns to the budget, which admits
     the next waiting requests;
+  * compaction: a finished member's memory stays with its cohort's handle until the handle
+    closes. When requests wait that do not fit and the finished members of a cohort hold at
+    least `compact` of its bytes, the cohort's unfinished members are evicted -- saved to host
+    memory at the chunk boundary (pd_save_sim) -- and the handle is closed, so its memory
+    returns at once; the evicted members wait at the front of the queue and, once admitted,
+    continue from their checkpoints (pd_load_sim), exactly as if never interrupted;
   * failures: a cohort whose handle reports an error (a device error word, a failed read) is
     closed and its memory returned; its unfinished members are queued again, each alone, and a
     member that fails alone gets the error as its result. Other cohorts are not affected.
@@ -30,7 +36,7 @@ from __future__ import annotations
 import threading
 import time
 from collections import deque
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 
 import numpy as np
 
@@ -44,6 +50,8 @@ class Request:
     config: dict
     steps: int
     arrival: float = 0.0
+    checkpoint: bytes | None = None  # set when the request was evicted: its state at that point
+    remaining: int | None = None     # steps left after the checkpoint
 
 
 @dataclass
@@ -85,13 +93,13 @@ class Server:
 
     make_batch(setups, configs, precision) -> handle with step(n, sync=False), poll(),
     finish(i), sim_state(i), sim_wall(i), device_bytes(), close() (and sim_damage(i) with
-    keep_damage); the default is
+    keep_damage; save_sim(i) and load_sim(blob, i) for compaction); the default is
     peridem_gb300.sim.Batch. estimate(setups, precision) -> bytes (default
     peridem_gb300.sim.estimate_bytes)."""
 
     def __init__(self, precision: str = "fp32c", capacity_bytes: int | None = None, chunk_steps: int = 500,
                  max_batch: int = 32, keep_state: bool = True, make_batch=None, estimate=None, tune=None,
-                 keep_damage: bool = False):
+                 keep_damage: bool = False, compact: float = 0.5):
         if make_batch is None or estimate is None:
             from . import sim as _sim
             make_batch = make_batch or _sim.Batch
@@ -117,6 +125,10 @@ class Server:
         self.create_s: list[float] = []  # host+device time to build each cohort's handle
         self._solo: set = set()          # requests to admit alone (their cohort failed)
         self.finish_s = 0.0              # time spent reading finished simulations back
+        self.compact = float(compact)    # finished share of a cohort's bytes that allows compaction (0: never)
+        self.evictions = 0               # simulations saved to host memory and re-queued
+        self.max_resident = 0            # most cohorts resident at once
+        self._est: dict = {}
 
     # -- admission ------------------------------------------------------------------------
     def _pick(self, waiting: deque, est: dict) -> list:
@@ -142,15 +154,19 @@ class Server:
                                 self.precision)
             if self.tune and hasattr(b, "tune"):
                 b.tune(**self.tune)
+            for i, r in enumerate(reqs):  # evicted requests continue from their checkpoints
+                if r.checkpoint is not None:
+                    b.load_sim(r.checkpoint, i)
             out["batch"] = b
         except Exception as e:  # reported per request
             out["error"] = str(e)
         out["create_s"] = time.perf_counter() - t0
 
     # -- one cohort -----------------------------------------------------------------------
-    def _advance(self, c: _Cohort, results: dict, now, realtime: bool) -> bool:
+    def _advance(self, c: _Cohort, results: dict, now, realtime: bool, waiting: deque | None = None) -> bool:
         """Reads back the members that reached their step count, closes the cohort when none is
-        left, else enqueues its next chunk. Returns whether anything happened."""
+        left, compacts it when that lets waiting requests in, else enqueues its next chunk.
+        Returns whether anything happened."""
         if not c.batch.poll():
             return False
         tdone = now()
@@ -173,10 +189,39 @@ class Server:
             self.cohorts.remove(c)
             self.log.append((now(), "close", [r.rid for r in c.members]))
             return True
+        if waiting and self._should_compact(c, waiting):
+            self._evict(c, waiting, now)
+            return True
         k = min(self.chunk, min(live))
         c.batch.step(k, sync=False)
         c.remaining = [max(0, x - k) if x > 0 else 0 for x in c.remaining]
         return True
+
+    def _should_compact(self, c: _Cohort, waiting: deque) -> bool:
+        """The first waiting request does not fit, and this cohort's finished members hold at
+        least `compact` of its bytes."""
+        if self.compact <= 0 or not c.finished or not hasattr(c.batch, "save_sim"):
+            return False
+        if self._est[waiting[0].rid] <= self.capacity - self.used:
+            return False
+        done = sum(self._est[c.members[i].rid] for i in c.finished)
+        return done >= self.compact * sum(self._est[r.rid] for r in c.members)
+
+    def _evict(self, c: _Cohort, waiting: deque, now) -> None:
+        """Saves the unfinished members to host memory, closes the handle (its memory returns)
+        and puts them back at the front of the queue, in their order."""
+        back = []
+        for i, r in enumerate(c.members):
+            if i in c.finished or c.remaining[i] == 0:
+                continue
+            back.append(replace(r, checkpoint=c.batch.save_sim(i), remaining=c.remaining[i]))
+        c.batch.close()
+        self.used -= c.nbytes
+        self.cohorts.remove(c)
+        self.evictions += len(back)
+        self.log.append((now(), "evict", [r.rid for r in back]))
+        for r in reversed(back):
+            waiting.appendleft(r)
 
     def _fail(self, c: _Cohort, err: Exception, waiting: deque, results: dict, now, realtime: bool) -> None:
         """A cohort whose handle reported an error (the device error word is per handle, so the
@@ -209,6 +254,7 @@ class Server:
         otherwise all arrive at once) and returns one Result per request, in rid order."""
         reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
         est = {r.rid: int(self.estimate([r.setup], self.precision)) for r in reqs}
+        self._est = est
         results: dict[int, Result] = {}
         waiting: deque = deque()
         nxt = 0
@@ -239,7 +285,9 @@ class Server:
                     nb = int(b.device_bytes()) if hasattr(b, "device_bytes") else reserved
                     self.used += nb - reserved
                     self.peak_used = max(self.peak_used, self.used)
-                    self.cohorts.append(_Cohort(b, areqs, [r.steps for r in areqs], now(), nb))
+                    self.cohorts.append(_Cohort(b, areqs, [r.remaining if r.checkpoint is not None else r.steps
+                                                           for r in areqs], now(), nb))
+                    self.max_resident = max(self.max_resident, len(self.cohorts))
                     self.log.append((now(), "admit", [r.rid for r in areqs]))
                 else:
                     self.used -= reserved
@@ -268,7 +316,7 @@ class Server:
             # advance cohorts
             for c in list(self.cohorts):
                 try:
-                    busy |= self._advance(c, results, now, realtime)
+                    busy |= self._advance(c, results, now, realtime, waiting)
                 except Exception as e:  # a device error of this handle (PdError), a failed read
                     self._fail(c, e, waiting, results, now, realtime)
                     busy = True

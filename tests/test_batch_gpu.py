@@ -75,8 +75,10 @@ def test_estimate_equals_device_bytes(precision):
 
 
 def test_server_results_equal_alone():
+    # request 1 runs long enough that the later arrivals are admitted as other cohorts while
+    # it is still resident: results must not depend on what runs beside them
     names = ["impact_walls", "cubes_gravity", "impact_free", "toggles", "impact_walls"]
-    steps = [30, 45, 20, 28, 12]
+    steps = [30, 3000, 20, 28, 12]
     arrivals = [0.0, 0.0, 0.05, 0.15, 0.3]
     reqs = []
     for rid, (n, k, t) in enumerate(zip(names, steps, arrivals)):
@@ -95,3 +97,32 @@ def test_server_results_equal_alone():
         assert r.done >= r.arrival
     summ = serve.summarize(res, max(r.done for r in res))
     assert summ["completed"] == len(reqs) and summ["ttc_p99_s"] >= summ["ttc_p50_s"] > 0
+    assert srv.max_resident >= 2  # two cohorts were on the device at once
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_server_compaction_results_equal_alone(precision):
+    """Budget for three requests: a long one shares the first cohort with two short ones while
+    three more wait. When the short ones finish, the cohort is compacted -- the long request is
+    saved to host memory, the handle closed, and the request continues in the next cohort with
+    the waiting ones (possibly several times). Every result equals the simulation run alone, bit
+    for bit."""
+    names = ["impact_walls", "impact_free", "impact_walls", "impact_free", "impact_walls", "impact_free"]
+    steps = [90, 12, 15, 20, 25, 18]
+    reqs = []
+    for rid, (n, k) in enumerate(zip(names, steps)):
+        s, cfg = cases.CASES[n]()
+        reqs.append(serve.Request(rid, s, cfg, k, 0.0))
+    per = max(estimate_bytes([r.setup], precision) for r in reqs)
+    srv = serve.Server(precision, capacity_bytes=3 * per, chunk_steps=5, max_batch=3, keep_damage=True)
+    res = srv.run(reqs, realtime=False)
+    assert srv.evictions >= 1 and [e for e in srv.log if e[1] == "evict"]
+    assert srv.used == 0 and not srv.cohorts
+    for r, n, k in zip(res, names, steps):
+        assert r.error is None and r.steps == k
+        st, wall, conn, dmg = _alone(n, precision, k)
+        for key in ("curpos", "vel", "acc", "force"):
+            np.testing.assert_array_equal(r.state[key], st[key], err_msg=f"request {r.rid} {key}")
+        np.testing.assert_array_equal(r.wall[0], wall[0])
+        np.testing.assert_array_equal(r.wall[1], wall[1])
+        np.testing.assert_array_equal(r.damage, dmg, err_msg=f"request {r.rid} damage")

@@ -45,6 +45,12 @@ class FakeBatch:
     def device_bytes(self):
         return self.nb
 
+    def save_sim(self, i):
+        return str(self.steps[i]).encode()
+
+    def load_sim(self, blob, i):
+        self.steps[i] = int(blob.decode())
+
     def close(self):
         self.closed = True
 
@@ -201,3 +207,24 @@ def test_a_failing_request_alone_reports_its_error():
     res = srv.run(reqs, realtime=False)
     assert res[0].error is not None and res[0].state is None
     assert srv.used == 0 and not srv.cohorts
+
+
+def test_compaction_frees_finished_members_memory():
+    """A long request shares a cohort with two short ones; three more wait that do not fit. When
+    the short ones finish, the cohort is compacted: the long one is saved, the handle closed,
+    and it continues in the next cohort with the waiting requests. Every request still stops at
+    exactly its step count, the budget is never exceeded and the long request's state passes
+    through the checkpoints."""
+    reqs = [_req(0, 1000, 200), _req(1, 1000, 20), _req(2, 1000, 20)] + [_req(3 + i, 1000, 30) for i in range(3)]
+    srv = _server(3000 * BYTES_PER_NODE, chunk_steps=10, max_batch=3)
+    res = srv.run(reqs, realtime=False)
+    assert all(r.error is None for r in res)
+    assert [r.state["steps"] for r in res] == [q.steps for q in reqs]
+    ev = [e for e in srv.log if e[1] == "evict"]
+    assert ev and ev[0][2] == [0] and srv.evictions >= 1
+    assert srv.peak_used <= 3000 * BYTES_PER_NODE and srv.used == 0
+    # without compaction the waiting requests sit until the long one ends
+    srv2 = _server(3000 * BYTES_PER_NODE, chunk_steps=10, max_batch=3, compact=0)
+    res2 = srv2.run(reqs, realtime=False)
+    assert not [e for e in srv2.log if e[1] == "evict"]
+    assert [r.state["steps"] for r in res2] == [q.steps for q in reqs]
