@@ -213,14 +213,14 @@ def ref_lib() -> C.CDLL:
     return _rlib
 
 
-def _put(file: str, path: str, arr: np.ndarray):
+def _put(file: str, path: str, arr: np.ndarray, lib=None):
     arr = np.asarray(arr)
     if arr.dtype.kind == "f":
         code, arr = SHIM_F64, np.ascontiguousarray(arr, dtype=np.float64)
     else:
         code, arr = SHIM_I64, np.ascontiguousarray(arr, dtype=np.int64)
     dims = (_u64 * max(1, arr.ndim))(*arr.shape)
-    ref_lib().h5mem_put(file.encode(), path.encode(), code, arr.ndim, dims, _ptr(arr) if arr.size else None)
+    (lib or ref_lib()).h5mem_put(file.encode(), path.encode(), code, arr.ndim, dims, _ptr(arr) if arr.size else None)
 
 
 def _get(file: str, path: str, dtype=np.float64) -> np.ndarray | None:
@@ -237,36 +237,37 @@ def _get(file: str, path: str, dtype=np.float64) -> np.ndarray | None:
     return out
 
 
-def put_setup(file: str, s) -> None:
+def put_setup(file: str, s, lib=None) -> None:
     """Write a Setup into the in-memory store in the dataset layout exp_dict.py:2119-2185 writes
-    (h5py stores Python ints as int64 and scalars as (1,1) datasets)."""
+    (h5py stores Python ints as int64 and scalars as (1,1) datasets). lib: another library built
+    with the stand-in HDF5 store (default: oracle/_ref/libpd_ref.so)."""
     for p in range(s.n_particles):
         g = "P_%05d" % p
         sl = s.particle_slice(p)
         n = sl.stop - sl.start
-        _put(file, g + "/Pos", s.pos[sl])
-        _put(file, g + "/Vol", s.vol[sl].reshape(n, 1))
-        _put(file, g + "/Connectivity", s.particle_conn(p).astype(np.int64).reshape(-1, 2))
+        _put(file, g + "/Pos", s.pos[sl], lib)
+        _put(file, g + "/Vol", s.vol[sl].reshape(n, 1), lib)
+        _put(file, g + "/Connectivity", s.particle_conn(p).astype(np.int64).reshape(-1, 2), lib)
         b = s.particle_list(s.bdry_offset, s.bdry, p)
-        _put(file, g + "/bdry_nodes", np.asarray(b, np.int64).reshape(-1, 1))
+        _put(file, g + "/bdry_nodes", np.asarray(b, np.int64).reshape(-1, 1), lib)
         cl = s.particle_list(s.clamped_offset, s.clamped, p)
-        _put(file, g + "/clamped_nodes", np.asarray(cl, np.int64).reshape(-1))
+        _put(file, g + "/clamped_nodes", np.asarray(cl, np.int64).reshape(-1), lib)
         for key, arr in (("disp", s.disp), ("vel", s.vel), ("acc", s.acc), ("extforce", s.extforce)):
-            _put(file, g + "/" + key, arr[sl])
+            _put(file, g + "/" + key, arr[sl], lib)
         for key, arr in (("delta", s.delta), ("rho", s.rho), ("cnot", s.cnot), ("snot", s.snot),
                          ("torque_val", s.torque_val)):
-            _put(file, g + "/" + key, np.array([[arr[p]]], dtype=np.float64))
+            _put(file, g + "/" + key, np.array([[arr[p]]], dtype=np.float64), lib)
         for key, arr in (("torque_axis", s.torque_axis), ("movable", s.movable), ("breakable", s.breakable),
                          ("stoppable", s.stoppable)):
-            _put(file, g + "/" + key, np.array([[int(arr[p])]], dtype=np.int64))
-    _put(file, "total_particles_univ", np.array([[s.n_particles]], dtype=np.int64))
-    _put(file, "pairwise/contact_radius", np.array([[s.contact_radius]]))
-    _put(file, "pairwise/normal_stiffness", np.array([[s.normal_stiffness]]))
-    _put(file, "pairwise/damping_ratio", np.array([[s.damping_ratio]]))
-    _put(file, "pairwise/friction_coefficient", np.array([[s.friction_coefficient]]))
-    _put(file, "wall/allow_wall", np.array([[int(s.allow_wall)]], dtype=np.int64))
+            _put(file, g + "/" + key, np.array([[int(arr[p])]], dtype=np.int64), lib)
+    _put(file, "total_particles_univ", np.array([[s.n_particles]], dtype=np.int64), lib)
+    _put(file, "pairwise/contact_radius", np.array([[s.contact_radius]]), lib)
+    _put(file, "pairwise/normal_stiffness", np.array([[s.normal_stiffness]]), lib)
+    _put(file, "pairwise/damping_ratio", np.array([[s.damping_ratio]]), lib)
+    _put(file, "pairwise/friction_coefficient", np.array([[s.friction_coefficient]]), lib)
+    _put(file, "wall/allow_wall", np.array([[int(s.allow_wall)]], dtype=np.int64), lib)
     g = s.geom_wall_info if s.geom_wall_info is not None else np.zeros(1)
-    _put(file, "wall/geom_wall_info", np.asarray(g, dtype=np.float64).reshape(-1, 1))
+    _put(file, "wall/geom_wall_info", np.asarray(g, dtype=np.float64).reshape(-1, 1), lib)
 
 
 def write_conf(path: str, cfg: dict) -> None:

@@ -136,6 +136,7 @@ int pd_create_from_arrays(const pd_setup_arrays *setup, const pd_config *cfg, in
   if (rc != PD_OK) return fail_global(rc, err);
   pd_sim *s = new pd_sim();
   s->cfg = *cfg;
+  s->outdir = cfg->output_dir;  // frames go where the config says (ConfigVal::output_dir)
   rc = s->eng.init(sims, precision);
   if (rc != PD_OK) {
     std::string e = s->eng.err;
