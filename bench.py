@@ -553,6 +553,9 @@ def ours(args):
     # ---- accuracy on dynamic workloads (impact, settling), both forms on the GPU
     acc_dyn = []
     if not args.no_accuracy:
+        # config 2's particle mix breaking under the top wall: the accuracy bar under fracture
+        if args.acc_steps_crush > 0:
+            acc_dyn.append(accuracy_run("crush_contact", args.acc_steps_crush, steps=args.acc_steps_crush))
         acc_dyn.append(accuracy_run("two_sphere", args.acc_steps_c0))
         acc_dyn.append(accuracy_run("cubes125", args.acc_steps_c1, steps=args.acc_steps_c1))
         if args.acc_steps_c2 > 0:
@@ -623,6 +626,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, help="bond-kernel variant (default: autotune)")
+    ap.add_argument("--acc-steps-crush", type=int, default=2000,
+                    help="steps of the fracturing crushing accuracy case (crush_contact; 0: skip)")
     ap.add_argument("--acc-steps-c0", type=int, default=2000)
     ap.add_argument("--acc-steps-c1", type=int, default=4000)
     ap.add_argument("--acc-steps-c2", type=int, default=0, help="also compare both forms on the bench workload")
@@ -634,8 +639,8 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=500)
     ap.add_argument("--serve-burst", type=int, default=1, help="also serve the stream with every request waiting at t=0")
     ap.add_argument("--serve-max-batch", type=int, default=32)
-    ap.add_argument("--serve-fp64-sample", type=int, default=6)
-    ap.add_argument("--serve-fp64-steps", type=int, default=100)
+    ap.add_argument("--serve-fp64-sample", type=int, default=12)
+    ap.add_argument("--serve-fp64-steps", type=int, default=300)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

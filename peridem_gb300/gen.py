@@ -17,6 +17,8 @@ Named workloads (seeded):
                mm, 12 mm box whose top wall moves down at 1 m/s, dt 5e-9, 10000 steps
   notched_plate  100 x 200 x 9 mm steel plate with two 50 mm x 1.5 mm edge notches, h = 0.5 mm,
                hit between the notches by a 50 mm wide steel block at 32 m/s, dt 2e-8, 5000 steps
+  crush_contact  crush512_4m's first 16 particles on a 1.2 mm pitch, touching, pressed by the top
+               wall at 20 m/s: contact and breaking from the first steps (accuracy under fracture)
 """
 from __future__ import annotations
 
@@ -362,6 +364,18 @@ def crush512_4m(steps=10000, count=None):
     return s, cfg
 
 
+def crush_contact(count=16, steps=2000, box=9.6 * MM, wall_speed=-20.0):
+    """Config 2's particle mix in contact and breaking from the first steps: the first `count`
+    particles of crush512_4m's packing (spheres, cubes and ellipsoids at h = 0.03, 0.045 and
+    0.06 mm, dt = 3e-9 s) drawn on a 1.2 mm pitch (box 9.6 mm) instead of 1.5 mm, so that
+    neighbours touch, with the top wall started at the top of the packing and moving down at
+    |wall_speed|."""
+    s, cfg = crush512(n=8, box=box, steps=steps, dt=3e-9, hs=(0.03 * MM, 0.045 * MM, 0.06 * MM), count=count)
+    cfg.update(wall_z_max=float(s.pos[:, 2].max()) + 0.01 * MM, speed_wall_z_max=wall_speed, compute_wall_reaction=1)
+    s.meta["name"] = "crush_contact"
+    return s, cfg
+
+
 def aggregate(n_particles: int, seed: int, steps: int, wall_speed: float = -1.0, dt=5e-9, pitch=1.5 * MM,
               hs=(0.05 * MM, 0.075 * MM, 0.1 * MM), smin=0.6 * MM, smax=1.4 * MM):
     """One aggregate of the serving stream: n_particles drawn like config 2's particles, packed
@@ -399,7 +413,7 @@ def serving_stream(n: int = 256, rate: float = 4.0, seed: int = 3, pmin: int = 8
 
 
 WORKLOADS = {"two_sphere": two_sphere, "cubes125": cubes125, "crush512": crush512, "crush512_4m": crush512_4m,
-             "notched_plate": notched_plate}
+             "notched_plate": notched_plate, "crush_contact": crush_contact}
 
 
 def build_aggregate(kw: dict):

@@ -4,9 +4,10 @@ Its records hold positions and displacements as floats relative to an anchor nod
 200 mm from the anchor carries rounding of ~1e-8 m on bond lengths of 0.5 mm, and a large rigid
 rotation makes the displacements as large as the particle. The engine bounds the resulting
 stretch error per particle and step (set_break_band: extent, shortest bond, rotation-proof
-first-order bound) and re-takes every decision inside that band in FP64. Here a 200 x 1.5 x 1.5
-mm steel bar at h = 0.5 mm, at rest or rigidly rotated by 0.6 rad, has bonds at both far ends
-planted at stretches snot (1 + d), d from -0.2 to +0.2 (down to |d| = 3e-5); after one step
+first-order bound) and re-takes every decision inside that band in FP64. Here a 200 x 3 x 3
+mm steel bar at h = 0.5 mm, at rest or rigidly rotated by 0.6 or 1.3 rad, has bonds 70-100 mm
+from its centre planted at stretches snot (1 + d), d from -0.2 to +0.2 (down to |d| = 3e-5,
+four bonds per d); after one step
 (zero velocity and acceleration, so the planted stretches are the ones evaluated) both forms
 must break exactly the bonds with d > 0 (particle2.h:196-237: s > snot breaks)."""
 import numpy as np
@@ -17,7 +18,7 @@ from peridem_gb300.sim import Sim
 
 pytestmark = pytest.mark.gpu
 MM = 1e-3
-DELTAS = (2e-4, -2e-4, 3e-5, -3e-5, 1e-3, -1e-3, 5e-2, -5e-2, 0.2, -0.2)
+DELTAS = (3e-5, -3e-5, 6e-5, -6e-5, 1.2e-4, -1.2e-4, 2e-4, -2e-4, 1e-3, -1e-3, 5e-2, -5e-2, 0.2, -0.2)
 
 
 def _rot(theta):
@@ -31,7 +32,7 @@ def _rot(theta):
 def bar_with_planted_bonds(theta):
     h = 0.5 * MM
     rng = np.random.default_rng(11)
-    loc = gen.lattice("box", (200 * MM, 1.5 * MM, 1.5 * MM), h)
+    loc = gen.lattice("box", (200 * MM, 3.0 * MM, 3.0 * MM), h)
     part = gen.make_particle(loc, h, gen.STEEL, 3.0, rng, 0.05, (0.0, 0.0, 0.0))
     s = gen.finish([part], 0.5 * h, 1e-9)
     pos, conn = s.pos, s.conn.astype(np.int64)
@@ -55,7 +56,7 @@ def bar_with_planted_bonds(theta):
             continue
         planted.append((a, b, DELTAS[len(planted) % len(DELTAS)]))
         used |= near
-        if len(planted) == 2 * len(DELTAS):
+        if len(planted) == 4 * len(DELTAS):
             break
     for a, b, d in planted:
         st = snot * (1.0 + d)
@@ -72,10 +73,10 @@ def _broken(sim, s):
     return {tuple(x) for x in s.conn.tolist()} - now
 
 
-@pytest.mark.parametrize("theta", [0.0, 0.6])
+@pytest.mark.parametrize("theta", [0.0, 0.6, 1.3])
 def test_far_end_breaking_decisions_equal_fp64(theta):
     s, cfg, planted, snot = bar_with_planted_bonds(theta)
-    assert len(planted) >= len(DELTAS)
+    assert len(planted) >= 3 * len(DELTAS)
     # the planted stretches, in FP64 as the reference computes them
     for a, b, d in planted:
         xi = s.pos[b] - s.pos[a]

@@ -29,9 +29,7 @@ MM = 1e-3
 
 
 def crush_contact(steps=20):
-    s, cfg = gen.crush512(n=8, box=9.6 * MM, steps=steps, dt=3e-9, hs=(0.03 * MM, 0.045 * MM, 0.06 * MM), count=16)
-    cfg.update(wall_z_max=float(s.pos[:, 2].max()) + 0.01 * MM, speed_wall_z_max=-20.0, compute_wall_reaction=1)
-    return s, cfg
+    return gen.crush_contact(steps=steps)
 
 
 def cubes_full(steps=20):
