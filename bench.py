@@ -619,7 +619,7 @@ def main():
     ap.add_argument("--workload", default="crush512_4m")
     ap.add_argument("--fp64-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--ref-budget", type=float, default=150.0,
+    ap.add_argument("--ref-budget", type=float, default=100.0,
                     help="seconds of timed steps in --impl reference (whole steps; at least one)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
