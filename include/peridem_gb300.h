@@ -49,6 +49,9 @@ extern "C" {
 #define PD_DERR_CONTACT_OVERFLOW 4u /* more in-range contacts than the per-node cap   */
 #define PD_DERR_STAGE_TIMEOUT 8u    /* a shared-memory staging copy missed its wait limit
                                        (the block used global loads; results unaffected) */
+#define PD_DERR_BARRIER_TIMEOUT 16u /* a block of the persistent step (launch mode 3) waited
+                                       longer than 2 s at a grid barrier; the launch stopped
+                                       there and the state is not a step boundary's */
 
 /*
  * pd_config: the run parameters of `main.conf`. Field names, meanings, defaults and
@@ -233,7 +236,9 @@ int pd_close(pd_sim *sim);
  * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the default below 131,072
  * nodes, 2 the same graph with the broad-phase rebuild kernels in a conditional node, the
  * default above: fewer launches per step, but the conditional node itself costs a few
- * microseconds, which small handles feel). */
+ * microseconds, which small handles feel; 3 all steps of a pd_step call in persistent
+ * cooperative launches, for FP32C handles without reset_partzero_y, prescribed-velocity or torque
+ * particles and with statistics off -- others step as in mode 2; same results as the graphs). */
 int pd_set_tuning(pd_sim *sim, double skin_frac, uint32_t cand_cap, int threads_per_block,
                   int stats, int use_graphs);
 /* Clears the device error word after the caller has handled it. */
@@ -254,7 +259,8 @@ int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *va
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);
 /* How steps are launched: 0 separate launches, 1 one CUDA graph per step, 2 a step graph whose
- * broad-phase rebuild kernels sit in a conditional node (see pd_set_tuning). */
+ * broad-phase rebuild kernels sit in a conditional node, 3 persistent launches of up to 1024
+ * steps each (see pd_set_tuning). */
 int pd_graph_mode(const pd_sim *sim);
 /* Copy of all device state that stepping changes, and its restore (checkpoint in HBM). */
 int pd_snapshot(pd_sim *sim);

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "pd_bp.cuh"
 #include "pd_device.cuh"
 #include "pd_engine.h"
 #include "pd_math.cuh"
@@ -25,18 +26,6 @@ namespace {
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
 constexpr int kScanBlock = kScanThreads * kScanPer;
-constexpr int kMaxCand = (int)kMaxCandCap;
-constexpr uint32_t kNoKey = 0xFFFFFFFFu;  // node not in the cell list
-
-__device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double cell, long long &cx,
-                                          long long &cy, long long &cz, double &x, double &y, double &z) {
-  x = v.pos[n] + v.disp[n];
-  y = v.pos[n + v.Ncap] + v.disp[n + v.Ncap];
-  z = v.pos[n + 2 * v.Ncap] + v.disp[n + 2 * v.Ncap];
-  cx = (long long)floor(x / cell);
-  cy = (long long)floor(y / cell);
-  cz = (long long)floor(z / cell);
-}
 
 // Decide whether this step rebuilds; also zero the wall reactions of every simulation
 // (Wall.setzero_reaction at the top of each step, timeloop.h:397). Inside the step graph the
@@ -44,12 +33,8 @@ __device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double c
 __global__ void k_bp_decide(DevView v, double half_skin, cudaGraphConditionalHandle cond) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t == 0) {
-    DevCounters &c = *v.cnt;
-    double stepmax = __longlong_as_double((long long)c.stepmax_bits);
-    c.rebuild = (c.moved + stepmax > half_skin) ? 1u : 0u;
-    if (cond) cudaGraphSetConditional(cond, c.rebuild);
-    c.contacts = 0;    // per-step counters
-    c.live_bonds = 0;
+    const uint32_t rebuild = bp_decide(v, half_skin);
+    if (cond) cudaGraphSetConditional(cond, rebuild);
   }
   for (uint32_t s = t; s < v.S; s += gridDim.x * blockDim.x)
     for (int k = 0; k < 18; ++k) v.ss[s].react[k] = 0.0;
@@ -66,17 +51,7 @@ __global__ void k_bp_count(DevView v, uint32_t *count, uint32_t *key, uint32_t *
   if (!v.cnt->rebuild) return;
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.N) return;
-  const uint32_t sim = v.parts[v.pid[n]].sim;
-  if (!v.ss[sim].active) {  // finished simulations leave the cell list
-    key[n] = kNoKey;
-    return;
-  }
-  long long cx, cy, cz;
-  double x, y, z;
-  node_cell(v, n, v.sp[sim].cell, cx, cy, cz, x, y, z);
-  uint32_t kk = cell_hash(cx, cy, cz, sim, mask);
-  key[n] = kk;
-  slot[n] = atomicAdd(&count[kk], 1u);
+  bp_count_node(v, n, count, key, slot, mask);
 }
 
 // exclusive scan, phase 1: per-block scan, block totals
@@ -146,8 +121,8 @@ __global__ void k_bp_scatter(DevView v, const uint32_t *start, const uint32_t *k
                              uint32_t *sorted) {
   if (!v.cnt->rebuild) return;
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.N || key[n] == kNoKey) return;
-  sorted[start[key[n]] + slot[n]] = (uint32_t)n;
+  if (n >= v.N) return;
+  bp_scatter_node(n, start, key, slot, sorted);
 }
 
 __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t *start, const uint32_t *sorted,
@@ -155,58 +130,7 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
   if (!v.cnt->rebuild) return;
   const uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.N) return;
-  const uint32_t sim = v.parts[v.pid[n]].sim;
-  if (!v.ss[sim].active) {
-    cand_n[n] = 0;
-    return;
-  }
-  const DevSimParams &sp = v.sp[sim];
-  long long cx, cy, cz;
-  double x, y, z;
-  node_cell(v, n, sp.cell, cx, cy, cz, x, y, z);
-  uint32_t list[kMaxCand];  // file indices: the reference visits contact partners in its numbering
-  int cnt = 0;
-  bool overflow = false;
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        uint32_t kk = cell_hash(cx + dx, cy + dy, cz + dz, sim, mask);
-        uint32_t b = start[kk], e = b + count[kk];
-        for (uint32_t it = b; it < e; ++it) {
-          uint32_t m = sorted[it];
-          if (m == n) continue;
-          if (v.parts[v.pid[m]].sim != sim) continue;
-          double mx = v.pos[m] + v.disp[m];
-          double my = v.pos[m + v.Ncap] + v.disp[m + v.Ncap];
-          double mz = v.pos[m + 2 * v.Ncap] + v.disp[m + 2 * v.Ncap];
-          double ddx = mx - x, ddy = my - y, ddz = mz - z;
-          if (ddx * ddx + ddy * ddy + ddz * ddz > sp.cand_r2) continue;
-          // insert keeping ascending file order; drop duplicates (hash collisions can make
-          // two stencil cells share a bucket)
-          const uint32_t fm = v.file_of[m];
-          int pos = cnt;
-          while (pos > 0 && list[pos - 1] > fm) --pos;
-          if (pos > 0 && list[pos - 1] == fm) continue;
-          if (cnt >= (int)cap) {
-            overflow = true;
-            break;
-          }
-          for (int q = cnt; q > pos; --q) list[q] = list[q - 1];
-          list[pos] = fm;
-          ++cnt;
-        }
-      }
-  if (overflow) {
-    // more partners than the list holds: the consumers walk the cell list for this node instead
-    // (CandWalk), which gives the same partners in the same order; the host grows the lists
-    cand_n[n] = kCandCells;
-    atomicAdd(&v.cnt->cand_cells, 1u);
-  } else {
-    uint32_t *out = cand + n * cap;
-    for (int i = 0; i < cnt; ++i) out[i] = v.node_of[list[i]];
-    cand_n[n] = (uint16_t)cnt;
-  }
-  if (cnt && v.xnodes) v.xnodes[atomicAdd(&v.xcount[0], 1u)] = (uint32_t)n;  // FP32 form: work list
+  bp_candidates_node(v, n, count, start, sorted, mask, cand, cand_n, cap);
 }
 
 }  // namespace

@@ -266,16 +266,22 @@ __device__ __forceinline__ bool nonfinite(double x) {
 //    roundings add at most 3 * 2^-22 s.
 // w is 1.25 times that bound over snot (the band is set from this step's extent and used in the
 // next), and at least 1e-4. xi_min is the particle's shortest setup bond: reference positions do
-// not change, so no bond gets shorter.
+// not change, so no bond gets shorter. Written with explicit roundings (no contraction), so
+// that every translation unit computes the same band.
 __device__ __forceinline__ void set_break_band(DevPart &P, double u_max) {
   const double eps = 5.9604644775390625e-08, two_sqrt3 = 3.4641016151377544;
-  const double s = 2.0 * P.snot;
-  const double a = two_sqrt3 * eps * P.ext_p, b = two_sqrt3 * eps * u_max;
-  const double ds = (b + (2.0 + s) * a) / P.xi_min + 4.0 * eps * (2.0 + s) * (4.0 + s) + 3.0 * 4.0 * eps * s;
-  double w = 1.25 * ds / P.snot;
+  const double s = __dmul_rn(2.0, P.snot);
+  const double te = __dmul_rn(two_sqrt3, eps);
+  const double a = __dmul_rn(te, P.ext_p), b = __dmul_rn(te, u_max);
+  const double s2 = __dadd_rn(2.0, s), s4 = __dadd_rn(4.0, s);
+  const double lin = __ddiv_rn(__dadd_rn(b, __dmul_rn(s2, a)), P.xi_min);
+  const double dot = __dmul_rn(__dmul_rn(__dmul_rn(4.0, eps), s2), s4);
+  const double rcp = __dmul_rn(__dmul_rn(3.0 * 4.0, eps), s);
+  const double ds = __dadd_rn(__dadd_rn(lin, dot), rcp);
+  double w = __ddiv_rn(__dmul_rn(1.25, ds), P.snot);
   if (!(w >= 1e-4)) w = 1e-4;  // also for a particle without bonds (xi_min infinite: ds finite)
-  P.snot_lo32 = __double2float_rd(P.snot * (1.0 - w));
-  P.snot_hi32 = __double2float_ru(P.snot * (1.0 + w));
+  P.snot_lo32 = __double2float_rd(__dmul_rn(P.snot, __dadd_rn(1.0, -w)));
+  P.snot_hi32 = __double2float_ru(__dmul_rn(P.snot, __dadd_rn(1.0, w)));
 }
 
 // Largest |component| of a particle's anchor-relative displacement, bounded from the box of its
@@ -320,7 +326,7 @@ __device__ __forceinline__ void end_particle_fp32c(const DevView &v, uint32_t k,
     for (int c = 0; c < 3; ++c) {
       const float lo = fval(e.L[c]), hi = fval(e.L[3 + c]);
       const double base = e.apos[c] + e.an[c];
-      const double w = 8.0 * (double)FLT_EPSILON * fmax(fabs((double)lo), fabs((double)hi)) + 1e-30;
+      const double w = __dadd_rn(__dmul_rn(8.0 * (double)FLT_EPSILON, fmax(fabs((double)lo), fabs((double)hi))), 1e-30);
       v.lrtb[6 * (uint64_t)k + c] = base + (double)lo - w;
       v.lrtb[6 * (uint64_t)k + 3 + c] = base + (double)hi + w;
       ext = fmax(ext, fmax(fabs((double)lo), fabs((double)hi)) + w);

@@ -1,0 +1,143 @@
+// pd_end.cuh -- the end of a step: each particle's end-of-step work and the simulations'
+// advance (walls, step index, sticky toggles, broad-phase movement bookkeeping). Called by
+// k_end_step (pd_kernels.cu) and by the persistent step (pd_fp32c.cu). Products and sums are
+// written with explicit round-to-nearest intrinsics so that the arithmetic is the same in every
+// translation unit, whatever its contraction setting: one rounding per multiply and per add, as
+// in the reference's compiled CPU code.
+#ifndef PD_END_CUH
+#define PD_END_CUH
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pd_device.cuh"
+#include "pd_engine.h"
+#include "pd_math.cuh"
+
+namespace pdg {
+
+// Flags a simulation uses in step t (the sticky toggles of timeloop.h:405-464).
+__device__ __forceinline__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t) {
+  if (sp.set_torque_ts != -1 && t == (uint32_t)sp.set_torque_ts) st.torque = 1;
+  if (sp.set_fracture_ts != -1 && t == (uint32_t)sp.set_fracture_ts) st.fracture = 1;
+  if (sp.set_self_contact_ts != -1 && t == (uint32_t)sp.set_self_contact_ts) st.self_contact = 1;
+  if (sp.set_damping_ts != -1 && t == (uint32_t)sp.set_damping_ts) st.damping = 1;
+  if (sp.set_zero_wall_speed_ts != -1 && t == (uint32_t)sp.set_zero_wall_speed_ts)
+    for (int c = 0; c < 6; ++c) st.spd[c] = 0;
+  if (sp.set_fix_velocity_ts != -1 && t == (uint32_t)sp.set_fix_velocity_ts) st.vconstraint = 1;
+  if (sp.gradient_extforce) {
+    double sc = (double)t / (double)sp.extforce_maxstep;
+    if (sc > 1) sc = 1;
+    st.extf_scale = sc;
+  }
+}
+
+// One particle's end of step: its AABB (and in the FP32 form its anchors, local wall planes and
+// breaking band), the FP64 form's clamped nodes, its toggles for the next step, and the FP32
+// form's list of particles with FP64 non-bond work next step. It reads its simulation's state of
+// this step and derives the next step's wall planes and step index with the same arithmetic as
+// end_step_advance, which runs once every particle is done.
+__device__ __forceinline__ void end_step_particle(const DevView &v, uint32_t k, const uint32_t *clamped_ptr,
+                                                  const uint32_t *clamped, double *clamped_disp) {
+  DevPart &P = v.parts[k];
+  const uint32_t sim = P.sim;
+  EndPre pre;
+  if (v.rec) end_pre_fp32c(v, k, P.anchor, P, pre);
+  const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);  // this step's bound
+  const DevSimState &st = v.ss[sim];
+  const DevSimParams &sp = v.sp[sim];
+  if (st.active) {
+    double wall_next[6];
+    for (int c = 0; c < 6; ++c) wall_next[c] = __dadd_rn(st.wall[c], __dmul_rn(st.spd[c], sp.dt));  // timeloop.h:791-796
+    const uint32_t tn = st.t + 1;
+    if (v.rec) {
+      end_particle_fp32c(v, k, pre, wall_next);
+    } else {
+      unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
+      if (P.movable) {
+        for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
+      }
+      for (int c = 0; c < 3; ++c) {
+        L[c] = ord_key(INFINITY);
+        L[3 + c] = ord_key(-INFINITY);
+      }
+    }
+    // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
+    // keeps this step's predicted displacement, saved for the readback (the fused FP32 form
+    // zeroes them in its corrector and keeps this step's displacement buffer intact)
+    if (clamped_ptr && !v.fused) {
+      double jump = 0;
+      for (uint32_t c = clamped_ptr[k]; c < clamped_ptr[k + 1]; ++c) {
+        uint64_t g = clamped[c];
+        D3 d = ld3(v.disp, g, v.Ncap);
+        clamped_disp[3 * (uint64_t)c] = d.x;
+        clamped_disp[3 * (uint64_t)c + 1] = d.y;
+        clamped_disp[3 * (uint64_t)c + 2] = d.z;
+        if (P.movable) {
+          jump = fmax(jump, norm3(d));
+          st3(v.disp, g, v.Ncap, d3(0.0, 0.0, 0.0));
+          st3(v.vel_out, g, v.Ncap, d3(0.0, 0.0, 0.0));
+          st3(v.acc, g, v.Ncap, d3(0.0, 0.0, 0.0));
+        }
+      }
+      if (jump > 0) atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(jump));
+    }
+    // per-particle toggles for the next step (timeloop.h:481-498)
+    const uint32_t kl = k - sp.p0;
+    if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
+      P.movable = 1;
+    if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
+        (uint32_t)sp.set_stoppable_ts == tn)
+      P.stoppable = 1;
+    // FP32 form: does any node of this particle need FP64 non-bond work next step besides
+    // contact (which the contact-node list covers)? External force, torque, or a wall within
+    // the contact radius of the particle's box grown by this step's movement bound
+    // (k_extra32 then tests each node exactly).
+    if (v.xparts) {
+      const bool torque_next = st.torque || (sp.set_torque_ts != -1 && tn == (uint32_t)sp.set_torque_ts);
+      bool need = (P.movable && P.has_ext) || torque_next;
+      if (!need && P.movable && P.stoppable && sp.allow_wall) {
+        const double lim = __dadd_rn(__dadd_rn(__dmul_rn(sp.Rc, 1.001), __dmul_rn(2.0, move)), 1e-12);
+        const double *b = v.lrtb + 6 * (uint64_t)k;
+        for (int f = 0; f < 6 && !need; ++f) {
+          const int c = f % 3;
+          need = (b[c] - lim <= wall_next[f]) && (b[3 + c] + lim >= wall_next[f]);
+        }
+      }
+      if (need) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;
+    }
+  }
+}
+
+// After every particle's end of step: the simulations advance (walls, step index, sticky
+// toggles, timeloop.h:785-797) and the broad phase's movement bookkeeping. Threads tid of
+// nthreads share the simulations.
+__device__ __forceinline__ void end_step_advance(const DevView &v, uint32_t tid, uint32_t nthreads) {
+  for (uint32_t s = tid; s < v.S; s += nthreads) {
+    const DevSimParams &sp = v.sp[s];
+    DevSimState &st = v.ss[s];
+    if (st.active) {
+      for (int c = 0; c < 6; ++c) st.wall[c] = __dadd_rn(st.wall[c], __dmul_rn(st.spd[c], sp.dt));  // timeloop.h:791-796
+      st.t += 1;
+      apply_sim_toggles(sp, st, st.t);
+    }
+  }
+  if (tid == 0) {
+    DevCounters &c = *v.cnt;
+    double stepmax = __longlong_as_double((long long)c.stepmax_bits);
+    if (c.rebuild) {
+      // with the fused predictor, stepmax already bounds the next step's movement
+      c.moved = v.fused ? stepmax : 0.0;
+      c.rebuilds += 1;
+    } else {
+      c.moved += stepmax;
+    }
+    c.last_stepmax = stepmax;
+    c.stepmax_bits = 0;
+    c.rebuild = 0;
+    c.end_blocks = 0;
+  }
+}
+
+}  // namespace pdg
+#endif

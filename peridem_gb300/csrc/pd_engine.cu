@@ -1111,6 +1111,48 @@ int Engine::capture_graphs() {
   return PD_OK;
 }
 
+// Steps per persistent launch: a launch of a small handle stays within tens of milliseconds.
+constexpr uint32_t kPersistMaxSteps = 1024;
+
+int Engine::launch_persist_steps(uint32_t n) {
+  if (!persist_ws_) {
+    const int mb = persist_max_blocks();
+    if (mb <= 0) {
+      err = "persistent step: no resident blocks";
+      return PD_ECUDA;
+    }
+    const uint64_t want = (N_ + 127) / 128;
+    persist_blocks_ = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)mb, want));
+    PD_TRY(dalloc(this, allocs_, &persist_ws_, 1 + (uint64_t)persist_blocks_, err));
+  }
+  PersistArgs a;
+  a.v[0] = view(0);
+  a.v[1] = view(1);
+  a.cur0 = (uint32_t)cur_;
+  a.nsteps = n;
+  a.half_skin = half_skin_;
+  a.count = bp_.count;
+  a.start = bp_.start;
+  a.key = bp_.key;
+  a.slot = bp_.slot;
+  a.sorted = bp_.sorted;
+  a.bar = persist_ws_;
+  a.sums = persist_ws_ + 1;
+  a.T = 1ull << bp_.table_bits;
+  a.mask = (uint32_t)(a.T - 1);
+  a.cand = bp_.cand;
+  a.cand_n = bp_.cand_n;
+  a.cap = bp_.cand_cap;
+  a.clamped_ptr = n_clamped_ ? d_clamped_ : nullptr;
+  a.clamped = n_clamped_ ? d_clamped_ + (P_ + 1) : nullptr;
+  a.clamped_disp = d_clamped_disp_;
+  PD_TRY(check(cudaMemsetAsync(persist_ws_, 0, 4, stream_), "persistent barrier reset"));
+  PD_TRY(check(launch_persist(a, persist_blocks_, stream_), "persistent step launch"));
+  cur_ ^= (int)(n & 1);
+  steps_done_ += n;
+  return PD_OK;
+}
+
 int Engine::step(uint32_t nsteps) {
   if (grow_cand_) {  // some node walked the cell list since the last grow: longer lists from now on
     grow_cand_ = false;
@@ -1118,6 +1160,16 @@ int Engine::step(uint32_t nsteps) {
     if (cap > bp_.cand_cap) PD_TRY(set_tuning(0.0, cap, 0, -1, -1));
     uint32_t z = 0;
     PD_TRY(cpy(&d_cnt_->cand_cells, &z, 4, "reset cell-walk count"));
+  }
+  if (use_persist_ && persist_eligible()) {
+    for (uint32_t done = 0; done < nsteps;) {
+      const uint32_t n = std::min(nsteps - done, kPersistMaxSteps);
+      PD_TRY(launch_persist_steps(n));
+      done += n;
+    }
+    for (uint32_t i = 0; i < S_; ++i)
+      if (!finished_[i]) sim_steps_[i] += nsteps;
+    return PD_OK;
   }
   if (!graphs_ok_ && use_graphs_) PD_TRY(capture_graphs());
   for (uint32_t i = 0; i < nsteps; ++i) {
@@ -1425,9 +1477,15 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
     stats_ = stats != 0;
     relaunch = true;
   }
-  if (use_graphs >= 0) {  // 0: separate launches, 1: plain step graph, 2: conditional broad phase
+  if (use_graphs >= 0) {  // 0: separate launches, 1: plain step graph, 2: conditional broad phase,
+                         // 3: persistent launches (where eligible; the graph of mode 2 otherwise)
+    if (use_graphs > 3) {
+      err = "launch mode above 3";
+      return PD_EINVAL;
+    }
     use_graphs_ = use_graphs != 0;
-    use_conditional_ = use_graphs != 1;
+    use_conditional_ = use_graphs >= 2;
+    use_persist_ = use_graphs == 3;
     graphs_ok_ = false;
   }
   if (relaunch) graphs_ok_ = false;
@@ -1765,16 +1823,18 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
   variant_ = best;
   graphs_ok_ = false;
   if (chosen) *chosen = best;
-  // launch mode: the plain step graph or the one with the conditional broad phase, timed as
-  // graph replays from the same snapshot
+  // launch mode: the plain step graph, the one with the conditional broad phase or (where
+  // eligible) the persistent launch, each timed from the same snapshot
   if (use_graphs_) {
     cudaEvent_t e0, e1;
     PD_TRY(check(cudaEventCreate(&e0), "event"));
     PD_TRY(check(cudaEventCreate(&e1), "event"));
     float best_mode_ms = 1e30f;
-    bool best_cond = use_conditional_;
-    for (int mode = 1; mode <= 2; ++mode) {
-      use_conditional_ = mode == 2;
+    bool best_cond = use_conditional_, best_persist = use_persist_;
+    const int last_mode = persist_eligible() ? 3 : 2;
+    for (int mode = 1; mode <= last_mode; ++mode) {
+      use_conditional_ = mode >= 2;
+      use_persist_ = mode == 3;
       graphs_ok_ = false;
       int rc = step(2);
       if (rc == PD_OK) rc = check(cudaEventRecord(e0, stream_), "event");
@@ -1786,7 +1846,12 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
       // the conditional graph counts only if it was really captured (it falls back otherwise)
       if (rc == PD_OK && (mode == 1 || use_conditional_) && ms < best_mode_ms) {
         best_mode_ms = ms;
-        best_cond = mode == 2;
+        best_cond = mode >= 2;
+        best_persist = mode == 3;
+      }
+      if (rc != PD_OK && mode == 3) {  // a device that cannot hold the cooperative grid: not a candidate
+        cudaGetLastError();
+        rc = PD_OK;
       }
       if (rc == PD_OK) rc = restore();
       if (rc != PD_OK) {
@@ -1798,6 +1863,7 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     use_conditional_ = best_cond;
+    use_persist_ = best_persist;
     graphs_ok_ = false;
   }
   return PD_OK;

@@ -372,8 +372,16 @@ class Engine {
   uint64_t num_nodes() const { return N_; }
   uint32_t num_particles() const { return P_; }
   uint64_t steps_done() const { return steps_done_; }
-  // 0: separate launches, 1: step graph, 2: step graph with the conditional broad phase
-  int graph_mode() const { return !use_graphs_ ? 0 : (graphs_ok_ && use_conditional_ ? 2 : 1); }
+  // 0: separate launches, 1: step graph, 2: step graph with the conditional broad phase,
+  // 3: persistent launches
+  int graph_mode() const {
+    if (use_persist_ && persist_eligible()) return 3;
+    return !use_graphs_ ? 0 : (graphs_ok_ && use_conditional_ ? 2 : 1);
+  }
+  // The persistent step covers the FP32 form's step without the phases it leaves out.
+  bool persist_eligible() const {
+    return precision_ == PD_FP32C && N_ > 0 && !reset_possible_ && !pv_possible_ && !torque_possible_ && !stats_;
+  }
   cudaStream_t stream() const { return stream_; }
   int precision() const { return precision_; }
   // Device view of the state between steps (what the next step reads).
@@ -433,6 +441,10 @@ class Engine {
   bool stats_ = false;
   bool use_graphs_ = true;
   bool grow_cand_ = false;  // a sync saw nodes walking the cell list: double the lists at the next step
+  bool use_persist_ = false;        // launch mode 3 (persistent step, FP32 form)
+  uint32_t *persist_ws_ = nullptr;  // its barrier counter and scan scratch
+  uint32_t persist_blocks_ = 0;     // its grid
+  int launch_persist_steps(uint32_t n);
   bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning
                                   // mode 2); init() picks by size
   int variant_ = 18;  // FP32 bond-kernel variant; init() picks by size (the autotuner's usual choices)
@@ -501,6 +513,27 @@ class Engine {
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
   bool graphs_ok_ = false;
 };
+
+// Arguments of the persistent step (k_persist, pd_fp32c.cu): the views of the two buffer
+// parities, the steps to run and the broad phase's buffers.
+struct PersistArgs {
+  DevView v[2];
+  uint32_t cur0, nsteps;
+  double half_skin;
+  uint32_t *count, *start, *key, *slot, *sorted;
+  uint32_t *sums;  // [grid] scan scratch
+  uint32_t *bar;   // barrier arrival counter, zero at launch
+  uint64_t T;
+  uint32_t mask;
+  uint32_t *cand;
+  uint16_t *cand_n;
+  uint32_t cap;
+  const uint32_t *clamped_ptr, *clamped;
+  double *clamped_disp;
+};
+// Blocks of the persistent step that fit on the current device at once (0 on error).
+int persist_max_blocks();
+cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, cudaStream_t s);
 
 // Device build of the SELL-32 bond arrays from a strictly sorted Connectivity (pd_sell.cu).
 struct SellBuild {

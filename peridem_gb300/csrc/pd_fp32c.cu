@@ -17,7 +17,9 @@
 #include <float.h>
 #include <math.h>
 
+#include "pd_bp.cuh"
 #include "pd_device.cuh"
+#include "pd_end.cuh"
 #include "pd_engine.h"
 #include "pd_math.cuh"
 
@@ -229,23 +231,39 @@ __device__ __noinline__ void band_check(const DevView &v, uint64_t n, uint32_t q
 }
 
 // A column entry: read once per step, so it is not allocated in L1, which is left to the
-// partner records (the bond kernel's working set).
+// partner records (the bond kernel's working set). NC = 0: a coherent load, for a launch that
+// writes the entries it reads in a later step (the persistent step).
+template <int NC = 1>
 __device__ __forceinline__ uint32_t ld_col(const uint32_t *p) {
   uint32_t r;
-  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
+  if (NC)
+    asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
+  else
+    asm volatile("ld.global.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p) : "memory");
   return r;
 }
 
-// A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector.
-template <int W>
+// A partner's record: one 256-bit load (W) or two 128-bit loads of the same 32-byte sector;
+// NC = 0 as for ld_col.
+template <int W, int NC = 1>
 __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
-  if (W) {
+  if (W && NC) {
     asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
         : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(u.x), "=f"(u.y), "=f"(u.z), "=f"(u.w)
         : "l"(r));
-  } else {
+  } else if (W) {
+    asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(u.x), "=f"(u.y), "=f"(u.z), "=f"(u.w)
+                 : "l"(r)
+                 : "memory");
+  } else if (NC) {
     p = __ldg(&r->p);
     u = __ldg(&r->u);
+  } else {
+    asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w) : "l"(&r->p) : "memory");
+    asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(u.x), "=f"(u.y), "=f"(u.z), "=f"(u.w) : "l"(&r->u) : "memory");
   }
 }
 
@@ -307,14 +325,14 @@ __device__ __forceinline__ void kahan_add(Acc32 &a, float g, float yx, float yy,
 // position's terms evaluated (a broken or missing bond's are discarded), the live ones summed in
 // position order, and -- once per group, only when some live stretch exceeds the lower edge of
 // the band around snot -- the breaking decisions taken (FP32 above the band, FP64 inside it).
-template <int U, int W>
+template <int U, int W, int NC = 1>
 __device__ __forceinline__ void bond_group(const DevView &v, uint64_t nn, const Rec32 *__restrict__ rec,
                                            const float4 &pi4, const float4 &ui4, const uint32_t (&q)[U], Acc32 &a,
                                            bool brk, float slo, float shi, double snot, uint32_t *maskp,
                                            uint32_t *colw, uint32_t lane) {
   float4 pq[U], uq[U];
 #pragma unroll
-  for (int u = 0; u < U; ++u) ld_rec<W>(rec + (q[u] & kColIndex), pq[u], uq[u]);
+  for (int u = 0; u < U; ++u) ld_rec<W, NC>(rec + (q[u] & kColIndex), pq[u], uq[u]);
   BondTerms bt[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u]);
@@ -428,7 +446,7 @@ __device__ __forceinline__ void verlet_tail(const DevView &v, uint64_t nn, uint3
 // groups are loaded ahead of this group's partner records, so that the column stream's latency
 // overlaps the gathers and arithmetic of the current group; FX: the FP64 non-bond work is
 // done here (extra_force) instead of in a separate k_extra32 launch.
-template <int U, int W, int PF, int FX>
+template <int U, int W, int PF, int FX, int NC = 1>
 __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
   const bool valid = n < v.N;
   const uint64_t nn = valid ? n : 0;
@@ -439,7 +457,7 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
   const bool run = valid && st.active;
   const uint64_t C3 = v.Ncap;
   float4 pi4, ui4;
-  ld_rec<W>(v.rec + nn, pi4, ui4);
+  ld_rec<W, NC>(v.rec + nn, pi4, ui4);
   Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   uint32_t live = 0;
   if (run && movable) {
@@ -461,7 +479,7 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     for (int d = 0; d < PF; ++d) {
       if ((d + 1) * U <= dg) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) qb[d][u] = ld_col(colp + 32 * (d * U + u));
+        for (int u = 0; u < U; ++u) qb[d][u] = ld_col<NC>(colp + 32 * (d * U + u));
       }
     }
     for (; j + U <= dg; j += U) {
@@ -476,19 +494,19 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
         }
         if (j + (PF + 1) * U <= dg) {
 #pragma unroll
-          for (int u = 0; u < U; ++u) qb[PF - 1][u] = ld_col(colp + 32 * (j + PF * U + u));
+          for (int u = 0; u < U; ++u) qb[PF - 1][u] = ld_col<NC>(colp + 32 * (j + PF * U + u));
         }
       } else {
 #pragma unroll
-        for (int u = 0; u < U; ++u) q[u] = ld_col(colp + 32 * (j + u));
+        for (int u = 0; u < U; ++u) q[u] = ld_col<NC>(colp + 32 * (j + u));
       }
-      bond_group<U, W>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
+      bond_group<U, W, NC>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
     }
     if (j < dg) {  // the row's last dg - j < U positions as one group; missing ones count as broken
       uint32_t q[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? ld_col(colp + 32 * (j + u)) : kColBroken;
-      bond_group<U, W>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
+      for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? ld_col<NC>(colp + 32 * (j + u)) : kColBroken;
+      bond_group<U, W, NC>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
     }
   }
   D3 f = d3(0.0, 0.0, 0.0);
@@ -655,6 +673,195 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
   // a copy that missed its wait limit may still be writing shared memory: let it land
   if (!copy_done && threadIdx.x == 0) (void)mbar_wait_bounded(&bar, 0, kStageWaitPolls);
   __syncthreads();
+}
+
+// ---- the persistent step (small handles) ------------------------------------------------
+//
+// A handle of a few tens of thousands of nodes steps in tens of microseconds, a good part of it
+// spent between the ~10 kernels of a step graph. k_persist runs all requested steps in one
+// cooperative launch, its phases separated by grid-wide barriers: per step the bond phase (the
+// FP32 bond loop with the FP64 non-bond work fused, the corrector and the next predictor), the
+// particles' end of step, then the simulations' advance with the next step's rebuild decision;
+// the broad phase runs only in the steps that rebuild (clear, count, scan, scatter, candidates).
+// Every phase calls the same device code as the per-phase kernels (pd_bp.cuh, pd_end.cuh,
+// bond_node), so the results are those of the step graph bit for bit. Records and column entries
+// are written from one step to the next inside the launch, so they are read with coherent loads.
+//
+// The blocks meet at a barrier of their own (GridBarrier) rather than a library grid sync, so
+// that every wait is bounded: a block that waits longer than kBarrierWaitNs sets
+// PD_DERR_BARRIER_TIMEOUT and every block leaves the launch at its next barrier. The launch is
+// cooperative, so all blocks are resident at once and every barrier is reachable.
+constexpr int kPersistThreads = 128;
+constexpr uint64_t kBarrierWaitNs = 2000000000ull;  // 2 s; a phase of a small handle takes microseconds
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Arrival counter (zeroed before each launch): barrier k of the launch waits until k * gridDim.x
+// blocks have arrived. sync() returns false when the launch must stop (a wait ran out here or in
+// another block).
+struct GridBarrier {
+  uint32_t *count;
+  uint32_t *err;
+  uint32_t target;
+  __device__ bool sync() {
+    __shared__ uint32_t ok;
+    target += gridDim.x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      uint32_t seen;
+      asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(seen) : "l"(count) : "memory");
+      seen += 1;
+      const uint64_t t0 = global_ns();
+      uint32_t polls = 0, good = 1;
+      while (seen < target) {
+        if ((++polls & 255u) == 0) {
+          if (*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT) {
+            good = 0;
+            break;
+          }
+          if (global_ns() - t0 > kBarrierWaitNs) {
+            atomicOr(err, PD_DERR_BARRIER_TIMEOUT);
+            good = 0;
+            break;
+          }
+        }
+        asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(seen) : "l"(count) : "memory");
+      }
+      __threadfence();
+      if (good && (*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT)) good = 0;
+      ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+  }
+};
+
+// Sum over the block (every thread gets it).
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *sh) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[w] = x;
+  __syncthreads();
+  uint32_t s = 0;
+  for (int i = 0; i < nw; ++i) s += sh[i];
+  return s;
+}
+
+// Inclusive scan over the block; *total receives the block's sum.
+__device__ __forceinline__ uint32_t block_incl_scan(uint32_t x, uint32_t *sh, uint32_t *total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  uint32_t before = 0, tot = 0;
+  for (int i = 0; i < nw; ++i) {
+    if (i < w) before += sh[i];
+    tot += sh[i];
+  }
+  *total = tot;
+  return x + before;
+}
+
+// start[i] = count[0] + ... + count[i-1] over the cell table (T entries): each block sums its
+// contiguous range, then (after one barrier) scans it from the sum of the ranges before it.
+__device__ __forceinline__ bool persist_scan(const PersistArgs &a, GridBarrier &bar) {
+  __shared__ uint32_t sh[kPersistThreads / 32];
+  const uint64_t G = gridDim.x, R = (a.T + G - 1) / G;
+  const uint64_t lo = min((uint64_t)a.T, (uint64_t)blockIdx.x * R), hi = min((uint64_t)a.T, lo + R);
+  uint32_t s = 0;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s += a.count[i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) a.sums[blockIdx.x] = s;
+  if (!bar.sync()) return false;
+  uint32_t o = 0;
+  for (uint32_t i = threadIdx.x; i < blockIdx.x; i += blockDim.x) o += a.sums[i];
+  o = block_sum(o, sh);
+  for (uint64_t base = lo; base < hi; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const uint32_t x = i < hi ? a.count[i] : 0u;
+    uint32_t tot;
+    const uint32_t incl = block_incl_scan(x, sh, &tot);
+    if (i < hi) a.start[i] = o + incl - x;
+    o += tot;
+  }
+  return true;
+}
+
+template <int U, int PF>
+__global__ void __launch_bounds__(kPersistThreads, 3) k_persist(const __grid_constant__ PersistArgs a) {
+  GridBarrier bar{a.bar, &a.v[0].cnt->err, 0u};
+  const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
+  {  // the first step's rebuild decision; wall reactions restart (k_bp_decide)
+    const DevView &v = a.v[a.cur0 & 1];
+    if (gtid == 0) bp_decide(v, a.half_skin);
+    for (uint64_t i = gtid; i < v.S; i += gsize)
+      for (int k = 0; k < 18; ++k) v.ss[i].react[k] = 0.0;
+  }
+  if (!bar.sync()) return;
+  for (uint32_t step = 0; step < a.nsteps; ++step) {
+    const DevView &v = a.v[(a.cur0 + step) & 1];
+    if (*(volatile const uint32_t *)&v.cnt->rebuild) {  // the broad phase (pd_bp.cuh)
+      if (gtid == 0 && v.xcount) v.xcount[0] = 0;
+      for (uint64_t i = gtid; i < a.T; i += gsize) a.count[i] = 0;
+      if (!bar.sync()) return;
+      for (uint64_t n = gtid; n < v.N; n += gsize) bp_count_node(v, n, a.count, a.key, a.slot, a.mask);
+      if (!bar.sync()) return;
+      if (!persist_scan(a, bar) || !bar.sync()) return;
+      for (uint64_t n = gtid; n < v.N; n += gsize) bp_scatter_node(n, a.start, a.key, a.slot, a.sorted);
+      if (!bar.sync()) return;
+      for (uint64_t n = gtid; n < v.N; n += gsize)
+        bp_candidates_node(v, n, a.count, a.start, a.sorted, a.mask, a.cand, a.cand_n, a.cap);
+      if (!bar.sync()) return;
+    }
+    // bond phase: whole blocks walk the nodes together (the bond loop's tail is warp-collective)
+    if (gtid == 0 && v.xcount) {
+      v.xcount[1] = 0;
+      v.cnt->xall = 0;
+    }
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < v.N; base += gsize)
+      bond_node<U, 1, PF, 1, 0>(v, base + threadIdx.x);
+    if (!bar.sync()) return;
+    for (uint64_t k = gtid; k < v.P; k += gsize)
+      end_step_particle(v, (uint32_t)k, a.clamped_ptr, a.clamped, a.clamped_disp);
+    if (!bar.sync()) return;
+    if (blockIdx.x == 0) {
+      end_step_advance(v, threadIdx.x, blockDim.x);
+      if (step + 1 < a.nsteps) {  // the next step's decision and reaction restart
+        __syncthreads();
+        const DevView &vn = a.v[(a.cur0 + step + 1) & 1];
+        if (threadIdx.x == 0) bp_decide(vn, a.half_skin);
+        for (uint32_t i = threadIdx.x; i < vn.S; i += blockDim.x)
+          for (int k = 0; k < 18; ++k) vn.ss[i].react[k] = 0.0;
+      }
+    }
+    if (!bar.sync()) return;
+  }
+}
+
+// Blocks of k_persist that fit on the current device at once (its grid may not exceed them).
+int persist_max_blocks() {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persist<4, 1>, kPersistThreads, 0) != cudaSuccess)
+    return 0;
+  return sms * per;
+}
+
+cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, cudaStream_t s) {
+  void *args[] = {const_cast<PersistArgs *>(&a)};
+  return cudaLaunchCooperativeKernel((const void *)k_persist<4, 1>, dim3(grid), dim3(kPersistThreads), args, 0, s);
 }
 
 int prepare_staged_kernels(uint32_t smem_bytes) {

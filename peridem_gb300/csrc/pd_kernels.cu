@@ -18,6 +18,7 @@
 #include <string.h>
 
 #include "pd_device.cuh"
+#include "pd_end.cuh"
 #include "pd_engine.h"
 #include "pd_math.cuh"
 
@@ -292,100 +293,13 @@ void launch_step_kernel(const DevView &v, int precision, int variant, cudaStream
 // ------------------------------------------------------------------------------------
 // end of step
 
-// Flags a simulation uses in step t (the sticky toggles of timeloop.h:405-464).
-__device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t) {
-  if (sp.set_torque_ts != -1 && t == (uint32_t)sp.set_torque_ts) st.torque = 1;
-  if (sp.set_fracture_ts != -1 && t == (uint32_t)sp.set_fracture_ts) st.fracture = 1;
-  if (sp.set_self_contact_ts != -1 && t == (uint32_t)sp.set_self_contact_ts) st.self_contact = 1;
-  if (sp.set_damping_ts != -1 && t == (uint32_t)sp.set_damping_ts) st.damping = 1;
-  if (sp.set_zero_wall_speed_ts != -1 && t == (uint32_t)sp.set_zero_wall_speed_ts)
-    for (int c = 0; c < 6; ++c) st.spd[c] = 0;
-  if (sp.set_fix_velocity_ts != -1 && t == (uint32_t)sp.set_fix_velocity_ts) st.vconstraint = 1;
-  if (sp.gradient_extforce) {
-    double sc = (double)t / (double)sp.extforce_maxstep;
-    if (sc > 1) sc = 1;
-    st.extf_scale = sc;
-  }
-}
-
-// Per-particle end of step, then (last block) the simulations' advance. One kernel: the
-// particles read their simulation's state of this step and derive the next step's wall planes
-// and step index themselves, with the same arithmetic as the advance, which the last block to
-// finish applies once every other block is done reading.
-__device__ void apply_sim_toggles(const DevSimParams &sp, DevSimState &st, uint32_t t);
-
+// Per-particle end of step, then (last block) the simulations' advance (pd_end.cuh). One kernel:
+// the particles read their simulation's state of this step and derive the next step's wall
+// planes and step index themselves, with the same arithmetic as the advance, which the last block
+// to finish applies once every other block is done reading.
 __global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_t *clamped, double *clamped_disp) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < v.P) {
-    DevPart &P = v.parts[k];
-    const uint32_t sim = P.sim;
-    EndPre pre;
-    if (v.rec) end_pre_fp32c(v, k, P.anchor, P, pre);
-    const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);  // this step's bound
-    const DevSimState &st = v.ss[sim];
-    const DevSimParams &sp = v.sp[sim];
-    if (st.active) {
-      double wall_next[6];
-      for (int c = 0; c < 6; ++c) wall_next[c] = st.wall[c] + st.spd[c] * sp.dt;  // timeloop.h:791-796
-      const uint32_t tn = st.t + 1;
-      if (v.rec) {
-        end_particle_fp32c(v, k, pre, wall_next);
-      } else {
-        unsigned long long *L = reinterpret_cast<unsigned long long *>(v.lrtb_next) + 6 * (uint64_t)k;
-        if (P.movable) {
-          for (int c = 0; c < 6; ++c) v.lrtb[6 * (uint64_t)k + c] = ord_val(L[c]);
-        }
-        for (int c = 0; c < 3; ++c) {
-          L[c] = ord_key(INFINITY);
-          L[3 + c] = ord_key(-INFINITY);
-        }
-      }
-      // clamped nodes are zeroed after the corrector (timeloop.h:767-774); their CurrPos
-      // keeps this step's predicted displacement, saved for the readback (the fused FP32 form
-      // zeroes them in its corrector and keeps this step's displacement buffer intact)
-      if (clamped_ptr && !v.fused) {
-        double jump = 0;
-        for (uint32_t c = clamped_ptr[k]; c < clamped_ptr[k + 1]; ++c) {
-          uint64_t g = clamped[c];
-          D3 d = ld3(v.disp, g, v.Ncap);
-          clamped_disp[3 * (uint64_t)c] = d.x;
-          clamped_disp[3 * (uint64_t)c + 1] = d.y;
-          clamped_disp[3 * (uint64_t)c + 2] = d.z;
-          if (P.movable) {
-            jump = fmax(jump, norm3(d));
-            st3(v.disp, g, v.Ncap, d3(0.0, 0.0, 0.0));
-            st3(v.vel_out, g, v.Ncap, d3(0.0, 0.0, 0.0));
-            st3(v.acc, g, v.Ncap, d3(0.0, 0.0, 0.0));
-          }
-        }
-        if (jump > 0) atomicMax(&v.cnt->stepmax_bits, (unsigned long long)__double_as_longlong(jump));
-      }
-      // per-particle toggles for the next step (timeloop.h:481-498)
-      const uint32_t kl = k - sp.p0;
-      if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
-        P.movable = 1;
-      if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
-          (uint32_t)sp.set_stoppable_ts == tn)
-        P.stoppable = 1;
-      // FP32 form: does any node of this particle need FP64 non-bond work next step besides
-      // contact (which the contact-node list covers)? External force, torque, or a wall within
-      // the contact radius of the particle's box grown by this step's movement bound
-      // (k_extra32 then tests each node exactly).
-      if (v.xparts) {
-        const bool torque_next = st.torque || (sp.set_torque_ts != -1 && tn == (uint32_t)sp.set_torque_ts);
-        bool need = (P.movable && P.has_ext) || torque_next;
-        if (!need && P.movable && P.stoppable && sp.allow_wall) {
-          const double lim = sp.Rc * 1.001 + 2.0 * move + 1e-12;
-          const double *b = v.lrtb + 6 * (uint64_t)k;
-          for (int f = 0; f < 6 && !need; ++f) {
-            const int c = f % 3;
-            need = (b[c] - lim <= wall_next[f]) && (b[3 + c] + lim >= wall_next[f]);
-          }
-        }
-        if (need) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;
-      }
-    }
-  }
+  if (k < v.P) end_step_particle(v, k, clamped_ptr, clamped, clamped_disp);
   // the last block to finish advances the simulations and the step counters
   __shared__ bool last;
   __threadfence();
@@ -394,30 +308,7 @@ __global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_
   __syncthreads();
   if (!last) return;
   __threadfence();
-  for (uint32_t s = threadIdx.x; s < v.S; s += blockDim.x) {
-    const DevSimParams &sp = v.sp[s];
-    DevSimState &st = v.ss[s];
-    if (st.active) {
-      for (int c = 0; c < 6; ++c) st.wall[c] += st.spd[c] * sp.dt;  // timeloop.h:791-796
-      st.t += 1;
-      apply_sim_toggles(sp, st, st.t);
-    }
-  }
-  if (threadIdx.x == 0) {
-    DevCounters &c = *v.cnt;
-    double stepmax = __longlong_as_double((long long)c.stepmax_bits);
-    if (c.rebuild) {
-      // with the fused predictor, stepmax already bounds the next step's movement
-      c.moved = v.fused ? stepmax : 0.0;
-      c.rebuilds += 1;
-    } else {
-      c.moved += stepmax;
-    }
-    c.last_stepmax = stepmax;
-    c.stepmax_bits = 0;
-    c.rebuild = 0;
-    c.end_blocks = 0;
-  }
+  end_step_advance(v, threadIdx.x, blockDim.x);
 }
 
 void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
