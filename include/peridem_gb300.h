@@ -251,13 +251,22 @@ double pd_step_bytes(const pd_sim *sim);
  * returns the summed device milliseconds in phase_ms[4] = {predictor, broad phase, fused
  * force+corrector kernel, end-of-step}. */
 int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
-/* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM)
- * for steps_per_variant steps from the same snapshot of the live state, restores the state
- * and keeps the fastest; then times the two step-graph modes of pd_set_tuning the same way. Results do not depend on the variant (same per-node summation
- * order). variant_ms (may be NULL) receives pd_num_variants() timings in ms per step. */
+/* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM,
+ * lanes per node) for steps_per_variant steps from the same snapshot of the live state, restores
+ * the state and keeps the fastest; then times the launch modes of pd_set_tuning the same way (the
+ * persistent step with 1, 2 and 4 lanes per node where it applies). Results do not depend on the
+ * variant or the mode: every form sums a node's bonds in the same four chains, merged in the same
+ * order. variant_ms (may be NULL) receives pd_num_variants() timings in ms per step. */
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);
+/* Lanes per node in the bond phase of the persistent step (launch mode 3): 1, 2 or 4, or 0 to
+ * choose by size (the most lanes, up to 4, whose threads all fit on the device at once). More
+ * lanes shorten each node's chain of gathers on handles too small to fill the GPU; results do not
+ * depend on it (each node's bond sum is taken in four chains fixed by the row's positions, merged
+ * in a fixed order). pd_autotune times 1, 2 and 4. */
+int pd_set_persist_lanes(pd_sim *sim, int lanes);
+int pd_persist_lanes(const pd_sim *sim);
 /* How steps are launched: 0 separate launches, 1 one CUDA graph per step, 2 a step graph whose
  * broad-phase rebuild kernels sit in a conditional node, 3 persistent launches of up to 1024
  * steps each (see pd_set_tuning). */

@@ -120,6 +120,8 @@ SIGNATURES = [
     ("pd_count_live_bonds_noalloc", C.c_int, [_P, C.POINTER(_u64)]),
     ("pd_autotune", C.c_int, [_P, _u32, C.POINTER(C.c_int), _P]),
     ("pd_set_variant", C.c_int, [_P, C.c_int]),
+    ("pd_set_persist_lanes", C.c_int, [_P, C.c_int]),
+    ("pd_persist_lanes", C.c_int, [_P]),
     ("pd_num_variants", C.c_int, []),
     ("pd_graph_mode", C.c_int, [_P]),
     ("pd_snapshot", C.c_int, [_P]),

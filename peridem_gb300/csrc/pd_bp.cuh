@@ -119,5 +119,69 @@ __device__ __forceinline__ void bp_candidates_node(const DevView &v, uint64_t n,
   if (cnt && v.xnodes) v.xnodes[atomicAdd(&v.xcount[0], 1u)] = (uint32_t)n;  // FP32 form: work list
 }
 
+// The same list built by one warp: lane l < 27 walks stencil cell l (a bucket that several
+// stencil cells share through a hash collision is walked once, by its lowest lane), the
+// qualifying nodes' file indices are gathered in the warp's shared buffer sh (kMaxCandCap + 1
+// words) and ranked into ascending order. Lists, overflow decisions and the work list equal
+// bp_candidates_node's: each node of the simulation is found at most once, and a list overflows
+// exactly when more than cap distinct nodes qualify. All 32 lanes of the warp call it with the
+// same n.
+__device__ __forceinline__ void bp_candidates_warp(const DevView &v, uint64_t n, uint32_t lane, const uint32_t *count,
+                                                   const uint32_t *start, const uint32_t *sorted, uint32_t mask,
+                                                   uint32_t *cand, uint16_t *cand_n, uint32_t cap, uint32_t *sh) {
+  const uint32_t sim = v.parts[v.pid[n]].sim;
+  if (!v.ss[sim].active) {
+    if (lane == 0) cand_n[n] = 0;
+    return;
+  }
+  const DevSimParams &sp = v.sp[sim];
+  long long cx, cy, cz;
+  double x, y, z;
+  node_cell(v, n, sp.cell, cx, cy, cz, x, y, z);
+  uint32_t kk = 0xFFFFFFFFu;
+  if (lane < 27) {
+    const int dx = (int)(lane % 3u) - 1, dy = (int)((lane / 3u) % 3u) - 1, dz = (int)(lane / 9u) - 1;
+    kk = cell_hash(cx + dx, cy + dy, cz + dz, sim, mask);
+  }
+  const uint32_t same = __match_any_sync(0xffffffffu, kk);
+  const bool walk = lane < 27 && (uint32_t)(__ffs(same) - 1) == lane;
+  if (lane == 0) sh[kMaxCandCap] = 0;
+  __syncwarp();
+  if (walk) {
+    const uint32_t b = start[kk], e = b + count[kk];
+    for (uint32_t it = b; it < e; ++it) {
+      const uint32_t m = sorted[it];
+      if (m == n) continue;
+      if (v.parts[v.pid[m]].sim != sim) continue;
+      const double mx = v.pos[m] + v.disp[m];
+      const double my = v.pos[m + v.Ncap] + v.disp[m + v.Ncap];
+      const double mz = v.pos[m + 2 * v.Ncap] + v.disp[m + 2 * v.Ncap];
+      const double ddx = mx - x, ddy = my - y, ddz = mz - z;
+      if (ddx * ddx + ddy * ddy + ddz * ddz > sp.cand_r2) continue;
+      const uint32_t slot = atomicAdd(&sh[kMaxCandCap], 1u);
+      if (slot < cap) sh[slot] = v.file_of[m];
+    }
+  }
+  __syncwarp();
+  const uint32_t total = sh[kMaxCandCap];
+  if (total > cap) {
+    if (lane == 0) {
+      cand_n[n] = kCandCells;
+      atomicAdd(&v.cnt->cand_cells, 1u);
+    }
+  } else {
+    uint32_t *out = cand + n * cap;
+    for (uint32_t i = lane; i < total; i += 32) {
+      const uint32_t fi = sh[i];
+      uint32_t r = 0;
+      for (uint32_t j = 0; j < total; ++j) r += sh[j] < fi;
+      out[r] = v.node_of[fi];
+    }
+    if (lane == 0) cand_n[n] = (uint16_t)total;
+  }
+  if (lane == 0 && total && v.xnodes) v.xnodes[atomicAdd(&v.xcount[0], 1u)] = (uint32_t)n;
+  __syncwarp();
+}
+
 }  // namespace pdg
 #endif

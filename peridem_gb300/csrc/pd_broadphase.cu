@@ -133,6 +133,18 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
   bp_candidates_node(v, n, count, start, sorted, mask, cand, cand_n, cap);
 }
 
+// One warp per node (bp_candidates_warp): small handles, whose one-thread-per-node search is a
+// long chain of dependent loads on few warps.
+__global__ void __launch_bounds__(128) k_bp_candidates_w(DevView v, const uint32_t *count, const uint32_t *start,
+                                                         const uint32_t *sorted, uint32_t mask, uint32_t *cand,
+                                                         uint16_t *cand_n, uint32_t cap) {
+  __shared__ uint32_t sh[4][kMaxCandCap + 1];
+  if (!v.cnt->rebuild) return;
+  const uint64_t n = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (n >= v.N) return;
+  bp_candidates_warp(v, n, threadIdx.x & 31, count, start, sorted, mask, cand, cand_n, cap, sh[threadIdx.x >> 5]);
+}
+
 }  // namespace
 
 void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s) {
@@ -147,8 +159,12 @@ void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s) {
   k_scan_add<<<(unsigned)((T + 255) / 256), 256, 0, s>>>(v, bp.start, bp.block_sums, T);
   if (nblk) {
     k_bp_scatter<<<(unsigned)nblk, 256, 0, s>>>(v, bp.start, bp.key, bp.slot, bp.sorted);
-    k_bp_candidates<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask,
-                                                                  bp.cand, bp.cand_n, bp.cand_cap);
+    if (v.N <= kWarpCandNodes)
+      k_bp_candidates_w<<<(unsigned)((v.N + 3) / 4), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask, bp.cand,
+                                                                 bp.cand_n, bp.cand_cap);
+    else
+      k_bp_candidates<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask,
+                                                                    bp.cand, bp.cand_n, bp.cand_cap);
   }
 }
 

@@ -277,6 +277,13 @@ int pd_set_variant(pd_sim *s, int variant) {
 
 int pd_num_variants(void) { return pdg::num_bond_variants(); }
 
+int pd_set_persist_lanes(pd_sim *s, int lanes) {
+  if (!s) return fail_global(PD_EINVAL, "null handle");
+  return s->eng.set_persist_lanes(lanes);
+}
+
+int pd_persist_lanes(const pd_sim *s) { return s ? s->eng.persist_lanes() : -1; }
+
 int pd_graph_mode(const pd_sim *s) { return s ? s->eng.graph_mode() : -1; }
 
 int pd_snapshot(pd_sim *s) {

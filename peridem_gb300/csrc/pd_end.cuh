@@ -109,6 +109,79 @@ __device__ __forceinline__ void end_step_particle(const DevView &v, uint32_t k, 
   }
 }
 
+// The FP32 form's end_step_particle for particle k by one warp (all 32 lanes call it with the same
+// k): lane c < 3 takes coordinate c of the box, the anchors and the extent, lane f < 6 face f of
+// the box keys, the wall planes and the wall test of the work list. Every quantity is computed with
+// end_step_particle's arithmetic, so both give the same state; the warp form shortens the chain
+// of dependent loads and FP64 operations each particle waits on.
+__device__ __forceinline__ void end_particle_warp(const DevView &v, uint32_t k, uint32_t lane) {
+  const unsigned full = 0xffffffffu;
+  DevPart &P = v.parts[k];
+  const uint32_t sim = P.sim;
+  const DevSimState &st = v.ss[sim];
+  const DevSimParams &sp = v.sp[sim];
+  unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
+  const uint64_t k3 = 3 * (uint64_t)k;
+  const unsigned int key = lane < 6 ? L[lane] : 0u;
+  double an = 0.0, ann = 0.0, dn = 0.0, apos = 0.0;
+  if (lane < 3) {
+    an = v.anchor[k3 + lane];
+    ann = v.anchor_next[k3 + lane];
+    dn = v.disp_next[P.anchor + lane * v.Ncap];
+    apos = P.anchor_pos[lane];
+  }
+  const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);  // this step's bound
+  if (!st.active) return;
+  const uint32_t c = lane % 3u;
+  const double wn = lane < 6 ? __dadd_rn(st.wall[lane], __dmul_rn(st.spd[lane], sp.dt)) : 0.0;  // timeloop.h:791-796
+  const uint32_t tn = st.t + 1;
+  const int32_t movable = P.movable;
+  // box from the local-frame keys (end_particle_fp32c)
+  const unsigned int klo = __shfl_sync(full, key, c), khi = __shfl_sync(full, key, c + 3);
+  double ext = 0.0;
+  if (movable && lane < 3) {
+    const float lo = fval(klo), hi = fval(khi);
+    const double base = apos + an;
+    const double w = __dadd_rn(__dmul_rn(8.0 * (double)FLT_EPSILON, fmax(fabs((double)lo), fabs((double)hi))), 1e-30);
+    v.lrtb[6 * (uint64_t)k + lane] = base + (double)lo - w;
+    v.lrtb[6 * (uint64_t)k + 3 + lane] = base + (double)hi + w;
+    ext = fmax(fabs((double)lo), fabs((double)hi)) + w;
+  }
+  for (int o = 1; o < 4; o <<= 1) ext = fmax(ext, __shfl_xor_sync(full, ext, o));
+  if (movable && lane == 0) set_break_band(P, u_extent(P, ext));
+  if (lane < 6) L[lane] = lane < 3 ? fkey(INFINITY) : fkey(-INFINITY);
+  // wall planes of the next step in the frame of the next step's anchor
+  const double apos_c = __shfl_sync(full, apos, c), ann_c = __shfl_sync(full, ann, c);
+  if (lane < 6) v.wall_local[6 * (uint64_t)k + lane] = (float)(wn - (apos_c + ann_c));
+  if (lane < 3) {
+    const_cast<double *>(v.anchor)[k3 + lane] = ann;
+    v.anchor_next[k3 + lane] = dn;
+  }
+  // per-particle toggles for the next step (timeloop.h:481-498)
+  if (lane == 0) {
+    const uint32_t kl = k - sp.p0;
+    if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
+      P.movable = 1;
+    if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
+        (uint32_t)sp.set_stoppable_ts == tn)
+      P.stoppable = 1;
+  }
+  __syncwarp();
+  // work list of particles with FP64 non-bond work next step (end_step_particle)
+  if (v.xparts) {
+    const bool torque_next = st.torque || (sp.set_torque_ts != -1 && tn == (uint32_t)sp.set_torque_ts);
+    const int32_t mov = *(volatile int32_t *)&P.movable, stop = *(volatile int32_t *)&P.stoppable;
+    bool need = (mov && P.has_ext) || torque_next;
+    if (!need && mov && stop && sp.allow_wall) {
+      const double lim = __dadd_rn(__dadd_rn(__dmul_rn(sp.Rc, 1.001), __dmul_rn(2.0, move)), 1e-12);
+      const volatile double *b = v.lrtb + 6 * (uint64_t)k;
+      const bool hit = lane < 6 && (b[c] - lim <= wn) && (b[3 + c] + lim >= wn);
+      need = __any_sync(full, hit);
+    }
+    if (need && lane == 0) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;
+  }
+}
+
 // After every particle's end of step: the simulations advance (walls, step index, sticky
 // toggles, timeloop.h:785-797) and the broad phase's movement bookkeeping. Threads tid of
 // nthreads share the simulations.

@@ -1115,15 +1115,30 @@ int Engine::capture_graphs() {
 constexpr uint32_t kPersistMaxSteps = 1024;
 
 int Engine::launch_persist_steps(uint32_t n) {
-  if (!persist_ws_) {
-    const int mb = persist_max_blocks();
+  if (persist_lanes_ == 0) {  // the most lanes per node whose threads all fit at once, up to 4
+    const uint64_t resident = 128ull * (uint64_t)std::max(0, persist_max_blocks(4));
+    persist_lanes_ = N_ * 4 <= resident ? 4 : (N_ * 2 <= resident ? 2 : 1);
+  }
+  if (persist_grid_lanes_ != persist_lanes_) {
+    const int mb = persist_max_blocks(persist_lanes_);
     if (mb <= 0) {
       err = "persistent step: no resident blocks";
       return PD_ECUDA;
     }
-    const uint64_t want = (N_ + 127) / 128;
+    // one block per SM, or fewer where the handle has fewer warps of work than SMs
+    const uint64_t want = (N_ * (uint64_t)persist_lanes_ + 31) / 32;
     persist_blocks_ = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)mb, want));
-    PD_TRY(dalloc(this, allocs_, &persist_ws_, 1 + (uint64_t)persist_blocks_, err));
+    persist_grid_lanes_ = persist_lanes_;
+  }
+  int dev = 0, sms = 0;
+  PD_TRY(check(cudaGetDevice(&dev), "device"));
+  PD_TRY(check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
+  // two barrier words + one scan word per block; a block holds at least 32 threads, an SM 2048
+  const uint64_t max_blocks = 64ull * (uint64_t)sms;
+  if (!persist_ws_) PD_TRY(dalloc(this, allocs_, &persist_ws_, 2 + max_blocks, err));
+  if (persist_blocks_ > max_blocks) {
+    err = "persistent step: grid larger than its scratch";
+    return PD_ECUDA;
   }
   PersistArgs a;
   a.v[0] = view(0);
@@ -1137,7 +1152,7 @@ int Engine::launch_persist_steps(uint32_t n) {
   a.slot = bp_.slot;
   a.sorted = bp_.sorted;
   a.bar = persist_ws_;
-  a.sums = persist_ws_ + 1;
+  a.sums = persist_ws_ + 2;
   a.T = 1ull << bp_.table_bits;
   a.mask = (uint32_t)(a.T - 1);
   a.cand = bp_.cand;
@@ -1146,8 +1161,8 @@ int Engine::launch_persist_steps(uint32_t n) {
   a.clamped_ptr = n_clamped_ ? d_clamped_ : nullptr;
   a.clamped = n_clamped_ ? d_clamped_ + (P_ + 1) : nullptr;
   a.clamped_disp = d_clamped_disp_;
-  PD_TRY(check(cudaMemsetAsync(persist_ws_, 0, 4, stream_), "persistent barrier reset"));
-  PD_TRY(check(launch_persist(a, persist_blocks_, stream_), "persistent step launch"));
+  PD_TRY(check(cudaMemsetAsync(persist_ws_, 0, 8, stream_), "persistent barrier reset"));
+  PD_TRY(check(launch_persist(a, persist_blocks_, persist_lanes_, stream_), "persistent step launch"));
   cur_ ^= (int)(n & 1);
   steps_done_ += n;
   return PD_OK;
@@ -1788,6 +1803,16 @@ int Engine::prepare_windows() {
   return PD_OK;
 }
 
+int Engine::set_persist_lanes(int lanes) {
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4) {
+    err = "persistent lanes per node must be 0, 1, 2 or 4";
+    return PD_EINVAL;
+  }
+  persist_lanes_ = lanes;
+  persist_grid_lanes_ = 0;
+  return PD_OK;
+}
+
 int Engine::set_variant(int variant) {
   if (variant < 0 || variant >= num_bond_variants()) {
     err = "bond kernel variant out of range";
@@ -1831,10 +1856,14 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
     PD_TRY(check(cudaEventCreate(&e1), "event"));
     float best_mode_ms = 1e30f;
     bool best_cond = use_conditional_, best_persist = use_persist_;
-    const int last_mode = persist_eligible() ? 3 : 2;
+    int best_lanes = persist_lanes_;
+    // modes 1 and 2, then (where eligible) the persistent step with 1, 2 and 4 lanes per node
+    const int last_mode = persist_eligible() ? 5 : 2;
     for (int mode = 1; mode <= last_mode; ++mode) {
+      const int lanes = mode >= 3 ? (1 << (mode - 3)) : 0;
       use_conditional_ = mode >= 2;
-      use_persist_ = mode == 3;
+      use_persist_ = mode >= 3;
+      if (mode >= 3) PD_TRY(set_persist_lanes(lanes));
       graphs_ok_ = false;
       int rc = step(2);
       if (rc == PD_OK) rc = check(cudaEventRecord(e0, stream_), "event");
@@ -1847,9 +1876,10 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
       if (rc == PD_OK && (mode == 1 || use_conditional_) && ms < best_mode_ms) {
         best_mode_ms = ms;
         best_cond = mode >= 2;
-        best_persist = mode == 3;
+        best_persist = mode >= 3;
+        best_lanes = lanes;
       }
-      if (rc != PD_OK && mode == 3) {  // a device that cannot hold the cooperative grid: not a candidate
+      if (rc != PD_OK && mode >= 3) {  // a device that cannot hold the cooperative grid: not a candidate
         cudaGetLastError();
         rc = PD_OK;
       }
@@ -1864,6 +1894,7 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
     cudaEventDestroy(e1);
     use_conditional_ = best_cond;
     use_persist_ = best_persist;
+    PD_TRY(set_persist_lanes(best_persist ? best_lanes : 0));
     graphs_ok_ = false;
   }
   return PD_OK;

@@ -304,6 +304,9 @@ class Engine {
   int clear_device_errors();
   // Bond-kernel variant (FP32 form); autotune() times each on the live state and restores it.
   int set_variant(int variant);
+  // lanes per node of the persistent step's bond phase: 0 chooses by size, else 1, 2 or 4
+  int set_persist_lanes(int lanes);
+  int persist_lanes() const { return persist_lanes_; }
   int autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms);
   // Copy of every mutable device buffer (and the host step counters), and its restore.
   int snapshot();
@@ -444,6 +447,8 @@ class Engine {
   bool use_persist_ = false;        // launch mode 3 (persistent step, FP32 form)
   uint32_t *persist_ws_ = nullptr;  // its barrier counter and scan scratch
   uint32_t persist_blocks_ = 0;     // its grid
+  int persist_lanes_ = 0;           // lanes per node of its bond phase (0: chosen by size)
+  int persist_grid_lanes_ = 0;      // the lanes persist_blocks_ was sized for
   int launch_persist_steps(uint32_t n);
   bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning
                                   // mode 2); init() picks by size
@@ -514,6 +519,10 @@ class Engine {
   bool graphs_ok_ = false;
 };
 
+// Handles up to this many nodes search contact candidates with one warp per node
+// (bp_candidates_warp), larger ones with one thread per node; the lists are the same.
+constexpr uint64_t kWarpCandNodes = 1ull << 20;
+
 // Arguments of the persistent step (k_persist, pd_fp32c.cu): the views of the two buffer
 // parities, the steps to run and the broad phase's buffers.
 struct PersistArgs {
@@ -522,7 +531,7 @@ struct PersistArgs {
   double half_skin;
   uint32_t *count, *start, *key, *slot, *sorted;
   uint32_t *sums;  // [grid] scan scratch
-  uint32_t *bar;   // barrier arrival counter, zero at launch
+  uint32_t *bar;   // barrier arrival and release counters, zero at launch
   uint64_t T;
   uint32_t mask;
   uint32_t *cand;
@@ -531,9 +540,10 @@ struct PersistArgs {
   const uint32_t *clamped_ptr, *clamped;
   double *clamped_disp;
 };
-// Blocks of the persistent step that fit on the current device at once (0 on error).
-int persist_max_blocks();
-cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, cudaStream_t s);
+// Blocks of the persistent step with `lanes` lanes per node in its bond phase (1, 2 or 4) that
+// fit on the current device at once (0 on error), and its cooperative launch.
+int persist_max_blocks(int lanes);
+cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, int lanes, cudaStream_t s);
 
 // Device build of the SELL-32 bond arrays from a strictly sorted Connectivity (pd_sell.cu).
 struct SellBuild {

@@ -267,10 +267,18 @@ __device__ __forceinline__ void ld_rec(const Rec32 *r, float4 &p, float4 &u) {
   }
 }
 
-// Kahan-compensated FP32 accumulator of a node's bond force density.
+// Kahan-compensated FP32 accumulator (sum s, compensation c; the value is s - c).
 struct Acc32 {
   float sx, sy, sz, cx, cy, cz;
 };
+
+// A node's bond force density is summed in up to four chains: its row of dg positions is cut
+// into consecutive blocks of chain_len(dg) = 8 ceil(dg / 32) positions, each block is
+// Kahan-summed from zero in row order, and the blocks' sums are merged left to right with exact
+// two-sums (kahan_merge). The order depends on the row alone, so every form of the bond loop -- one
+// thread walking the row, or two or four lanes per node each taking whole blocks -- gives the same
+// bits. One thread holds only the running total and the current block's sum.
+__device__ __forceinline__ int chain_len(int dg) { return 8 * ((dg + 31) >> 5); }
 
 // Approximate reciprocal square root and reciprocal (one special-function instruction each;
 // subnormal inputs flush to zero, which never occurs for squared bond lengths).
@@ -321,15 +329,41 @@ __device__ __forceinline__ void kahan_add(Acc32 &a, float g, float yx, float yy,
   y = fmaf(g, yz, -a.cz); t = a.sz + y; a.cz = (t - a.sz) - y; a.sz = t;
 }
 
-// One load group of U positions of a node's row: the partner records are gathered, every
-// position's terms evaluated (a broken or missing bond's are discarded), the live ones summed in
-// position order, and -- once per group, only when some live stretch exceeds the lower edge of
-// the band around snot -- the breaking decisions taken (FP32 above the band, FP64 inside it).
+// (s, c) + (s2, c2) -> (S, (c + c2) - e) with S + e = s + s2 exactly (Knuth's two-sum): the
+// result does not depend on the order of the operands.
+__device__ __forceinline__ void merge1(float &s, float &c, float s2, float c2) {
+  const float S = s + s2;
+  const float bb = S - s;
+  const float e = (s - (S - bb)) + (s2 - bb);
+  c = (c + c2) - e;
+  s = S;
+}
+__device__ __forceinline__ void kahan_merge(Acc32 &a, const Acc32 &b) {
+  merge1(a.sx, a.cx, b.sx, b.cx);
+  merge1(a.sy, a.cy, b.sy, b.cy);
+  merge1(a.sz, a.cz, b.sz, b.cz);
+}
+__device__ __forceinline__ D3 acc_value(const Acc32 &a) {
+  return d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
+}
+// Lane src's accumulator, all lanes taking part.
+__device__ __forceinline__ Acc32 acc_shfl(const Acc32 &a, uint32_t src) {
+  const unsigned full = 0xffffffffu;
+  return Acc32{__shfl_sync(full, a.sx, src), __shfl_sync(full, a.sy, src), __shfl_sync(full, a.sz, src),
+               __shfl_sync(full, a.cx, src), __shfl_sync(full, a.cy, src), __shfl_sync(full, a.cz, src)};
+}
+
+// One load group of U positions of a node's row (U = 4 or 8, the group starting at a multiple of
+// U, so inside one block of the row): the partner records are gathered, every position's terms
+// evaluated (a broken or missing bond's are discarded), the live ones added to the block's sum in
+// position order, and -- once per group, only when some live stretch exceeds the lower edge of the
+// band around snot -- the breaking decisions taken (FP32 above the band, FP64 inside it).
 template <int U, int W, int NC = 1>
 __device__ __forceinline__ void bond_group(const DevView &v, uint64_t nn, const Rec32 *__restrict__ rec,
                                            const float4 &pi4, const float4 &ui4, const uint32_t (&q)[U], Acc32 &a,
                                            bool brk, float slo, float shi, double snot, uint32_t *maskp,
                                            uint32_t *colw, uint32_t lane) {
+  static_assert(U == 4 || U == 8, "groups inside one block of the row");
   float4 pq[U], uq[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) ld_rec<W, NC>(rec + (q[u] & kColIndex), pq[u], uq[u]);
@@ -458,7 +492,7 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
   const uint64_t C3 = v.Ncap;
   float4 pi4, ui4;
   ld_rec<W, NC>(v.rec + nn, pi4, ui4);
-  Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  Acc32 tot = {}, a = {};  // merged blocks so far, current block
   uint32_t live = 0;
   if (run && movable) {
     const uint32_t lane = (uint32_t)(nn & 31);
@@ -471,6 +505,8 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     const float slo = P.snot_lo32, shi = P.snot_hi32;
     const Rec32 *__restrict__ rec = v.rec;
     if (v.stats) live = row_live(colp, dg);
+    const int cl = chain_len(dg);
+    int next = cl, merged = 0;
     int j = 0;
     // column entries (index + broken flag) of the next PF groups, loaded ahead (static
     // indices only, so that the ring stays in registers)
@@ -500,18 +536,31 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
 #pragma unroll
         for (int u = 0; u < U; ++u) q[u] = ld_col<NC>(colp + 32 * (j + u));
       }
+      if (j == next) {  // a new block of the row
+        kahan_merge(tot, a);
+        a = Acc32{};
+        next += cl;
+        ++merged;
+      }
       bond_group<U, W, NC>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
     }
     if (j < dg) {  // the row's last dg - j < U positions as one group; missing ones count as broken
       uint32_t q[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) q[u] = (j + u < dg) ? ld_col<NC>(colp + 32 * (j + u)) : kColBroken;
+      if (j == next) {
+        kahan_merge(tot, a);
+        a = Acc32{};
+        ++merged;
+      }
       bond_group<U, W, NC>(v, nn, rec, pi4, ui4, q, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
     }
+    kahan_merge(tot, a);  // the last block, then the empty ones: four merges in every form
+    for (++merged; merged < 4; ++merged) kahan_merge(tot, Acc32{});
   }
   D3 f = d3(0.0, 0.0, 0.0);
   if (run) {
-    f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
+    f = acc_value(tot);
     if (FX) {  // the non-bond work of k_extra32, fused (same arithmetic, same order)
       if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
     } else if (v.extra_flag[nn]) {
@@ -524,6 +573,120 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
     for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
     if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
   }
+}
+
+// The bond loop of bond_node with L = 2 or 4 lanes per node (small handles: few nodes, long rows,
+// so few warps that each wait on a long chain). Global thread t serves node t / L; lane s of the
+// node takes whole blocks of its row (chain_len): block s with L = 4, blocks 2s and 2s + 1 with
+// L = 2, in rounds of U positions; at the end the node's first lane merges the four block sums in
+// row order, as bond_node does, so the sums are bond_node's bit for bit. The breaking decisions
+// are taken by the lane that evaluated the bond. All lanes of a warp run the same number of rounds
+// (the warp's longest block run); positions past a block's or the row's end count as broken. The
+// non-bond work and the corrector run on the node's first lane.
+template <int L, int U, int FX, int NC = 1>
+__device__ __forceinline__ void bond_node_split(const DevView &v, uint64_t t) {
+  static_assert((L == 2 || L == 4) && (U == 4 || U == 8), "two or four lanes per node, groups inside a block");
+  const unsigned full = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t sub = lane & (L - 1), first = lane - sub;
+  const uint64_t n = t / L;
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  const uint32_t k = v.pid[nn];
+  const DevPart &P = v.parts[k];
+  const int32_t movable = P.movable;
+  const DevSimState &st = v.ss[P.sim];
+  const bool run = valid && st.active;
+  const uint64_t C3 = v.Ncap;
+  float4 pi4, ui4;
+  ld_rec<1, NC>(v.rec + nn, pi4, ui4);
+  Acc32 A = {}, C = {};  // L = 2: the lane's first block once done; the current block
+  uint32_t live = 0;
+  const uint32_t lane_n = (uint32_t)(nn & 31);  // the node's lane in its 32-node slice
+  const uint64_t sbase = v.slice_ptr[nn >> 5];
+  const uint32_t *colp = v.col + sbase + lane_n;
+  uint32_t *colw = const_cast<uint32_t *>(colp);
+  uint32_t *maskp = v.mask + (sbase >> 5);
+  const int dg = (run && movable) ? (int)v.deg[nn] : 0;
+  const int cl = chain_len(dg), len = (4 / L) * cl, base = (int)sub * len;
+  const bool brk = st.fracture && P.breakable && P.break_bonds;
+  const float slo = P.snot_lo32, shi = P.snot_hi32;
+  const Rec32 *__restrict__ rec = v.rec;
+  if (v.stats && sub == 0 && dg) live = row_live(colp, dg);
+  const int rounds = (int)__reduce_max_sync(full, (unsigned)((len + U - 1) / U));
+  for (int r = 0; r < rounds; ++r) {
+    const int m0 = r * U;
+    if (L == 2 && m0 == cl) {  // the lane's second block
+      A = C;
+      C = Acc32{};
+    }
+    uint32_t q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int m = m0 + u, j = base + m;
+      q[u] = (m < len && j < dg) ? ld_col<NC>(colp + 32 * j) : kColBroken;
+    }
+    float4 pq[U], uq[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) ld_rec<1, NC>(rec + (q[u] & kColIndex), pq[u], uq[u]);
+    BondTerms bt[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (!(q[u] & kColBroken)) kahan_add(C, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
+    if (brk) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!(q[u] & kColBroken) && bt[u].str > slo) {
+          const int j = base + m0 + u;
+          if (bt[u].str > shi) cut_bond(&maskp[j], lane_n, colw + 32 * j, q[u]);
+          else band_check(v, nn, q[u], &maskp[j], lane_n, P.snot, colw + 32 * j);
+        }
+      }
+    }
+  }
+  // the four block sums in row order, merged from zero as bond_node does
+  Acc32 tot = {};
+  if (L == 4) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const Acc32 x = acc_shfl(C, first + b);
+      kahan_merge(tot, x);
+    }
+  } else {
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const Acc32 x = acc_shfl(A, first + b), y = acc_shfl(C, first + b);
+      kahan_merge(tot, x);
+      kahan_merge(tot, y);
+    }
+  }
+  const bool lead = run && sub == 0;
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (lead) {
+    f = acc_value(tot);
+    if (FX) {
+      if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
+    } else if (v.extra_flag[nn]) {
+      f = f + ld3(v.f_extra, nn, C3);
+      v.extra_flag[nn] = 0;
+    }
+  }
+  verlet_tail(v, nn, k, P, st, lead, f, pi4, ui4);
+  if (v.stats) {
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(full, live, o);
+    if (lane == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
+  }
+}
+
+template <int L, int U, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_bond32l(const __grid_constant__ DevView v) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && v.xcount) {
+    v.xcount[1] = 0;
+    v.cnt->xall = 0;
+  }
+  bond_node_split<L, U, 1>(v, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <int U, int MINB, int W, int PF, int FX>
@@ -581,7 +744,8 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
   const uint64_t C3 = v.Ncap;
   float4 pi4, ui4;
   ld_rec<1>(v.rec + nn, pi4, ui4);
-  Acc32 a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  Acc32 tot = {}, a = {};  // merged blocks so far, current block (bond_node)
+  static_assert(U == 4 || U == 8, "groups inside one block of the row");
   uint32_t live = 0;
   if (run && movable) {
     const uint32_t lane = (uint32_t)(nn & 31);
@@ -604,6 +768,8 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
         ld_rec<1>(rec + q, p, u);
       }
     };
+    const int cl = chain_len(dg);
+    int next = cl, merged = 0;
     int j = 0;
     uint32_t qb[PF][U];
 #pragma unroll
@@ -626,6 +792,12 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
 #pragma unroll
         for (int u = 0; u < U; ++u) qb[PF - 1][u] = __ldg(colp + 32 * (j + PF * U + u));
       }
+      if (j == next) {  // a new block of the row
+        kahan_merge(tot, a);
+        a = Acc32{};
+        next += cl;
+        ++merged;
+      }
       float4 pq[U], uq[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) partner(q[u] & kColIndex, pq[u], uq[u]);
@@ -644,6 +816,12 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
       }
     }
     for (; j < dg; ++j) {
+      if (j == next) {
+        kahan_merge(tot, a);
+        a = Acc32{};
+        next += cl;
+        ++merged;
+      }
       const uint32_t q = __ldg(colp + 32 * j);
       if (q & kColBroken) continue;
       float4 pq, uq;
@@ -656,10 +834,12 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
         else band_check(v, nn, q, &maskp[j], lane, P.snot, colw + 32 * j);
       }
     }
+    kahan_merge(tot, a);  // the last block, then the empty ones: four merges in every form
+    for (++merged; merged < 4; ++merged) kahan_merge(tot, Acc32{});
   }
   D3 f = d3(0.0, 0.0, 0.0);
   if (run) {
-    f = d3((double)a.sx - (double)a.cx, (double)a.sy - (double)a.cy, (double)a.sz - (double)a.cz);
+    f = acc_value(tot);
     if (v.extra_flag[nn]) {
       f = f + ld3(v.f_extra, nn, C3);
       v.extra_flag[nn] = 0;
@@ -684,14 +864,15 @@ __global__ void __launch_bounds__(kStageNodes, 1) k_bond32s(const __grid_constan
 // particles' end of step, then the simulations' advance with the next step's rebuild decision;
 // the broad phase runs only in the steps that rebuild (clear, count, scan, scatter, candidates).
 // Every phase calls the same device code as the per-phase kernels (pd_bp.cuh, pd_end.cuh,
-// bond_node), so the results are those of the step graph bit for bit. Records and column entries
+// bond_node), so the results are those of the step graph bit for bit. Per step: the bond phase,
+// a barrier, the end of step (its last block advancing the simulations), a barrier. Records and column entries
 // are written from one step to the next inside the launch, so they are read with coherent loads.
 //
 // The blocks meet at a barrier of their own (GridBarrier) rather than a library grid sync, so
 // that every wait is bounded: a block that waits longer than kBarrierWaitNs sets
 // PD_DERR_BARRIER_TIMEOUT and every block leaves the launch at its next barrier. The launch is
 // cooperative, so all blocks are resident at once and every barrier is reachable.
-constexpr int kPersistThreads = 128;
+constexpr int kPersistThreads = 512;  // one block per SM (128 registers a thread)
 constexpr uint64_t kBarrierWaitNs = 2000000000ull;  // 2 s; a phase of a small handle takes microseconds
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -700,41 +881,78 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Arrival counter (zeroed before each launch): barrier k of the launch waits until k * gridDim.x
-// blocks have arrived. sync() returns false when the launch must stop (a wait ran out here or in
-// another block).
+// Two words, zeroed before each launch: the arrival counter (barrier k of the launch waits until
+// k * gridDim.x blocks have arrived) and the release counter of barriers with a last-block action.
+// sync() and sync_last() return false when the launch must stop (a wait ran out here or in another
+// block).
 struct GridBarrier {
   uint32_t *count;
   uint32_t *err;
-  uint32_t target;
+  uint32_t target;   // arrivals the next barrier waits for
+  uint32_t release;  // last-block actions done so far
+
+  // Thread 0: bounded wait until *word >= want; false when it ran out or another block's did.
+  __device__ bool wait_for(const uint32_t *word, uint32_t want) {
+    const uint64_t t0 = global_ns();
+    uint32_t polls = 0, seen;
+    asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(seen) : "l"(word) : "memory");
+    while (seen < want) {
+      if ((++polls & 255u) == 0) {
+        if (*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT) return false;
+        if (global_ns() - t0 > kBarrierWaitNs) {
+          atomicOr(err, PD_DERR_BARRIER_TIMEOUT);
+          return false;
+        }
+      }
+      asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(seen) : "l"(word) : "memory");
+    }
+    return !(*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT);
+  }
+
+  // Thread 0: arrive; returns the number of blocks arrived so far, this one included.
+  __device__ uint32_t arrive() {
+    __threadfence();
+    uint32_t seen;
+    asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(seen) : "l"(count) : "memory");
+    return seen + 1;
+  }
+
   __device__ bool sync() {
     __shared__ uint32_t ok;
     target += gridDim.x;
     __syncthreads();
     if (threadIdx.x == 0) {
+      const uint32_t seen = arrive();
+      ok = (seen >= target || wait_for(count, target)) ? 1u : 0u;
       __threadfence();
-      uint32_t seen;
-      asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(seen) : "l"(count) : "memory");
-      seen += 1;
-      const uint64_t t0 = global_ns();
-      uint32_t polls = 0, good = 1;
-      while (seen < target) {
-        if ((++polls & 255u) == 0) {
-          if (*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT) {
-            good = 0;
-            break;
-          }
-          if (global_ns() - t0 > kBarrierWaitNs) {
-            atomicOr(err, PD_DERR_BARRIER_TIMEOUT);
-            good = 0;
-            break;
-          }
-        }
-        asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(seen) : "l"(count) : "memory");
+    }
+    __syncthreads();
+    return ok != 0;
+  }
+
+  // A barrier whose last block to arrive runs fn (all its threads) before any block leaves.
+  template <class F>
+  __device__ bool sync_last(F &&fn) {
+    __shared__ uint32_t last, ok;
+    target += gridDim.x;
+    ++release;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      last = arrive() == target ? 1u : 0u;
+      __threadfence();
+    }
+    __syncthreads();
+    if (last) {
+      fn();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        asm volatile("st.release.gpu.u32 [%0], %1;" ::"l"(count + 1), "r"(release) : "memory");
+        ok = !(*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT);
       }
+    } else if (threadIdx.x == 0) {
+      ok = wait_for(count + 1, release) ? 1u : 0u;
       __threadfence();
-      if (good && (*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT)) good = 0;
-      ok = good;
     }
     __syncthreads();
     return ok != 0;
@@ -797,14 +1015,22 @@ __device__ __forceinline__ bool persist_scan(const PersistArgs &a, GridBarrier &
   return true;
 }
 
-template <int U, int PF>
-__global__ void __launch_bounds__(kPersistThreads, 3) k_persist(const __grid_constant__ PersistArgs a) {
-  GridBarrier bar{a.bar, &a.v[0].cnt->err, 0u};
+template <int L>
+__global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_constant__ PersistArgs a) {
+  GridBarrier bar{a.bar, &a.v[0].cnt->err, 0u, 0u};
   const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
+  // warps are dealt round-robin over the blocks (one per SM), so that a small handle's nodes
+  // spread over every SM
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gwarp = (uint64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  const uint64_t nwarps = gsize >> 5;
   {  // the first step's rebuild decision; wall reactions restart (k_bp_decide)
     const DevView &v = a.v[a.cur0 & 1];
-    if (gtid == 0) bp_decide(v, a.half_skin);
+    if (gtid == 0) {
+      bp_decide(v, a.half_skin);
+      v.cnt->end_blocks = 0;  // the end-of-step tickets (a launch stopped at a barrier leaves them set)
+    }
     for (uint64_t i = gtid; i < v.S; i += gsize)
       for (int k = 0; k < 18; ++k) v.ss[i].react[k] = 0.0;
   }
@@ -820,48 +1046,65 @@ __global__ void __launch_bounds__(kPersistThreads, 3) k_persist(const __grid_con
       if (!persist_scan(a, bar) || !bar.sync()) return;
       for (uint64_t n = gtid; n < v.N; n += gsize) bp_scatter_node(n, a.start, a.key, a.slot, a.sorted);
       if (!bar.sync()) return;
-      for (uint64_t n = gtid; n < v.N; n += gsize)
-        bp_candidates_node(v, n, a.count, a.start, a.sorted, a.mask, a.cand, a.cand_n, a.cap);
+      {  // one warp per node
+        __shared__ uint32_t csh[kPersistThreads / 32][kMaxCandCap + 1];
+        for (uint64_t n = gwarp; n < v.N; n += nwarps)
+          bp_candidates_warp(v, n, lane, a.count, a.start, a.sorted, a.mask, a.cand, a.cand_n, a.cap,
+                             csh[threadIdx.x >> 5]);
+      }
       if (!bar.sync()) return;
     }
-    // bond phase: whole blocks walk the nodes together (the bond loop's tail is warp-collective)
+    // bond phase: whole warps take 32 threads' worth of nodes (the bond loop is warp-collective)
     if (gtid == 0 && v.xcount) {
       v.xcount[1] = 0;
       v.cnt->xall = 0;
     }
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < v.N; base += gsize)
-      bond_node<U, 1, PF, 1, 0>(v, base + threadIdx.x);
-    if (!bar.sync()) return;
-    for (uint64_t k = gtid; k < v.P; k += gsize)
-      end_step_particle(v, (uint32_t)k, a.clamped_ptr, a.clamped, a.clamped_disp);
-    if (!bar.sync()) return;
-    if (blockIdx.x == 0) {
-      end_step_advance(v, threadIdx.x, blockDim.x);
-      if (step + 1 < a.nsteps) {  // the next step's decision and reaction restart
-        __syncthreads();
-        const DevView &vn = a.v[(a.cur0 + step + 1) & 1];
-        if (threadIdx.x == 0) bp_decide(vn, a.half_skin);
-        for (uint32_t i = threadIdx.x; i < vn.S; i += blockDim.x)
-          for (int k = 0; k < 18; ++k) vn.ss[i].react[k] = 0.0;
-      }
+    if constexpr (L == 1) {
+      for (uint64_t w = gwarp; w * 32 < v.N; w += nwarps) bond_node<4, 1, 1, 1, 0>(v, w * 32 + lane);
+    } else {  // L lanes per node (bond_node_split)
+      for (uint64_t w = gwarp; w * 32 < v.N * L; w += nwarps)
+        bond_node_split<L, 4, 1, 0>(v, w * 32 + lane);
     }
     if (!bar.sync()) return;
+    // end of step, one warp per particle; the last block to arrive at the barrier advances the
+    // simulations and takes the next step's rebuild decision (k_end_step_w, k_bp_decide)
+    for (uint64_t k = gwarp; k < v.P; k += nwarps) end_particle_warp(v, (uint32_t)k, lane);
+    const bool more = step + 1 < a.nsteps;
+    const DevView &vn = a.v[(a.cur0 + step + 1) & 1];
+    if (!bar.sync_last([&] {
+          end_step_advance(v, threadIdx.x, blockDim.x);
+          if (more) {
+            __syncthreads();
+            if (threadIdx.x == 0) bp_decide(vn, a.half_skin);
+            for (uint32_t i = threadIdx.x; i < vn.S; i += blockDim.x)
+              for (int k = 0; k < 18; ++k) vn.ss[i].react[k] = 0.0;
+          }
+        }))
+      return;
+  }
+}
+
+static const void *persist_kernel(int lanes) {
+  switch (lanes) {
+    case 2: return (const void *)k_persist<2>;
+    case 4: return (const void *)k_persist<4>;
+    default: return (const void *)k_persist<1>;
   }
 }
 
 // Blocks of k_persist that fit on the current device at once (its grid may not exceed them).
-int persist_max_blocks() {
+int persist_max_blocks(int lanes) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persist<4, 1>, kPersistThreads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, persist_kernel(lanes), kPersistThreads, 0) != cudaSuccess)
     return 0;
   return sms * per;
 }
 
-cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, cudaStream_t s) {
+cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, int lanes, cudaStream_t s) {
   void *args[] = {const_cast<PersistArgs *>(&a)};
-  return cudaLaunchCooperativeKernel((const void *)k_persist<4, 1>, dim3(grid), dim3(kPersistThreads), args, 0, s);
+  return cudaLaunchCooperativeKernel(persist_kernel(lanes), dim3(grid), dim3(kPersistThreads), args, 0, s);
 }
 
 int prepare_staged_kernels(uint32_t smem_bytes) {
@@ -869,10 +1112,10 @@ int prepare_staged_kernels(uint32_t smem_bytes) {
   auto set = [&](const void *fn) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   };
-  set((const void *)k_bond32s<2, 2>);
+  set((const void *)k_bond32s<4, 1>);
   set((const void *)k_bond32s<4, 2>);
-  set((const void *)k_bond32s<2, 3>);
-  set((const void *)k_bond32s<1, 4>);
+  set((const void *)k_bond32s<4, 3>);
+  set((const void *)k_bond32s<8, 1>);
   return e == cudaSuccess ? PD_OK : PD_ECUDA;
 }
 
@@ -992,7 +1235,7 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 // Bond-kernel variants the autotuner chooses from: k_bond32 <positions per load group, min
 // blocks/SM, 256-bit record loads, column prefetch, fused non-bond work> with 128-thread blocks
 // (0-9, 18-20) and with 32/64-thread blocks (14-17), and the staged k_bond32s (10-13).
-const int kNumBondVariants = 21;
+const int kNumBondVariants = 25;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -1000,36 +1243,42 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
   const uint64_t blocks = (v.N + 127) / 128;
   if (!blocks) return;
   const unsigned b = (unsigned)blocks;
-  const bool fused_extra = (variant >= 6 && variant <= 9) || (variant >= 14 && variant <= 16) || variant == 19;
   // nothing to stage (or the ranges not computed): the plain kernel
-  if (variant >= kFirstStagedVariant && !v.win_max) variant = 3;
+  if (variant >= kFirstStagedVariant && variant < kFirstStagedVariant + 4 && !v.win_max) variant = 3;
+  const bool fused_extra = (variant >= 6 && variant <= 9) || (variant >= 14 && variant <= 16) || variant == 19 ||
+                           variant >= 21;
   if (!fused_extra) k_extra32<<<152 * 8, 128, 0, s>>>(v);
   const unsigned bs = (unsigned)((v.N + kStageNodes - 1) / kStageNodes);
   const size_t sm = (size_t)v.win_max * sizeof(Rec32);
   switch (variant) {
     case 1: k_bond32<4, 6, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
     case 2: k_bond32<4, 4, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
-    case 3: k_bond32<2, 6, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
+    case 3: k_bond32<4, 6, 1, 2, 0><<<b, 128, 0, s>>>(v); break;
     case 4: k_bond32<8, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
     case 5: k_bond32<4, 4, 1, 0, 0><<<b, 128, 0, s>>>(v); break;
     case 6: k_bond32<4, 4, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
     case 7: k_bond32<4, 4, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
     case 8: k_bond32<4, 6, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
-    case 9: k_bond32<2, 6, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
-    case 10: k_bond32s<2, 2><<<bs, kStageNodes, sm, s>>>(v); break;
+    case 9: k_bond32<4, 6, 1, 2, 1><<<b, 128, 0, s>>>(v); break;
+    case 10: k_bond32s<4, 1><<<bs, kStageNodes, sm, s>>>(v); break;
     case 11: k_bond32s<4, 2><<<bs, kStageNodes, sm, s>>>(v); break;
-    case 12: k_bond32s<2, 3><<<bs, kStageNodes, sm, s>>>(v); break;
-    case 13: k_bond32s<1, 4><<<bs, kStageNodes, sm, s>>>(v); break;
+    case 12: k_bond32s<4, 3><<<bs, kStageNodes, sm, s>>>(v); break;
+    case 13: k_bond32s<8, 1><<<bs, kStageNodes, sm, s>>>(v); break;
     // small handles: a few hundred 128-thread blocks leave some SMs one block more than others;
     // 32- and 64-thread blocks of the same kernels spread the warps evenly
     case 14: k_bond32<4, 4, 1, 1, 1><<<(unsigned)((v.N + 31) / 32), 32, 0, s>>>(v); break;
     case 15: k_bond32<4, 4, 1, 2, 1><<<(unsigned)((v.N + 31) / 32), 32, 0, s>>>(v); break;
     case 16: k_bond32<4, 4, 1, 2, 1><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
-    case 17: k_bond32<2, 6, 1, 2, 0><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
+    case 17: k_bond32<4, 6, 1, 2, 0><<<(unsigned)((v.N + 63) / 64), 64, 0, s>>>(v); break;
     // 5 blocks/SM (96 registers, no spills)
     case 18: k_bond32<4, 5, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
     case 19: k_bond32<4, 5, 1, 1, 1><<<b, 128, 0, s>>>(v); break;
-    case 20: k_bond32<3, 5, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    case 20: k_bond32<8, 5, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
+    // L lanes per node (bond_node_split): small handles
+    case 21: k_bond32l<2, 4, 4><<<(unsigned)((2 * v.N + 127) / 128), 128, 0, s>>>(v); break;
+    case 22: k_bond32l<2, 8, 4><<<(unsigned)((2 * v.N + 127) / 128), 128, 0, s>>>(v); break;
+    case 23: k_bond32l<4, 4, 4><<<(unsigned)((4 * v.N + 127) / 128), 128, 0, s>>>(v); break;
+    case 24: k_bond32l<4, 8, 4><<<(unsigned)((4 * v.N + 127) / 128), 128, 0, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }

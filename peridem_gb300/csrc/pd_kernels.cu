@@ -311,8 +311,27 @@ __global__ void k_end_step(DevView v, const uint32_t *clamped_ptr, const uint32_
   end_step_advance(v, threadIdx.x, blockDim.x);
 }
 
+// The FP32 form's end of step with one warp per particle (end_particle_warp), the last block
+// advancing the simulations as in k_end_step.
+__global__ void __launch_bounds__(128) k_end_step_w(DevView v) {
+  const uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (k < v.P) end_particle_warp(v, (uint32_t)k, threadIdx.x & 31);
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&v.cnt->end_blocks, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  end_step_advance(v, threadIdx.x, blockDim.x);
+}
+
 void launch_end_step(const DevView &v, const uint32_t *clamped, uint64_t n_clamped, double *clamped_disp,
                      cudaStream_t s) {
+  if (v.rec && v.fused) {  // FP32 form (its clamped nodes are handled by the corrector)
+    k_end_step_w<<<(v.P + 3) / 4, 128, 0, s>>>(v);
+    return;
+  }
   const uint32_t *cptr = n_clamped ? clamped : nullptr;
   const uint32_t *clist = n_clamped ? clamped + (v.P + 1) : nullptr;
   k_end_step<<<(v.P + 127) / 128, 128, 0, s>>>(v, cptr, clist, clamped_disp);

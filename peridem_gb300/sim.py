@@ -149,8 +149,16 @@ class Sim:
         self._ck(lib().pd_set_variant(self.h, int(v)))
 
     def graph_mode(self) -> int:
-        """0 separate launches, 1 step graph, 2 step graph with a conditional broad phase."""
+        """0 separate launches, 1 step graph, 2 step graph with a conditional broad phase,
+        3 persistent launches."""
         return int(lib().pd_graph_mode(self.h))
+
+    def set_persist_lanes(self, lanes: int):
+        """Lanes per node of the persistent step's bond phase (0: by size)."""
+        self._ck(lib().pd_set_persist_lanes(self.h, int(lanes)))
+
+    def persist_lanes(self) -> int:
+        return int(lib().pd_persist_lanes(self.h))
 
     def snapshot(self):
         self._ck(lib().pd_snapshot(self.h))

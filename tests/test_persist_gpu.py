@@ -45,14 +45,16 @@ def _compare(a, b, n_particles, tag):
         np.testing.assert_array_equal(a.connectivity(p), b.connectivity(p), err_msg=f"{tag} conn {p}")
 
 
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4])
 @pytest.mark.parametrize("chunks", [(25,), (7, 1, 17)])
 @pytest.mark.parametrize("name", sorted(PCASES))
-def test_persistent_step_equals_step_graph(name, chunks):
+def test_persistent_step_equals_step_graph(name, chunks, lanes):
     s, cfg = PCASES[name]()
     a = Sim(s, cfg, "fp32c")
     b = Sim(s, cfg, "fp32c")
     a.tune(graphs=1)
     b.tune(graphs=3)
+    b.set_persist_lanes(lanes)
     assert b.graph_mode() == 3
     for n in chunks:
         a.step(n)
@@ -76,6 +78,22 @@ def test_persistent_step_beyond_one_launch():
     a.step(1100)
     b.step(1100)
     _compare(a, b, s.n_particles, "1100 steps")
+    a.close()
+    b.close()
+
+
+def test_persistent_step_with_overflowing_candidate_lists():
+    """Lists of 2 candidates overflow in contact: those nodes walk the cell list, in both modes,
+    and the lists grow at the same pd_step calls."""
+    s, cfg = cases.impact_walls()
+    a = Sim(s, cfg, "fp32c")
+    b = Sim(s, cfg, "fp32c")
+    a.tune(graphs=1, cand_cap=2)
+    b.tune(graphs=3, cand_cap=2)
+    for n in (10, 10, 10):
+        a.step(n)
+        b.step(n)
+    _compare(a, b, s.n_particles, "cand_cap 2")
     a.close()
     b.close()
 
