@@ -583,9 +583,11 @@ def ours(args):
     # 6-9, 14-16 and 19), the bond kernel, k_end_step; the 7 broad-phase kernels run only in
     # rebuild steps when the step graph holds them in a conditional node, else every step
     # (exiting at once unless due)
-    per_step = 3 if (6 <= variant <= 9 or 14 <= variant <= 16 or variant == 19) else 4
+    fused = 6 <= variant <= 9 or 14 <= variant <= 16 or variant == 19 or variant >= 21
+    per_step = 3 if fused else 4
     bp = 7 * (sim.rebuilds_timed if graph_mode == 2 else K)
-    gpu_launches = per_step * K + bp
+    # the persistent step: one cooperative launch per pd_step call of up to 1024 steps
+    gpu_launches = -(-K // 1024) if graph_mode == 3 else per_step * K + bp
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -600,7 +602,8 @@ def ours(args):
         "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64, "accuracy_vs_fp64": acc,
         "accuracy_dynamic": acc_dyn, "serving": serving, "other_configs": others,
         "gpu_launches": gpu_launches, "broadphase_rebuilds_timed": sim.rebuilds_timed, "clocks": clocks,
-        "graph_mode": {0: "separate launches", 1: "step graph", 2: "step graph, conditional broad phase"}.get(graph_mode),
+        "graph_mode": {0: "separate launches", 1: "step graph", 2: "step graph, conditional broad phase",
+                       3: "persistent step"}.get(graph_mode),
     }
     sim.close()
     if r == 0:

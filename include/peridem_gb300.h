@@ -233,12 +233,15 @@ int pd_close(pd_sim *sim);
  * candidates walks the broad phase's cell list instead, and after a pd_sync that saw one the
  * next pd_step doubles the capacity, up to 64), threads per block (<= 0 keeps it), per-step
  * statistics on/off (< 0 keeps it; on adds the pair-count kernel), step launch mode
- * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the default below 131,072
+ * (< 0 keeps it; 0 separate launches, 1 one CUDA graph per step, the FP64 default below 131,072
  * nodes, 2 the same graph with the broad-phase rebuild kernels in a conditional node, the
  * default above: fewer launches per step, but the conditional node itself costs a few
  * microseconds, which small handles feel; 3 all steps of a pd_step call in persistent
- * cooperative launches, for FP32C handles without reset_partzero_y, prescribed-velocity or torque
- * particles and with statistics off -- others step as in mode 2; same results as the graphs). */
+ * cooperative launches of one block per SM (up to 1024 steps each), the FP32C default below
+ * 131,072 nodes, for handles without reset_partzero_y, prescribed-velocity or torque particles
+ * and with statistics off -- others step as in mode 2. A persistent launch occupies every SM
+ * while it runs: handles stepping concurrently on other streams wait for it, so a server of
+ * many small handles steps them with mode 1. All modes give the same results). */
 int pd_set_tuning(pd_sim *sim, double skin_frac, uint32_t cand_cap, int threads_per_block,
                   int stats, int use_graphs);
 /* Clears the device error word after the caller has handled it. */

@@ -223,6 +223,7 @@ DevSimParams layout_free(DevSimParams sp) {
   sp.node0 = 0;
   sp.nnodes = 0;
   sp.cell = 0;
+  sp.inv_cell = 0;
   sp.cand_r2 = 0;
   return sp;
 }

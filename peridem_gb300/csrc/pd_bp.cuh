@@ -16,14 +16,16 @@ namespace pdg {
 
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;  // node not in the cell list
 
-__device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double cell, long long &cx,
+// Node n's current position and cell (a cell is wider than the candidate radius, so two nodes
+// within it lie in the same or adjacent cells; CandWalk computes the cell the same way).
+__device__ __forceinline__ void node_cell(const DevView &v, uint64_t n, double inv_cell, long long &cx,
                                           long long &cy, long long &cz, double &x, double &y, double &z) {
   x = v.pos[n] + v.disp[n];
   y = v.pos[n + v.Ncap] + v.disp[n + v.Ncap];
   z = v.pos[n + 2 * v.Ncap] + v.disp[n + 2 * v.Ncap];
-  cx = (long long)floor(x / cell);
-  cy = (long long)floor(y / cell);
-  cz = (long long)floor(z / cell);
+  cx = (long long)floor(__dmul_rn(x, inv_cell));
+  cy = (long long)floor(__dmul_rn(y, inv_cell));
+  cz = (long long)floor(__dmul_rn(z, inv_cell));
 }
 
 // Whether this step rebuilds (one thread): the accumulated movement bound against half the
@@ -47,7 +49,7 @@ __device__ __forceinline__ void bp_count_node(const DevView &v, uint64_t n, uint
   }
   long long cx, cy, cz;
   double x, y, z;
-  node_cell(v, n, v.sp[sim].cell, cx, cy, cz, x, y, z);
+  node_cell(v, n, v.sp[sim].inv_cell, cx, cy, cz, x, y, z);
   const uint32_t kk = cell_hash(cx, cy, cz, sim, mask);
   key[n] = kk;
   slot[n] = atomicAdd(&count[kk], 1u);
@@ -73,7 +75,7 @@ __device__ __forceinline__ void bp_candidates_node(const DevView &v, uint64_t n,
   const DevSimParams &sp = v.sp[sim];
   long long cx, cy, cz;
   double x, y, z;
-  node_cell(v, n, sp.cell, cx, cy, cz, x, y, z);
+  node_cell(v, n, sp.inv_cell, cx, cy, cz, x, y, z);
   uint32_t list[kMaxCand];  // file indices: the reference visits contact partners in its numbering
   int cnt = 0;
   bool overflow = false;
@@ -137,7 +139,7 @@ __device__ __forceinline__ void bp_candidates_warp(const DevView &v, uint64_t n,
   const DevSimParams &sp = v.sp[sim];
   long long cx, cy, cz;
   double x, y, z;
-  node_cell(v, n, sp.cell, cx, cy, cz, x, y, z);
+  node_cell(v, n, sp.inv_cell, cx, cy, cz, x, y, z);
   uint32_t kk = 0xFFFFFFFFu;
   if (lane < 27) {
     const int dx = (int)(lane % 3u) - 1, dy = (int)((lane / 3u) % 3u) - 1, dz = (int)(lane / 9u) - 1;

@@ -12,6 +12,8 @@
 // k_bp_decide and returns at once when no rebuild is due, so the whole sequence can sit
 // in a CUDA graph that replays every step.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 
 #include "pd_bp.cuh"
@@ -140,9 +142,11 @@ __global__ void __launch_bounds__(128) k_bp_candidates_w(DevView v, const uint32
                                                          uint16_t *cand_n, uint32_t cap) {
   __shared__ uint32_t sh[4][kMaxCandCap + 1];
   if (!v.cnt->rebuild) return;
-  const uint64_t n = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (n >= v.N) return;
-  bp_candidates_warp(v, n, threadIdx.x & 31, count, start, sorted, mask, cand, cand_n, cap, sh[threadIdx.x >> 5]);
+  // a bounded grid whose warps take nodes in turn: in steps without a rebuild the launch costs
+  // a few waves less than one warp per node would
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t n = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < v.N; n += nwarps)
+    bp_candidates_warp(v, n, threadIdx.x & 31, count, start, sorted, mask, cand, cand_n, cap, sh[threadIdx.x >> 5]);
 }
 
 }  // namespace
@@ -160,8 +164,8 @@ void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s) {
   if (nblk) {
     k_bp_scatter<<<(unsigned)nblk, 256, 0, s>>>(v, bp.start, bp.key, bp.slot, bp.sorted);
     if (v.N <= kWarpCandNodes)
-      k_bp_candidates_w<<<(unsigned)((v.N + 3) / 4), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask, bp.cand,
-                                                                 bp.cand_n, bp.cand_cap);
+      k_bp_candidates_w<<<(unsigned)std::min<uint64_t>((v.N + 3) / 4, 152 * 8), 128, 0, s>>>(
+          v, bp.count, bp.start, bp.sorted, mask, bp.cand, bp.cand_n, bp.cand_cap);
     else
       k_bp_candidates<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask,
                                                                     bp.cand, bp.cand_n, bp.cand_cap);

@@ -182,9 +182,9 @@ struct CandWalk {
       x = v.pos[n] + v.disp[n];
       y = v.pos[n + v.Ncap] + v.disp[n + v.Ncap];
       z = v.pos[n + 2 * v.Ncap] + v.disp[n + 2 * v.Ncap];
-      cx = (long long)floor(x / sp.cell);
-      cy = (long long)floor(y / sp.cell);
-      cz = (long long)floor(z / sp.cell);
+      cx = (long long)floor(__dmul_rn(x, sp.inv_cell));  // as node_cell
+      cy = (long long)floor(__dmul_rn(y, sp.inv_cell));
+      cz = (long long)floor(__dmul_rn(z, sp.inv_cell));
       r2 = sp.cand_r2;
     }
   }
@@ -266,22 +266,25 @@ __device__ __forceinline__ bool nonfinite(double x) {
 //    roundings add at most 3 * 2^-22 s.
 // w is 1.25 times that bound over snot (the band is set from this step's extent and used in the
 // next), and at least 1e-4. xi_min is the particle's shortest setup bond: reference positions do
-// not change, so no bond gets shorter. Written with explicit roundings (no contraction), so
-// that every translation unit computes the same band.
+// not change, so no bond gets shorter. The bound is evaluated in FP32 with every operation rounded
+// towards +infinity on positive quantities (inputs rounded up, divisors down), so it is an upper
+// bound of the formula's exact value; the band's edges are rounded outwards. The same code runs in
+// every translation unit (no contraction applies to explicitly rounded operations).
 __device__ __forceinline__ void set_break_band(DevPart &P, double u_max) {
-  const double eps = 5.9604644775390625e-08, two_sqrt3 = 3.4641016151377544;
-  const double s = __dmul_rn(2.0, P.snot);
-  const double te = __dmul_rn(two_sqrt3, eps);
-  const double a = __dmul_rn(te, P.ext_p), b = __dmul_rn(te, u_max);
-  const double s2 = __dadd_rn(2.0, s), s4 = __dadd_rn(4.0, s);
-  const double lin = __ddiv_rn(__dadd_rn(b, __dmul_rn(s2, a)), P.xi_min);
-  const double dot = __dmul_rn(__dmul_rn(__dmul_rn(4.0, eps), s2), s4);
-  const double rcp = __dmul_rn(__dmul_rn(3.0 * 4.0, eps), s);
-  const double ds = __dadd_rn(__dadd_rn(lin, dot), rcp);
-  double w = __ddiv_rn(__dmul_rn(1.25, ds), P.snot);
-  if (!(w >= 1e-4)) w = 1e-4;  // also for a particle without bonds (xi_min infinite: ds finite)
-  P.snot_lo32 = __double2float_rd(__dmul_rn(P.snot, __dadd_rn(1.0, -w)));
-  P.snot_hi32 = __double2float_ru(__dmul_rn(P.snot, __dadd_rn(1.0, w)));
+  const float eps4 = 4.0f * 5.9604644775390625e-08f, eps12 = 12.0f * 5.9604644775390625e-08f;  // exact
+  const float te = 0x1.bb67b0p-23f;  // 2 sqrt(3) * 2^-24, rounded up
+  const float snot_u = __double2float_ru(P.snot), snot_d = __double2float_rd(P.snot);
+  const float s = __fmul_ru(2.0f, snot_u);
+  const float a = __fmul_ru(te, __double2float_ru(P.ext_p)), b = __fmul_ru(te, __double2float_ru(u_max));
+  const float s2 = __fadd_ru(2.0f, s), s4 = __fadd_ru(4.0f, s);
+  const float lin = __fdiv_ru(__fadd_ru(b, __fmul_ru(s2, a)), __double2float_rd(P.xi_min));
+  const float dot = __fmul_ru(__fmul_ru(eps4, s2), s4);
+  const float rcp = __fmul_ru(eps12, s);
+  const float ds = __fadd_ru(__fadd_ru(lin, dot), rcp);
+  float w = __fdiv_ru(__fmul_ru(1.25f, ds), snot_d);
+  if (!(w >= 0x1.a36e30p-14f)) w = 0x1.a36e30p-14f;  // at least 1e-4 (also for a particle without bonds)
+  P.snot_lo32 = __fmul_rd(snot_d, __fsub_rd(1.0f, w));
+  P.snot_hi32 = __fmul_ru(snot_u, __fadd_ru(1.0f, w));
 }
 
 // Largest |component| of a particle's anchor-relative displacement, bounded from the box of its

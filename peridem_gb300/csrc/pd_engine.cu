@@ -189,8 +189,11 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   // kernel, one launch less per step)
   variant_ = N_ < 131072 ? 6 : 18;
   // and the step graph: on large handles the broad phase's kernels are worth skipping in
-  // steps without a rebuild (a conditional node); small handles replay them, exiting at once
+  // steps without a rebuild (a conditional node); small handles replay them, exiting at once.
+  // Small FP32 handles step in persistent launches (where the handle's features allow it,
+  // persist_eligible), faster than either graph on every small workload measured.
   use_conditional_ = N_ >= 131072;
+  use_persist_ = precision_ == PD_FP32C && N_ < 131072;
   sim_node0_.assign(S_ + 1, 0);
   sim_p0_.assign(S_ + 1, 0);
   for (uint32_t i = 0; i < S_; ++i) {
@@ -672,6 +675,7 @@ int Engine::alloc_and_upload() {
     const double skin = bp_.skin_frac * s.Rc;
     const double rcand = (s.Rc + skin) * (1.0 + 1e-9);
     sp.cell = rcand * (1.0 + 1e-9);
+    sp.inv_cell = 1.0 / sp.cell;
     sp.cand_r2 = rcand * rcand;
     min_half_skin = std::min(min_half_skin, 0.5 * skin);
     sp.nl_bdry_only = cf.nl_bdry_only;
@@ -1116,7 +1120,7 @@ constexpr uint32_t kPersistMaxSteps = 1024;
 
 int Engine::launch_persist_steps(uint32_t n) {
   if (persist_lanes_ == 0) {  // the most lanes per node whose threads all fit at once, up to 4
-    const uint64_t resident = 128ull * (uint64_t)std::max(0, persist_max_blocks(4));
+    const uint64_t resident = (uint64_t)persist_threads() * (uint64_t)std::max(0, persist_max_blocks(4));
     persist_lanes_ = N_ * 4 <= resident ? 4 : (N_ * 2 <= resident ? 2 : 1);
   }
   if (persist_grid_lanes_ != persist_lanes_) {
@@ -1464,6 +1468,7 @@ int Engine::set_tuning(double skin_frac, uint32_t cand_cap, int tpb, int stats, 
       const double skin = skin_frac * sp.Rc;
       const double rcand = (sp.Rc + skin) * (1.0 + 1e-9);
       sp.cell = rcand * (1.0 + 1e-9);
+      sp.inv_cell = 1.0 / sp.cell;
       sp.cand_r2 = rcand * rcand;
       mh = std::min(mh, 0.5 * skin);
     }

@@ -91,6 +91,7 @@ struct DevSimParams {
   double Rc, Kn, sc, zeta2, mu;  // contact radius, stiffness, Kn*Rc, 2*damping, friction
   double pi3, pi4;            // M_PI/3, M_PI/4 (segment_mass)
   double cell;                // broad-phase cell edge (Rc + skin, slightly enlarged)
+  double inv_cell;            // 1 / cell: cell coordinates are floor(x * inv_cell) everywhere
   double cand_r2;             // squared candidate radius
   int32_t nl_bdry_only, compute_wall_reaction, gradient_extforce, allow_wall;
   uint32_t extforce_maxstep;
@@ -543,6 +544,7 @@ struct PersistArgs {
 // Blocks of the persistent step with `lanes` lanes per node in its bond phase (1, 2 or 4) that
 // fit on the current device at once (0 on error), and its cooperative launch.
 int persist_max_blocks(int lanes);
+int persist_threads();  // threads per block of the persistent step
 cudaError_t launch_persist(const PersistArgs &a, uint32_t grid, int lanes, cudaStream_t s);
 
 // Device build of the SELL-32 bond arrays from a strictly sorted Connectivity (pd_sell.cu).

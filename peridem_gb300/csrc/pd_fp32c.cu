@@ -1092,6 +1092,8 @@ static const void *persist_kernel(int lanes) {
   }
 }
 
+int persist_threads() { return kPersistThreads; }
+
 // Blocks of k_persist that fit on the current device at once (its grid may not exceed them).
 int persist_max_blocks(int lanes) {
   int dev = 0, sms = 0, per = 0;

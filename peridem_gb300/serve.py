@@ -154,6 +154,10 @@ class Server:
                                 self.precision)
             if self.tune and hasattr(b, "tune"):
                 b.tune(**self.tune)
+            elif hasattr(b, "graph_mode") and b.graph_mode() == 3:
+                # cohorts share the GPU: a persistent launch holds every SM for its steps and
+                # would run the cohorts one after another, so small cohorts step with the graph
+                b.tune(graphs=1)
             for i, r in enumerate(reqs):  # evicted requests continue from their checkpoints
                 if r.checkpoint is not None:
                     b.load_sim(r.checkpoint, i)
