@@ -263,11 +263,13 @@ int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);
-/* Lanes per node in the bond phase of the persistent step (launch mode 3): 1, 2 or 4, or 0 to
- * choose by size (the most lanes, up to 4, whose threads all fit on the device at once). More
- * lanes shorten each node's chain of gathers on handles too small to fill the GPU; results do not
- * depend on it (each node's bond sum is taken in four chains fixed by the row's positions, merged
- * in a fixed order). pd_autotune times 1, 2 and 4. */
+/* Lanes per node in the bond phase of the persistent step (launch mode 3): 1, 2 or 4, or 0 (the
+ * default) to mix them by row length: every 32-node slice is one warp with one lane per node,
+ * except that the slices with the longest rows take 2 or 4 lanes per node (all of them 4 where
+ * that fits) as long as the warps all fit on the device at once. More lanes shorten a node's
+ * chain of gathers on handles too small to fill the GPU; results do not depend on it (each node's
+ * bond sum is taken in four blocks of its row, merged in a fixed order). pd_autotune times 1, 2,
+ * 4 and the mix. */
 int pd_set_persist_lanes(pd_sim *sim, int lanes);
 int pd_persist_lanes(const pd_sim *sim);
 /* How steps are launched: 0 separate launches, 1 one CUDA graph per step, 2 a step graph whose

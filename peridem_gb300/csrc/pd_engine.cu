@@ -30,6 +30,7 @@ inline uint64_t round_up(uint64_t x, uint64_t m) { return (x + m - 1) / m * m; }
 // can admit and retire simulations while others keep the GPU busy.
 Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
+  if (h_stage_) cudaFreeHost(h_stage_);
   for (int i = 0; i < 2; ++i)
     if (graph_[i]) cudaGraphExecDestroy(graph_[i]);
   for (void *p : allocs_) cudaFreeAsync(p, capture_stream_);
@@ -666,6 +667,7 @@ int Engine::alloc_and_upload() {
     sp.hdt2 = (cf.dt * cf.dt) * 0.5;
     sp.hdt = 0.5 * cf.dt;
     sp.Rc = s.Rc;
+    sp.rc2_far = (s.Rc * s.Rc) * (1.0 + 1e-12);
     sp.Kn = Kn;
     sp.sc = Kn * s.Rc;
     sp.zeta2 = 2 * zeta;
@@ -1118,21 +1120,68 @@ int Engine::capture_graphs() {
 // Steps per persistent launch: a launch of a small handle stays within tens of milliseconds.
 constexpr uint32_t kPersistMaxSteps = 1024;
 
-int Engine::launch_persist_steps(uint32_t n) {
-  if (persist_lanes_ == 0) {  // the most lanes per node whose threads all fit at once, up to 4
-    const uint64_t resident = (uint64_t)persist_threads() * (uint64_t)std::max(0, persist_max_blocks(4));
-    persist_lanes_ = N_ * 4 <= resident ? 4 : (N_ * 2 <= resident ? 2 : 1);
+// The mixed bond phase's warp tasks: every 32-node slice is one task of one lane per node,
+// except that the slices with the longest rows are split into two tasks of two lanes or four of
+// four, as long as the tasks still fit in the resident warps; tasks are ordered longest rows
+// first, so that the warps dealt over the SMs start with them.
+int Engine::build_persist_tasks(uint64_t resident_warps) {
+  std::vector<uint16_t> deg(Ncap_);
+  PD_TRY(cpy(deg.data(), d_deg_, Ncap_ * 2, "read row lengths"));
+  const uint64_t ns = (N_ + 31) / 32;
+  std::vector<std::pair<uint32_t, uint32_t>> sl(ns);  // (longest row, slice)
+  for (uint64_t s = 0; s < ns; ++s) {
+    uint32_t m = 0;
+    for (uint64_t k = 32 * s; k < std::min<uint64_t>(N_, 32 * s + 32); ++k) m = std::max<uint32_t>(m, deg[k]);
+    sl[s] = {m, (uint32_t)s};
   }
-  if (persist_grid_lanes_ != persist_lanes_) {
+  std::sort(sl.begin(), sl.end(), [](const auto &a, const auto &b) { return a.first > b.first || (a.first == b.first && a.second < b.second); });
+  // lanes per slice: all four where even that fits, else two for the longest rows while it fits
+  std::vector<int> code(ns, 0);
+  uint64_t tasks = ns;
+  if (4 * ns <= resident_warps) {
+    std::fill(code.begin(), code.end(), 2);
+    tasks = 4 * ns;
+  } else {
+    for (uint64_t i = 0; i < ns && tasks + 1 <= resident_warps; ++i) {
+      code[i] = 1;
+      tasks += 1;
+    }
+  }
+  std::vector<uint32_t> h;
+  h.reserve(tasks);
+  for (uint64_t i = 0; i < ns; ++i) {
+    const uint32_t node0 = 32 * sl[i].second;
+    const int parts = code[i] == 0 ? 1 : (code[i] == 1 ? 2 : 4);
+    for (int p = 0; p < parts; ++p) h.push_back((node0 + (uint32_t)(p * (32 / parts))) | (uint32_t)code[i]);
+  }
+  if (persist_tasks_) {
+    cudaFreeAsync(persist_tasks_, stream_);
+    allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)persist_tasks_), allocs_.end());
+    persist_tasks_ = nullptr;
+  }
+  PD_TRY(dalloc(this, allocs_, &persist_tasks_, std::max<uint64_t>(h.size(), 1), err));
+  PD_TRY(cpy(persist_tasks_, h.data(), h.size() * 4, "upload bond tasks"));
+  persist_ntasks_ = (uint32_t)h.size();
+  return PD_OK;
+}
+
+int Engine::launch_persist_steps(uint32_t n) {
+  if (persist_grid_lanes_ != persist_lanes_ + 1) {  // (re)size the grid for these lanes
     const int mb = persist_max_blocks(persist_lanes_);
     if (mb <= 0) {
       err = "persistent step: no resident blocks";
       return PD_ECUDA;
     }
+    uint64_t warps;
+    if (persist_lanes_ == 0) {
+      PD_TRY(build_persist_tasks((uint64_t)mb * (uint64_t)(persist_threads() / 32)));
+      warps = persist_ntasks_;
+    } else {
+      warps = (N_ * (uint64_t)persist_lanes_ + 31) / 32;
+    }
     // one block per SM, or fewer where the handle has fewer warps of work than SMs
-    const uint64_t want = (N_ * (uint64_t)persist_lanes_ + 31) / 32;
-    persist_blocks_ = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)mb, want));
-    persist_grid_lanes_ = persist_lanes_;
+    persist_blocks_ = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)mb, warps));
+    persist_grid_lanes_ = persist_lanes_ + 1;
   }
   int dev = 0, sms = 0;
   PD_TRY(check(cudaGetDevice(&dev), "device"));
@@ -1165,6 +1214,8 @@ int Engine::launch_persist_steps(uint32_t n) {
   a.clamped_ptr = n_clamped_ ? d_clamped_ : nullptr;
   a.clamped = n_clamped_ ? d_clamped_ + (P_ + 1) : nullptr;
   a.clamped_disp = d_clamped_disp_;
+  a.tasks = persist_tasks_;
+  a.ntasks = persist_ntasks_;
   PD_TRY(check(cudaMemsetAsync(persist_ws_, 0, 8, stream_), "persistent barrier reset"));
   PD_TRY(check(launch_persist(a, persist_blocks_, persist_lanes_, stream_), "persistent step launch"));
   cur_ ^= (int)(n & 1);
@@ -1265,6 +1316,12 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
   const bool fused = precision_ == PD_FP32C;
   const double *dcur = fused ? d_dispb_[cur_ ^ 1] : d_disp_;
   const uint32_t *clist = n_clamped_ ? d_clamped_ + (P_ + 1) : nullptr;
+  // Large handles copy through a pinned staging buffer and fill the caller's (pageable) arrays
+  // from it on all host cores: a pageable device-to-host copy runs at a few GB/s.
+  if (N_ >= kPinnedStageNodes && !h_stage_ && cudaMallocHost((void **)&h_stage_, 3 * N_ * 8) != cudaSuccess) {
+    cudaGetLastError();
+    h_stage_ = nullptr;
+  }
   int rc = PD_OK;
   auto out = [&](const double *src, const double *add, int clamped_mode, double *dst) {
     if (!dst || rc != PD_OK) return;
@@ -1273,8 +1330,16 @@ int Engine::get_state(double *curpos, double *vel, double *acc, double *force, d
     if (clamped_mode == 2)
       launch_clamped_rows(clist, n_clamped_, d_file_of_, d_pos_, d_clamped_disp_, Ncap_, rows, stream_);
     rc = check(cudaGetLastError(), "read state");
-    if (rc == PD_OK) rc = check(cudaMemcpyAsync(dst, rows, 3 * N_ * 8, cudaMemcpyDeviceToHost, stream_), "read state");
+    double *to = h_stage_ ? h_stage_ : dst;
+    if (rc == PD_OK) rc = check(cudaMemcpyAsync(to, rows, 3 * N_ * 8, cudaMemcpyDeviceToHost, stream_), "read state");
     if (rc == PD_OK) rc = check(cudaStreamSynchronize(stream_), "read state");
+    if (rc == PD_OK && h_stage_) {
+      const uint64_t n = 3 * N_, chunk = 1ull << 17;  // 1 MB per item
+      parallel_items((n + chunk - 1) / chunk, [&](uint64_t i) {
+        const uint64_t a = i * chunk, b = std::min(n, a + chunk);
+        std::memcpy(dst + a, h_stage_ + a, (b - a) * 8);
+      });
+    }
   };
   const bool stepped = steps_done_ > 0 && n_clamped_;
   // clamped nodes end each step at zero (timeloop.h:767-774); the FP64 form's CurrPos keeps
@@ -1863,9 +1928,10 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
     bool best_cond = use_conditional_, best_persist = use_persist_;
     int best_lanes = persist_lanes_;
     // modes 1 and 2, then (where eligible) the persistent step with 1, 2 and 4 lanes per node
-    const int last_mode = persist_eligible() ? 5 : 2;
+    // and with lanes mixed by row length
+    const int last_mode = persist_eligible() ? 6 : 2;
     for (int mode = 1; mode <= last_mode; ++mode) {
-      const int lanes = mode >= 3 ? (1 << (mode - 3)) : 0;
+      const int lanes = mode >= 3 && mode <= 5 ? (1 << (mode - 3)) : 0;
       use_conditional_ = mode >= 2;
       use_persist_ = mode >= 3;
       if (mode >= 3) PD_TRY(set_persist_lanes(lanes));

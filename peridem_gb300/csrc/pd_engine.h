@@ -89,6 +89,8 @@ struct DevPart {
 struct DevSimParams {
   double dt, hdt2, hdt;       // dt, (dt*dt)*0.5, 0.5*dt
   double Rc, Kn, sc, zeta2, mu;  // contact radius, stiffness, Kn*Rc, 2*damping, friction
+  double rc2_far;             // Rc^2 (1 + 1e-12): a pair whose squared distance reaches it fails both
+                              // contact tests (dn < Rc, dn <= Rc), so its square root is skipped
   double pi3, pi4;            // M_PI/3, M_PI/4 (segment_mass)
   double cell;                // broad-phase cell edge (Rc + skin, slightly enlarged)
   double inv_cell;            // 1 / cell: cell coordinates are floor(x * inv_cell) everywhere
@@ -305,7 +307,7 @@ class Engine {
   int clear_device_errors();
   // Bond-kernel variant (FP32 form); autotune() times each on the live state and restores it.
   int set_variant(int variant);
-  // lanes per node of the persistent step's bond phase: 0 chooses by size, else 1, 2 or 4
+  // lanes per node of the persistent step's bond phase: 0 mixes them by row length, else 1, 2 or 4
   int set_persist_lanes(int lanes);
   int persist_lanes() const { return persist_lanes_; }
   int autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms);
@@ -448,8 +450,11 @@ class Engine {
   bool use_persist_ = false;        // launch mode 3 (persistent step, FP32 form)
   uint32_t *persist_ws_ = nullptr;  // its barrier counter and scan scratch
   uint32_t persist_blocks_ = 0;     // its grid
-  int persist_lanes_ = 0;           // lanes per node of its bond phase (0: chosen by size)
-  int persist_grid_lanes_ = 0;      // the lanes persist_blocks_ was sized for
+  int persist_lanes_ = 0;           // lanes per node of its bond phase (0: mixed, by row length)
+  uint32_t *persist_tasks_ = nullptr;  // the mixed bond phase's warp tasks
+  uint32_t persist_ntasks_ = 0;
+  int build_persist_tasks(uint64_t resident_warps);
+  int persist_grid_lanes_ = 0;      // 1 + the lanes persist_blocks_ was sized for (0: not yet)
   int launch_persist_steps(uint32_t n);
   bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning
                                   // mode 2); init() picks by size
@@ -511,6 +516,7 @@ class Engine {
   DevCounters *d_cnt_ = nullptr;
   uint32_t *d_clamped_ = nullptr;  // [P+1] offsets followed by engine node indices
   double *d_clamped_disp_ = nullptr;
+  double *h_stage_ = nullptr;  // pinned host staging of state reads on large handles (3 N doubles)
   uint64_t n_clamped_ = 0;
   double *d_afd_ = nullptr;
   bool pv_possible_ = false, reset_possible_ = false;
@@ -523,6 +529,8 @@ class Engine {
 // Handles up to this many nodes search contact candidates with one warp per node
 // (bp_candidates_warp), larger ones with one thread per node; the lists are the same.
 constexpr uint64_t kWarpCandNodes = 1ull << 20;
+// Handles of at least this many nodes read their state back through pinned host memory.
+constexpr uint64_t kPinnedStageNodes = 1ull << 18;
 
 // Arguments of the persistent step (k_persist, pd_fp32c.cu): the views of the two buffer
 // parities, the steps to run and the broad phase's buffers.
@@ -540,6 +548,10 @@ struct PersistArgs {
   uint32_t cap;
   const uint32_t *clamped_ptr, *clamped;
   double *clamped_disp;
+  // mixed lanes (k_persist<0>): the bond phase's warp tasks, node0 | code (node0 a multiple of 8;
+  // code 0: 32 nodes, one lane each; 1: 16 nodes, two lanes; 2: 8 nodes, four lanes)
+  const uint32_t *tasks;
+  uint32_t ntasks;
 };
 // Blocks of the persistent step with `lanes` lanes per node in its bond phase (1, 2 or 4) that
 // fit on the current device at once (0 on error), and its cooperative launch.

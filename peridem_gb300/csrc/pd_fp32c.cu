@@ -79,7 +79,9 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
         if (sp.nl_bdry_only && !v.bdry[m]) continue;
         D3 xi = ld3(v.pos, m, C3) - pi;
         D3 dir = (ld3(v.disp, m, C3) - di) + xi;
-        double dn = norm3(dir);
+        const double q = sq3(dir);
+        if (q >= sp.rc2_far) continue;  // outside Rc for certain: skip the square root
+        double dn = sqrt(q);
         if (!(dn <= sp.Rc)) continue;
         double xin = norm3(xi);
         double len_ref = sp.Rc, sc = sp.sc;
@@ -146,7 +148,9 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
       const D3 pm = ld3(v.pos, m, C3), dm = ld3(v.disp, m, C3);
       if (km > k) {
         D3 dir = (dm - di) + (pm - pi);
-        double dn = norm3(dir);
+        const double q = sq3(dir);
+        if (q >= sp.rc2_far) continue;
+        double dn = sqrt(q);
         if (!(dn < sp.Rc)) continue;
         PairForce pf;
         pair_force(dir, dn, sp.Rc, sp.sc, v.vol[m], P.rho, vi, ld3(v.vel_in, m, C3), sp, st, pf);
@@ -156,7 +160,9 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
         if (v.stats) atomicAdd(&v.cnt->contacts, 1ull);
       } else {
         D3 dir = (di - dm) + (pi - pm);
-        double dn = norm3(dir);
+        const double q = sq3(dir);
+        if (q >= sp.rc2_far) continue;
+        double dn = sqrt(q);
         if (!(dn < sp.Rc)) continue;
         const double volm = v.vol[m];
         PairForce pf;
@@ -1059,7 +1065,14 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_con
       v.xcount[1] = 0;
       v.cnt->xall = 0;
     }
-    if constexpr (L == 1) {
+    if constexpr (L == 0) {  // warp tasks of 1, 2 or 4 lanes per node, longest rows first
+      for (uint64_t w = gwarp; w < a.ntasks; w += nwarps) {
+        const uint32_t task = a.tasks[w], node0 = task & ~7u, code = task & 7u;
+        if (code == 0) bond_node<4, 1, 1, 1, 0>(v, (uint64_t)node0 + lane);
+        else if (code == 1) bond_node_split<2, 4, 1, 0>(v, 2ull * node0 + lane);
+        else bond_node_split<4, 4, 1, 0>(v, 4ull * node0 + lane);
+      }
+    } else if constexpr (L == 1) {
       for (uint64_t w = gwarp; w * 32 < v.N; w += nwarps) bond_node<4, 1, 1, 1, 0>(v, w * 32 + lane);
     } else {  // L lanes per node (bond_node_split)
       for (uint64_t w = gwarp; w * 32 < v.N * L; w += nwarps)
@@ -1086,6 +1099,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_con
 
 static const void *persist_kernel(int lanes) {
   switch (lanes) {
+    case 0: return (const void *)k_persist<0>;
     case 2: return (const void *)k_persist<2>;
     case 4: return (const void *)k_persist<4>;
     default: return (const void *)k_persist<1>;

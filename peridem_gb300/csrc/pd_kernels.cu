@@ -123,7 +123,9 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
         if (sp.nl_bdry_only && !v.bdry[m]) continue;
         D3 xi = ld3(v.pos, m, C3) - pi;
         D3 dir = (ld3(v.disp, m, C3) - di) + xi;
-        double dn = norm3(dir);
+        const double q = sq3(dir);
+        if (q >= sp.rc2_far) continue;  // outside Rc for certain: skip the square root
+        double dn = sqrt(q);
         if (!(dn <= sp.Rc)) continue;
         double xin = norm3(xi);
         double len_ref = sp.Rc, sc = sp.sc;
@@ -201,7 +203,9 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
       if (km > k) {
         D3 xi = pm - pi;
         D3 dir = (dm - di) + xi;
-        double dn = norm3(dir);
+        const double q = sq3(dir);
+        if (q >= sp.rc2_far) continue;
+        double dn = sqrt(q);
         if (!(dn <= sp.Rc) || !(dn < sp.Rc)) continue;
         PairForce pf;
         pair_force(dir, dn, sp.Rc, sp.sc, volm, P.rho, vi, vm, sp, st, pf);
@@ -212,7 +216,9 @@ __global__ void __launch_bounds__(128) k_step(DevView v) {
       } else {
         D3 xi = pi - pm;
         D3 dir = (di - dm) + xi;
-        double dn = norm3(dir);
+        const double q = sq3(dir);
+        if (q >= sp.rc2_far) continue;
+        double dn = sqrt(q);
         if (!(dn <= sp.Rc) || !(dn < sp.Rc)) continue;
         PairForce pf;
         pair_force(dir, dn, sp.Rc, sp.sc, voli, v.parts[km].rho, vm, vi, sp, st, pf);
@@ -508,7 +514,8 @@ __global__ void k_reset_y(DevView v) {
     }
     const double dest = (max_bulk_y + sp.wheel_rad) + sp.Rc;
     move = dest - m0[1];
-    v.cnt->xall = 1;  // particle 0 moved: the non-bond work lists are stale for this step
+    v.cnt->xall = 1;       // particle 0 moved: the non-bond work lists are stale for this step
+    v.cnt->moved = 1e300;  // and so are the contact candidate lists: this step rebuilds them
     if (v.fused) {  // the FP32 form keeps positions relative to the particle's anchor
       DevPart &Pw = v.parts[sp.p0];
       Pw.anchor_pos[1] = Pw.anchor_pos[1] + move;

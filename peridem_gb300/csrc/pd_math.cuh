@@ -24,7 +24,8 @@ __device__ __forceinline__ void set_comp(D3 &a, int k, double v) {
   else a.z = v;
 }
 // Eigen 3.3 reduction order for a 1x3 row: (x0 + x1) + x2.
-__device__ __forceinline__ double norm3(D3 a) { return sqrt((a.x * a.x + a.y * a.y) + a.z * a.z); }
+__device__ __forceinline__ double sq3(D3 a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
+__device__ __forceinline__ double norm3(D3 a) { return sqrt(sq3(a)); }
 __device__ __forceinline__ double dot3(D3 a, D3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 
 // a / b, correctly rounded, from rb = RN(1/b): one correction step with an exact
