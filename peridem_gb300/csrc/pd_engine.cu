@@ -1138,7 +1138,8 @@ int Engine::build_persist_tasks(uint64_t resident_warps) {
   // lanes per slice: all four where even that fits, else two for the longest rows while it fits
   std::vector<int> code(ns, 0);
   uint64_t tasks = ns;
-  if (4 * ns <= resident_warps) {
+  if (4 * ns <= resident_warps) {  // four lanes for every slice, in node order (measured faster
+    for (uint64_t s = 0; s < ns; ++s) sl[s] = {0u, (uint32_t)s};  // than longest first here)
     std::fill(code.begin(), code.end(), 2);
     tasks = 4 * ns;
   } else {
