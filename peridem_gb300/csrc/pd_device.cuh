@@ -234,8 +234,15 @@ __device__ __forceinline__ bool row_has_live(const DevView &v, uint64_t n, uint3
   const uint64_t base = v.slice_ptr[s] + lane;
   const uint64_t mbase = v.slice_ptr[s] >> 5;
   const int dg = v.deg[n];
-  for (int j = 0; j < dg; ++j) {
-    if (v.col[base + 32ull * j] == m) return (v.mask[mbase + j] >> lane) & 1u;
+  // eight entries requested at once: the row's entries lie 128 bytes apart, one load each, and a
+  // load-compare-branch chain would wait on every one of them in turn
+  for (int j0 = 0; j0 < dg; j0 += 8) {
+    uint32_t c[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) c[k] = (j0 + k < dg) ? v.col[base + 32ull * (j0 + k)] : 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (c[k] == m) return (v.mask[mbase + j0 + k] >> lane) & 1u;
   }
   return false;
 }

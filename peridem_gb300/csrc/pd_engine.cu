@@ -1174,9 +1174,14 @@ int Engine::launch_persist_steps(uint32_t n) {
       return PD_ECUDA;
     }
     uint64_t warps;
+    persist_kernel_lanes_ = persist_lanes_;
     if (persist_lanes_ == 0) {
       PD_TRY(build_persist_tasks((uint64_t)mb * (uint64_t)(persist_threads() / 32)));
       warps = persist_ntasks_;
+      // every slice alike: the kernel of that lane count (no task list to read)
+      const uint64_t ns = (N_ + 31) / 32;
+      if (persist_ntasks_ == 4 * ns) persist_kernel_lanes_ = 4;
+      else if (persist_ntasks_ == ns) persist_kernel_lanes_ = 1;
     } else {
       warps = (N_ * (uint64_t)persist_lanes_ + 31) / 32;
     }
@@ -1218,7 +1223,7 @@ int Engine::launch_persist_steps(uint32_t n) {
   a.tasks = persist_tasks_;
   a.ntasks = persist_ntasks_;
   PD_TRY(check(cudaMemsetAsync(persist_ws_, 0, 8, stream_), "persistent barrier reset"));
-  PD_TRY(check(launch_persist(a, persist_blocks_, persist_lanes_, stream_), "persistent step launch"));
+  PD_TRY(check(launch_persist(a, persist_blocks_, persist_kernel_lanes_, stream_), "persistent step launch"));
   cur_ ^= (int)(n & 1);
   steps_done_ += n;
   return PD_OK;

@@ -453,6 +453,7 @@ class Engine {
   int persist_lanes_ = 0;           // lanes per node of its bond phase (0: mixed, by row length)
   uint32_t *persist_tasks_ = nullptr;  // the mixed bond phase's warp tasks
   uint32_t persist_ntasks_ = 0;
+  int persist_kernel_lanes_ = 1;    // the kernel launched (0: the task list)
   int build_persist_tasks(uint64_t resident_warps);
   int persist_grid_lanes_ = 0;      // 1 + the lanes persist_blocks_ was sized for (0: not yet)
   int launch_persist_steps(uint32_t n);

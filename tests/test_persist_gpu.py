@@ -68,6 +68,23 @@ def test_persistent_step_equals_step_graph(name, chunks, lanes):
     b.close()
 
 
+def test_mixed_lanes_on_a_mid_size_aggregate():
+    """53k nodes: too many slices for four lanes each, so the slices with the longest rows take
+    two lanes and the rest one (the task-list kernel); bit-identical to the step graph."""
+    from peridem_gb300 import gen
+    s, cfg = gen.aggregate(20, seed=7, steps=100)
+    a = Sim(s, cfg, "fp32c")
+    b = Sim(s, cfg, "fp32c")
+    a.tune(graphs=1)
+    b.tune(graphs=3)
+    b.set_persist_lanes(0)
+    a.step(30)
+    b.step(30)
+    _compare(a, b, s.n_particles, "aggregate 53k")
+    a.close()
+    b.close()
+
+
 def test_persistent_step_beyond_one_launch():
     """More steps than one persistent launch takes (1024): the call is cut into launches."""
     s, cfg = cases.impact_free(steps=1100)
@@ -118,6 +135,17 @@ def test_persistent_batch_with_finished_member():
         assert ba.sim_steps(i) == bb.sim_steps(i)
     ba.close()
     bb.close()
+
+
+def test_persist_lanes_out_of_range_is_rejected():
+    from peridem_gb300.sim import PdError
+    s, cfg = cases.impact_free()
+    a = Sim(s, cfg, "fp32c")
+    with pytest.raises(PdError):
+        a.set_persist_lanes(3)
+    a.set_persist_lanes(2)
+    assert a.persist_lanes() == 2
+    a.close()
 
 
 @pytest.mark.parametrize("precision,stats", [("fp64", -1), ("fp32c", 1)])
