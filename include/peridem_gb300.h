@@ -240,8 +240,9 @@ int pd_close(pd_sim *sim);
  * cooperative launches of one block per SM (up to 1024 steps each), the FP32C default below
  * 131,072 nodes, for handles without reset_partzero_y, prescribed-velocity or torque particles
  * and with statistics off -- others step as in mode 2. A persistent launch occupies every SM
- * while it runs: handles stepping concurrently on other streams wait for it, so a server of
- * many small handles steps them with mode 1. All modes give the same results). */
+ * while it runs: handles stepping concurrently on other streams wait for it, so small handles
+ * that step at the same time (a server's cohorts) should use mode 1. Its grid barriers wait at
+ * most 2 s each (PD_DERR_BARRIER_TIMEOUT). All modes give the same results). */
 int pd_set_tuning(pd_sim *sim, double skin_frac, uint32_t cand_cap, int threads_per_block,
                   int stats, int use_graphs);
 /* Clears the device error word after the caller has handled it. */
@@ -257,9 +258,10 @@ int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 /* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM,
  * lanes per node) for steps_per_variant steps from the same snapshot of the live state, restores
  * the state and keeps the fastest; then times the launch modes of pd_set_tuning the same way (the
- * persistent step with 1, 2 and 4 lanes per node where it applies). Results do not depend on the
- * variant or the mode: every form sums a node's bonds in the same four chains, merged in the same
- * order. variant_ms (may be NULL) receives pd_num_variants() timings in ms per step. */
+ * persistent step with 1, 2 and 4 lanes per node and with lanes mixed by row length, where it
+ * applies). Results do not depend on the variant or the mode: every form sums a node's bonds in
+ * the same four blocks of its row, merged in the same order. variant_ms (may be NULL) receives
+ * pd_num_variants() timings in ms per step. */
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);

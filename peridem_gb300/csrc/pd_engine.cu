@@ -1168,7 +1168,9 @@ int Engine::build_persist_tasks(uint64_t resident_warps) {
 
 int Engine::launch_persist_steps(uint32_t n) {
   if (persist_grid_lanes_ != persist_lanes_ + 1) {  // (re)size the grid for these lanes
-    const int mb = persist_max_blocks(persist_lanes_);
+    // the mix may launch the one- or four-lane kernel: a grid all of them can hold at once
+    const int mb = persist_lanes_ != 0 ? persist_max_blocks(persist_lanes_)
+                                       : std::min({persist_max_blocks(0), persist_max_blocks(1), persist_max_blocks(4)});
     if (mb <= 0) {
       err = "persistent step: no resident blocks";
       return PD_ECUDA;
