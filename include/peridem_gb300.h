@@ -357,6 +357,13 @@ int pd_load_sim(pd_sim *sim, uint32_t i, const void *buf, uint64_t bytes);
  * not). Runs on the current device. Errors: pd_pairs_error(). */
 int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double *radius,
                    uint32_t n_particles, uint32_t *pairs, uint64_t cap, uint64_t *pair_offset);
+/* near[q] = 1 for every node q within radius[p] of a node of its particle p with marked[] set
+ * (the marked nodes themselves included), else 0: the nonlocal boundary nodes the reference's
+ * setup scripts find by scanning every node for every edge node (gen_nonlocal_boundry_nodes,
+ * exp_dict.py:1231-1248), with its test sqrt((dx*dx + dy*dy) + dz*dz) <= r in FP64 without
+ * contraction. marked and near hold one byte per node; same inputs and errors as pd_query_pairs. */
+int pd_query_near(const double *pos, const uint64_t *node_offset, const double *radius, uint32_t n_particles,
+                  const uint8_t *marked, uint8_t *near);
 const char *pd_pairs_error(void);
 
 #ifdef __cplusplus

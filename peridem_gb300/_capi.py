@@ -151,6 +151,7 @@ SIGNATURES = [
     ("pd_save_sim", C.c_int, [_P, _u32, _P, _u64, C.POINTER(_u64)]),
     ("pd_load_sim", C.c_int, [_P, _u32, _P, _u64]),
     ("pd_query_pairs", C.c_int, [_P, _P, _P, _u32, _P, _u64, _P]),
+    ("pd_query_near", C.c_int, [_P, _P, _P, _u32, _P, _P]),
     ("pd_pairs_error", C.c_char_p, []),
 ]
 

@@ -113,6 +113,37 @@ __global__ void k_pairs(PairsArgs a) {
   }
 }
 
+// Flags every node q that lies within r of a marked node of its particle (itself included), with
+// the reference's test: d = sqrt((dx*dx + dy*dy) + dz*dz), d <= r (gen_nonlocal_boundry_nodes,
+// exp_dict.py:1231-1248, which scans every node for every edge node).
+__global__ void k_near(PairsArgs a, const uint8_t *marked, uint8_t *near) {
+  for (uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.N; n += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = a.pid[n];
+    const double xi = a.pos[3 * n], yi = a.pos[3 * n + 1], zi = a.pos[3 * n + 2];
+    const double r = a.r[p];
+    long long cx, cy, cz;
+    cell_of(a, n, p, cx, cy, cz);
+    uint8_t hit = 0;
+    for (int dz = -1; dz <= 1 && !hit; ++dz)
+      for (int dy = -1; dy <= 1 && !hit; ++dy)
+        for (int dx = -1; dx <= 1 && !hit; ++dx) {
+          const uint32_t k = hash_cell(p, cx + dx, cy + dy, cz + dz, a.mask);
+          const uint32_t b = a.start[k], e = b + a.count[k];
+          for (uint32_t it = b; it < e; ++it) {
+            const uint32_t m = a.sorted[it];
+            if (!marked[m] || a.pid[m] != p) continue;
+            const double ex = xi - a.pos[3 * (uint64_t)m], ey = yi - a.pos[3 * (uint64_t)m + 1],
+                         ez = zi - a.pos[3 * (uint64_t)m + 2];
+            if (sqrt((ex * ex + ey * ey) + ez * ez) <= r) {
+              hit = 1;
+              break;
+            }
+          }
+        }
+    near[n] = hit;
+  }
+}
+
 // Sorts each node's partner segment (j ascending): rows are already grouped by i in node order.
 __global__ void k_sort_rows(PairsArgs a, const uint64_t *end) {
   for (uint64_t n = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.N; n += (uint64_t)gridDim.x * blockDim.x) {
@@ -157,27 +188,23 @@ int fail(int rc, const std::string &m) {
   return rc;
 }
 
-}  // namespace
-
-extern "C" {
-
-const char *pd_pairs_error(void) { return g_pairs_error.c_str(); }
-
-int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double *radius, uint32_t n_particles,
-                   uint32_t *pairs, uint64_t cap, uint64_t *pair_offset) {
-  if (!pos || !node_offset || !radius || !pair_offset) return fail(PD_EINVAL, "null argument");
+// Per-particle boxes and cells a little larger than r, the hashed cell list of all nodes
+// (counting sort: count on the device, exclusive scan on the host, scatter on the device), on d's
+// stream; a receives the device arrays.
+static int check_inputs(const double *pos, const uint64_t *node_offset, const double *radius, uint32_t n_particles) {
+  if (!pos || !node_offset || !radius) return fail(PD_EINVAL, "null argument");
   if (node_offset[0] != 0) return fail(PD_EINVAL, "node_offset must start at 0");
-  const uint64_t N = node_offset[n_particles];
   for (uint32_t p = 0; p < n_particles; ++p) {
     if (node_offset[p + 1] < node_offset[p]) return fail(PD_EINVAL, "node_offset not monotone");
     if (!(radius[p] > 0) || !std::isfinite(radius[p])) return fail(PD_EINVAL, "radius must be positive");
   }
-  if (N >= 0xFFFFFFF0ull) return fail(PD_EINVAL, "too many nodes");
-  pair_offset[0] = 0;
-  if (N == 0) {
-    for (uint32_t p = 0; p < n_particles; ++p) pair_offset[p + 1] = 0;
-    return PD_OK;
-  }
+  if (node_offset[n_particles] >= 0xFFFFFFF0ull) return fail(PD_EINVAL, "too many nodes");
+  return PD_OK;
+}
+
+static int build_grid(const double *pos, const uint64_t *node_offset, const double *radius, uint32_t n_particles,
+                      Dev &d, PairsArgs &a) {
+  const uint64_t N = node_offset[n_particles];
   // per-particle boxes and cells (host: one pass over the points)
   std::vector<double> lo(3 * (size_t)n_particles, 0.0), cell(n_particles), hi(3 * (size_t)n_particles, 0.0);
   std::vector<uint32_t> pid(N);
@@ -207,15 +234,13 @@ int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double 
   if (bits > 31) return fail(PD_EINVAL, "too many nodes");
   const uint64_t T = 1ull << bits;
 
-  Dev d;
   if (cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking) != cudaSuccess)
     return fail(PD_ECUDA, "stream create failed");
-  PairsArgs a;
   a.N = N;
   a.mask = (uint32_t)(T - 1);
   double *dpos, *dr, *dlo, *dcell;
   uint32_t *dpid;
-  uint64_t *dg0, *end;
+  uint64_t *dg0;
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t x) {
     if (e == cudaSuccess) e = x;
@@ -232,7 +257,6 @@ int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double 
   ck(d.alloc(&a.slot, N));
   ck(d.alloc(&a.sorted, N));
   ck(d.alloc(&a.deg, N));
-  ck(d.alloc(&end, N));
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA, cudaGetErrorString(e));
   ck(cudaMemcpyAsync(dpos, pos, 3 * N * 8, cudaMemcpyHostToDevice, d.s));
   ck(cudaMemcpyAsync(dpid, pid.data(), N * 4, cudaMemcpyHostToDevice, d.s));
@@ -263,6 +287,40 @@ int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double 
   }
   ck(cudaMemcpyAsync(a.start, cnt.data(), T * 4, cudaMemcpyHostToDevice, d.s));
   k_scatter<<<grid, kThreads, 0, d.s>>>(a);
+  ck(cudaGetLastError());
+  if (e != cudaSuccess) return fail(PD_ECUDA, cudaGetErrorString(e));
+  return PD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *pd_pairs_error(void) { return g_pairs_error.c_str(); }
+
+int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double *radius, uint32_t n_particles,
+                   uint32_t *pairs, uint64_t cap, uint64_t *pair_offset) {
+  if (!pair_offset) return fail(PD_EINVAL, "null argument");
+  const int bad = check_inputs(pos, node_offset, radius, n_particles);
+  if (bad != PD_OK) return bad;
+  const uint64_t N = node_offset[n_particles];
+  pair_offset[0] = 0;
+  if (N == 0) {
+    for (uint32_t p = 0; p < n_particles; ++p) pair_offset[p + 1] = 0;
+    return PD_OK;
+  }
+  Dev d;
+  PairsArgs a;
+  const int rc = build_grid(pos, node_offset, radius, n_particles, d, a);
+  if (rc != PD_OK) return rc;
+  const unsigned grid = 152 * 8;
+  uint64_t *end;
+  cudaError_t e = cudaSuccess;
+  auto ck = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  ck(d.alloc(&end, N));
+  if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA, cudaGetErrorString(e));
   k_pairs<false><<<grid, kThreads, 0, d.s>>>(a);
   std::vector<uint64_t> deg(N);
   ck(cudaMemcpyAsync(deg.data(), a.deg, N * 8, cudaMemcpyDeviceToHost, d.s));
@@ -289,6 +347,34 @@ int pd_query_pairs(const double *pos, const uint64_t *node_offset, const double 
   k_sort_rows<<<grid, kThreads, 0, d.s>>>(a, end);
   ck(cudaGetLastError());
   ck(cudaMemcpyAsync(pairs, dout, 2 * M * 4, cudaMemcpyDeviceToHost, d.s));
+  ck(cudaStreamSynchronize(d.s));
+  if (e != cudaSuccess) return fail(PD_ECUDA, cudaGetErrorString(e));
+  return PD_OK;
+}
+
+int pd_query_near(const double *pos, const uint64_t *node_offset, const double *radius, uint32_t n_particles,
+                  const uint8_t *marked, uint8_t *near) {
+  if (!marked || !near) return fail(PD_EINVAL, "null argument");
+  const int bad = check_inputs(pos, node_offset, radius, n_particles);
+  if (bad != PD_OK) return bad;
+  const uint64_t N = node_offset[n_particles];
+  if (N == 0) return PD_OK;
+  Dev d;
+  PairsArgs a;
+  const int rc = build_grid(pos, node_offset, radius, n_particles, d, a);
+  if (rc != PD_OK) return rc;
+  uint8_t *dmark, *dnear;
+  cudaError_t e = cudaSuccess;
+  auto ck = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  ck(d.alloc(&dmark, N));
+  ck(d.alloc(&dnear, N));
+  if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? PD_ENOMEM : PD_ECUDA, cudaGetErrorString(e));
+  ck(cudaMemcpyAsync(dmark, marked, N, cudaMemcpyHostToDevice, d.s));
+  k_near<<<152 * 8, kThreads, 0, d.s>>>(a, dmark, dnear);
+  ck(cudaGetLastError());
+  ck(cudaMemcpyAsync(near, dnear, N, cudaMemcpyDeviceToHost, d.s));
   ck(cudaStreamSynchronize(d.s));
   if (e != cudaSuccess) return fail(PD_ECUDA, cudaGetErrorString(e));
   return PD_OK;

@@ -125,18 +125,48 @@ def bonds(pos: np.ndarray, delta: float) -> np.ndarray:
 
 
 def boundary_nodes(pos: np.ndarray, conn: np.ndarray, Rc: float) -> np.ndarray:
-    """Nodes within Rc of a surface node (gen_nonlocal_boundry_nodes, exp_dict.py:1231-1248);
-    surface nodes are those with a degree below 90% of the particle's maximum."""
-    from scipy.spatial import cKDTree
+    """Nodes within Rc of a surface node (gen_nonlocal_boundry_nodes, exp_dict.py:1231-1248),
+    ascending; surface nodes are those with a degree below 90% of the particle's maximum. The
+    test is the reference's, sqrt((dx*dx + dy*dy) + dz*dz) <= Rc in FP64: candidates from a k-d
+    tree (CPU builder) or pd_query_near (GPU builder), the same set."""
     n = len(pos)
     deg = np.bincount(conn.reshape(-1).astype(np.int64), minlength=n) if len(conn) else np.zeros(n, int)
-    edge = np.nonzero(deg < 0.9 * max(1, deg.max()))[0]
-    if len(edge) == 0:
+    marked = deg < 0.9 * max(1, deg.max())
+    if not marked.any():
         return np.zeros(0, np.uint32)
-    t = cKDTree(pos)
-    hits = t.query_ball_point(pos[edge], Rc)
-    s = sorted(set(int(j) for lst in hits for j in lst))
-    return np.asarray(s, dtype=np.uint32)
+    if _BOND_BUILDER == "gpu":
+        return np.nonzero(near_gpu([pos], [marked], [Rc])[0])[0].astype(np.uint32)
+    from scipy.spatial import cKDTree
+    edge = np.nonzero(marked)[0]
+    hits = cKDTree(pos).query_ball_point(pos[edge], Rc * (1.0 + 1e-9))
+    near = np.zeros(n, dtype=bool)
+    for e, lst in zip(edge, hits):
+        if not lst:
+            continue
+        j = np.asarray(lst, dtype=np.int64)
+        d = pos[j] - pos[e]
+        near[j[np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) <= Rc]] = True
+    return np.nonzero(near)[0].astype(np.uint32)
+
+
+def near_gpu(positions: list, marked: list, radii: list) -> list:
+    """For each point set, a bool per point: within r of one of the set's marked points
+    (pd_query_near, one GPU call for all sets)."""
+    from ._capi import lib, ptr
+    L = lib()
+    P = len(positions)
+    off = np.zeros(P + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(x) for x in positions])
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=np.float64).reshape(-1, 3) for x in positions])
+                               if P else np.zeros((0, 3)))
+    mk = np.ascontiguousarray(np.concatenate([np.asarray(m, dtype=np.uint8) for m in marked]) if P
+                              else np.zeros(0, np.uint8))
+    rad = np.ascontiguousarray(radii, dtype=np.float64)
+    out = np.zeros(max(int(off[-1]), 1), dtype=np.uint8)
+    rc = L.pd_query_near(ptr(pos), ptr(off), ptr(rad), P, ptr(mk), ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"pd_query_near: [{rc}] {L.pd_pairs_error().decode()}")
+    return [out[int(off[p]):int(off[p + 1])].astype(bool) for p in range(P)]
 
 
 def make_particle(local: np.ndarray, h: float, mat: dict, delta_factor: float, rng, jitter: float,

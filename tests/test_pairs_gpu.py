@@ -95,3 +95,58 @@ def test_generator_setups_identical_with_gpu_builder():
     for p in range(s_cpu.n_particles):
         sl = s_cpu.particle_slice(p)
         _same_up_to_boundary(s_gpu.particle_conn(p), s_cpu.particle_conn(p), s_cpu.pos[sl], 3 * s_cpu.meta["h"][p])
+
+
+def _near_formula(pos, marked, r):
+    """The reference's nonlocal boundary pass (exp_dict.py:1231-1248) as numpy evaluates it: q is
+    kept when sqrt((dx*dx + dy*dy) + dz*dz) <= r for some marked node (itself included)."""
+    near = np.zeros(len(pos), dtype=bool)
+    for e in np.nonzero(marked)[0]:
+        d = pos - pos[e]
+        near |= np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) <= r
+    return near
+
+
+def test_near_marked_nodes_equal_the_reference_test():
+    """pd_query_near on jittered lattices with random marked nodes, plus points placed within a
+    few ulps of the radius of a marked point: the same flags as the reference's test, bit for
+    bit, with several particles in one call (an empty one among them)."""
+    rng = np.random.default_rng(11)
+    sets, marks, radii = [], [], []
+    for kind, size, h in (("sphere", 1.0e-3, 1e-4), ("cube", 0.7e-3, 0.9e-4), ("ellipsoid", (1.1e-3, 0.6e-3, 0.8e-3), 1e-4)):
+        P = gen.lattice(kind, size, h) + rng.uniform(-0.05 * h, 0.05 * h, size=(len(gen.lattice(kind, size, h)), 3))
+        m = rng.random(len(P)) < 0.05
+        sets.append(P)
+        marks.append(m)
+        radii.append(0.5 * h * 1.37)
+    # a marked point and points at r * (1 + k eps) in random directions
+    r = 1e-4
+    c = np.array([[2e-3, -1e-3, 5e-4]])
+    dirs = rng.normal(size=(400, 3))
+    dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+    scale = r * (1.0 + rng.integers(-4, 5, size=400) * np.finfo(float).eps)
+    pts = np.concatenate([c, c + dirs * scale[:, None]])
+    m = np.zeros(len(pts), dtype=bool)
+    m[0] = True
+    sets += [pts, np.zeros((0, 3))]
+    marks += [m, np.zeros(0, dtype=bool)]
+    radii += [r, 1e-4]
+    got = gen.near_gpu(sets, marks, radii)
+    for P, m, rr, g in zip(sets, marks, radii, got):
+        np.testing.assert_array_equal(g, _near_formula(P, m, rr))
+    assert 0 < got[3].sum() < len(pts)  # both sides of the radius are exercised
+
+
+def test_boundary_nodes_same_with_either_builder():
+    rng = np.random.default_rng(5)
+    h = 1e-4
+    P = gen.lattice("sphere", 1.2e-3, h) + rng.uniform(-0.05 * h, 0.05 * h, size=(len(gen.lattice("sphere", 1.2e-3, h)), 3))
+    conn = gen.bonds(P, 3 * h)
+    cpu = gen.boundary_nodes(P, conn, 0.6 * h)
+    gen.set_bond_builder("gpu")
+    try:
+        gpu = gen.boundary_nodes(P, conn, 0.6 * h)
+    finally:
+        gen.set_bond_builder("cpu")
+    np.testing.assert_array_equal(cpu, gpu)
+    assert 0 < len(cpu) < len(P)
