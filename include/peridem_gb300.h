@@ -258,20 +258,18 @@ int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 /* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM,
  * lanes per node) for steps_per_variant steps from the same snapshot of the live state, restores
  * the state and keeps the fastest; then times the launch modes of pd_set_tuning the same way (the
- * persistent step with 1, 2 and 4 lanes per node and with lanes mixed by row length, where it
- * applies). Results do not depend on the variant or the mode: every form sums a node's bonds in
+ * persistent step with 1, 2 and 4 lanes per node, where it applies). Results do not depend on the variant or the mode: every form sums a node's bonds in
  * the same four blocks of its row, merged in the same order. variant_ms (may be NULL) receives
  * pd_num_variants() timings in ms per step. */
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);
 int pd_set_variant(pd_sim *sim, int variant);
 int pd_num_variants(void);
 /* Lanes per node in the bond phase of the persistent step (launch mode 3): 1, 2 or 4, or 0 (the
- * default) to mix them by row length: every 32-node slice is one warp with one lane per node,
- * except that the slices with the longest rows take 2 or 4 lanes per node (all of them 4 where
- * that fits) as long as the warps all fit on the device at once. More lanes shorten a node's
- * chain of gathers on handles too small to fill the GPU; results do not depend on it (each node's
- * bond sum is taken in four blocks of its row, merged in a fixed order). pd_autotune times 1, 2,
- * 4 and the mix. */
+ * default) to choose by size: 4 where four threads per node all fit on the device at once, else
+ * 1 (one lane per node, each partner record requested one group of bonds ahead of its use). More
+ * lanes shorten a node's chain of gathers on handles too small to fill the GPU; results do not
+ * depend on it (each node's bond sum is taken in four blocks of its row, merged in a fixed
+ * order). pd_autotune times 1, 2 and 4. */
 int pd_set_persist_lanes(pd_sim *sim, int lanes);
 int pd_persist_lanes(const pd_sim *sim);
 /* How steps are launched: 0 separate launches, 1 one CUDA graph per step, 2 a step graph whose

@@ -188,7 +188,7 @@ int Engine::init(std::vector<HostSim> &sims, int precision) {
   // default bond-kernel variant: the autotuner's choice on small and on large handles (small
   // handles are launch-latency bound and gain most from doing the non-bond work in the bond
   // kernel, one launch less per step)
-  variant_ = N_ < 131072 ? 6 : 18;
+  variant_ = N_ < 131072 ? 25 : 18;
   // and the step graph: on large handles the broad phase's kernels are worth skipping in
   // steps without a rebuild (a conditional node); small handles replay them, exiting at once.
   // Small FP32 handles step in persistent launches (where the handle's features allow it,
@@ -1120,73 +1120,20 @@ int Engine::capture_graphs() {
 // Steps per persistent launch: a launch of a small handle stays within tens of milliseconds.
 constexpr uint32_t kPersistMaxSteps = 1024;
 
-// The mixed bond phase's warp tasks: every 32-node slice is one task of one lane per node,
-// except that the slices with the longest rows are split into two tasks of two lanes or four of
-// four, as long as the tasks still fit in the resident warps; tasks are ordered longest rows
-// first, so that the warps dealt over the SMs start with them.
-int Engine::build_persist_tasks(uint64_t resident_warps) {
-  std::vector<uint16_t> deg(Ncap_);
-  PD_TRY(cpy(deg.data(), d_deg_, Ncap_ * 2, "read row lengths"));
-  const uint64_t ns = (N_ + 31) / 32;
-  std::vector<std::pair<uint32_t, uint32_t>> sl(ns);  // (longest row, slice)
-  for (uint64_t s = 0; s < ns; ++s) {
-    uint32_t m = 0;
-    for (uint64_t k = 32 * s; k < std::min<uint64_t>(N_, 32 * s + 32); ++k) m = std::max<uint32_t>(m, deg[k]);
-    sl[s] = {m, (uint32_t)s};
-  }
-  std::sort(sl.begin(), sl.end(), [](const auto &a, const auto &b) { return a.first > b.first || (a.first == b.first && a.second < b.second); });
-  // lanes per slice: all four where even that fits, else two for the longest rows while it fits
-  std::vector<int> code(ns, 0);
-  uint64_t tasks = ns;
-  if (4 * ns <= resident_warps) {  // four lanes for every slice, in node order (measured faster
-    for (uint64_t s = 0; s < ns; ++s) sl[s] = {0u, (uint32_t)s};  // than longest first here)
-    std::fill(code.begin(), code.end(), 2);
-    tasks = 4 * ns;
-  } else {
-    for (uint64_t i = 0; i < ns && tasks + 1 <= resident_warps; ++i) {
-      code[i] = 1;
-      tasks += 1;
-    }
-  }
-  std::vector<uint32_t> h;
-  h.reserve(tasks);
-  for (uint64_t i = 0; i < ns; ++i) {
-    const uint32_t node0 = 32 * sl[i].second;
-    const int parts = code[i] == 0 ? 1 : (code[i] == 1 ? 2 : 4);
-    for (int p = 0; p < parts; ++p) h.push_back((node0 + (uint32_t)(p * (32 / parts))) | (uint32_t)code[i]);
-  }
-  if (persist_tasks_) {
-    cudaFreeAsync(persist_tasks_, stream_);
-    allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)persist_tasks_), allocs_.end());
-    persist_tasks_ = nullptr;
-  }
-  PD_TRY(dalloc(this, allocs_, &persist_tasks_, std::max<uint64_t>(h.size(), 1), err));
-  PD_TRY(cpy(persist_tasks_, h.data(), h.size() * 4, "upload bond tasks"));
-  persist_ntasks_ = (uint32_t)h.size();
-  return PD_OK;
-}
-
 int Engine::launch_persist_steps(uint32_t n) {
   if (persist_grid_lanes_ != persist_lanes_ + 1) {  // (re)size the grid for these lanes
-    // the mix may launch the one- or four-lane kernel: a grid all of them can hold at once
-    const int mb = persist_lanes_ != 0 ? persist_max_blocks(persist_lanes_)
-                                       : std::min({persist_max_blocks(0), persist_max_blocks(1), persist_max_blocks(4)});
+    if (persist_lanes_ == 0) {  // four lanes per node where all threads fit at once, else one
+      const uint64_t resident = (uint64_t)persist_threads() * (uint64_t)std::max(0, persist_max_blocks(4));
+      persist_kernel_lanes_ = 4 * N_ <= resident ? 4 : 1;
+    } else {
+      persist_kernel_lanes_ = persist_lanes_;
+    }
+    const int mb = persist_max_blocks(persist_kernel_lanes_);
     if (mb <= 0) {
       err = "persistent step: no resident blocks";
       return PD_ECUDA;
     }
-    uint64_t warps;
-    persist_kernel_lanes_ = persist_lanes_;
-    if (persist_lanes_ == 0) {
-      PD_TRY(build_persist_tasks((uint64_t)mb * (uint64_t)(persist_threads() / 32)));
-      warps = persist_ntasks_;
-      // every slice alike: the kernel of that lane count (no task list to read)
-      const uint64_t ns = (N_ + 31) / 32;
-      if (persist_ntasks_ == 4 * ns) persist_kernel_lanes_ = 4;
-      else if (persist_ntasks_ == ns) persist_kernel_lanes_ = 1;
-    } else {
-      warps = (N_ * (uint64_t)persist_lanes_ + 31) / 32;
-    }
+    const uint64_t warps = (N_ * (uint64_t)persist_kernel_lanes_ + 31) / 32;
     // one block per SM, or fewer where the handle has fewer warps of work than SMs
     persist_blocks_ = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)mb, warps));
     persist_grid_lanes_ = persist_lanes_ + 1;
@@ -1222,8 +1169,6 @@ int Engine::launch_persist_steps(uint32_t n) {
   a.clamped_ptr = n_clamped_ ? d_clamped_ : nullptr;
   a.clamped = n_clamped_ ? d_clamped_ + (P_ + 1) : nullptr;
   a.clamped_disp = d_clamped_disp_;
-  a.tasks = persist_tasks_;
-  a.ntasks = persist_ntasks_;
   PD_TRY(check(cudaMemsetAsync(persist_ws_, 0, 8, stream_), "persistent barrier reset"));
   PD_TRY(check(launch_persist(a, persist_blocks_, persist_kernel_lanes_, stream_), "persistent step launch"));
   cur_ ^= (int)(n & 1);
@@ -1936,10 +1881,9 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
     bool best_cond = use_conditional_, best_persist = use_persist_;
     int best_lanes = persist_lanes_;
     // modes 1 and 2, then (where eligible) the persistent step with 1, 2 and 4 lanes per node
-    // and with lanes mixed by row length
-    const int last_mode = persist_eligible() ? 6 : 2;
+    const int last_mode = persist_eligible() ? 5 : 2;
     for (int mode = 1; mode <= last_mode; ++mode) {
-      const int lanes = mode >= 3 && mode <= 5 ? (1 << (mode - 3)) : 0;
+      const int lanes = mode >= 3 ? (1 << (mode - 3)) : 0;
       use_conditional_ = mode >= 2;
       use_persist_ = mode >= 3;
       if (mode >= 3) PD_TRY(set_persist_lanes(lanes));

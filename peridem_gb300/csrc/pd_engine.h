@@ -307,7 +307,7 @@ class Engine {
   int clear_device_errors();
   // Bond-kernel variant (FP32 form); autotune() times each on the live state and restores it.
   int set_variant(int variant);
-  // lanes per node of the persistent step's bond phase: 0 mixes them by row length, else 1, 2 or 4
+  // lanes per node of the persistent step's bond phase: 0 chooses by size, else 1, 2 or 4
   int set_persist_lanes(int lanes);
   int persist_lanes() const { return persist_lanes_; }
   int autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms);
@@ -450,11 +450,8 @@ class Engine {
   bool use_persist_ = false;        // launch mode 3 (persistent step, FP32 form)
   uint32_t *persist_ws_ = nullptr;  // its barrier counter and scan scratch
   uint32_t persist_blocks_ = 0;     // its grid
-  int persist_lanes_ = 0;           // lanes per node of its bond phase (0: mixed, by row length)
-  uint32_t *persist_tasks_ = nullptr;  // the mixed bond phase's warp tasks
-  uint32_t persist_ntasks_ = 0;
-  int persist_kernel_lanes_ = 1;    // the kernel launched (0: the task list)
-  int build_persist_tasks(uint64_t resident_warps);
+  int persist_lanes_ = 0;           // lanes per node of its bond phase (0: by size)
+  int persist_kernel_lanes_ = 1;    // the lanes of the kernel launched
   int persist_grid_lanes_ = 0;      // 1 + the lanes persist_blocks_ was sized for (0: not yet)
   int launch_persist_steps(uint32_t n);
   bool use_conditional_ = false;  // broad phase in a conditional graph node (pd_set_tuning
@@ -549,10 +546,6 @@ struct PersistArgs {
   uint32_t cap;
   const uint32_t *clamped_ptr, *clamped;
   double *clamped_disp;
-  // mixed lanes (k_persist<0>): the bond phase's warp tasks, node0 | code (node0 a multiple of 8;
-  // code 0: 32 nodes, one lane each; 1: 16 nodes, two lanes; 2: 8 nodes, four lanes)
-  const uint32_t *tasks;
-  uint32_t ntasks;
 };
 // Blocks of the persistent step with `lanes` lanes per node in its bond phase (1, 2 or 4) that
 // fit on the current device at once (0 on error), and its cooperative launch.

@@ -364,6 +364,36 @@ __device__ __forceinline__ Acc32 acc_shfl(const Acc32 &a, uint32_t src) {
 // evaluated (a broken or missing bond's are discarded), the live ones added to the block's sum in
 // position order, and -- once per group, only when some live stretch exceeds the lower edge of the
 // band around snot -- the breaking decisions taken (FP32 above the band, FP64 inside it).
+// bond_group_eval is the part after the gathers, on partner records already loaded (pq, uq; U may
+// also be 2); bond_group gathers them and evaluates the same way.
+template <int U>
+__device__ __forceinline__ void bond_group_eval(const DevView &v, uint64_t nn, const float4 &pi4, const float4 &ui4,
+                                                const uint32_t (&q)[U], const float4 (&pq)[U], const float4 (&uq)[U],
+                                                Acc32 &a, bool brk, float slo, float shi, double snot,
+                                                uint32_t *maskp, uint32_t *colw, uint32_t lane) {
+  static_assert(U == 2 || U == 4 || U == 8, "groups inside one block of the row");
+  BondTerms bt[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) bt[u] = bond32_terms(pi4, ui4, pq[u], uq[u]);
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (!(q[u] & kColBroken)) kahan_add(a, bt[u].g, bt[u].yx, bt[u].yy, bt[u].yz);
+  if (brk) {
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < U; ++u) any |= !(q[u] & kColBroken) && bt[u].str > slo;
+    if (any) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!(q[u] & kColBroken) && bt[u].str > slo) {
+          if (bt[u].str > shi) cut_bond(&maskp[u], lane, colw + 32 * u, q[u]);
+          else band_check(v, nn, q[u], &maskp[u], lane, snot, colw + 32 * u);
+        }
+      }
+    }
+  }
+}
+
 template <int U, int W, int NC = 1>
 __device__ __forceinline__ void bond_group(const DevView &v, uint64_t nn, const Rec32 *__restrict__ rec,
                                            const float4 &pi4, const float4 &ui4, const uint32_t (&q)[U], Acc32 &a,
@@ -581,6 +611,84 @@ __device__ __forceinline__ void bond_node(const DevView &v, uint64_t n) {
   }
 }
 
+// bond_node's loop with the partner records of the next load group requested before the
+// current group is evaluated and its column entries two groups ahead (small handles: with few
+// warps per SM the gathers' latency is not hidden by other warps). The same positions in the same
+// order as bond_node, the same sums. FP64 non-bond work fused; coherent loads where NC = 0.
+template <int U, int NC = 1>
+__device__ __forceinline__ void bond_node_ahead(const DevView &v, uint64_t n) {
+  const bool valid = n < v.N;
+  const uint64_t nn = valid ? n : 0;
+  const uint32_t k = v.pid[nn];
+  const DevPart &P = v.parts[k];
+  const int32_t movable = P.movable;
+  const DevSimState &st = v.ss[P.sim];
+  const bool run = valid && st.active;
+  float4 pi4, ui4;
+  ld_rec<1, NC>(v.rec + nn, pi4, ui4);
+  Acc32 tot = {};
+  uint32_t live = 0;
+  if (run && movable) {
+    const uint32_t lane = (uint32_t)(nn & 31);
+    const uint64_t sbase = v.slice_ptr[nn >> 5];
+    const uint32_t *colp = v.col + sbase + lane;
+    uint32_t *colw = const_cast<uint32_t *>(colp);
+    uint32_t *maskp = v.mask + (sbase >> 5);
+    const int dg = v.deg[nn];
+    const bool brk = st.fracture && P.breakable && P.break_bonds;
+    const float slo = P.snot_lo32, shi = P.snot_hi32;
+    const Rec32 *__restrict__ rec = v.rec;
+    if (v.stats) live = row_live(colp, dg);
+    const int cl = chain_len(dg), ng = (dg + U - 1) / U;
+    int next = cl, merged = 0;
+    Acc32 a = {};
+    uint32_t qc[U], qn[U];
+    float4 pc[U], uc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      qc[u] = u < dg ? ld_col<NC>(colp + 32 * u) : kColBroken;
+      qn[u] = U + u < dg ? ld_col<NC>(colp + 32 * (U + u)) : kColBroken;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) ld_rec<1, NC>(rec + (qc[u] & kColIndex), pc[u], uc[u]);
+    for (int g = 0; g < ng; ++g) {
+      const int j = g * U;
+      float4 pn[U], un[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) ld_rec<1, NC>(rec + (qn[u] & kColIndex), pn[u], un[u]);
+      uint32_t qnn[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) qnn[u] = j + 2 * U + u < dg ? ld_col<NC>(colp + 32 * (j + 2 * U + u)) : kColBroken;
+      if (j == next) {  // a new block of the row
+        kahan_merge(tot, a);
+        a = Acc32{};
+        next += cl;
+        ++merged;
+      }
+      bond_group_eval<U>(v, nn, pi4, ui4, qc, pc, uc, a, brk, slo, shi, P.snot, maskp + j, colw + 32 * j, lane);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        qc[u] = qn[u];
+        qn[u] = qnn[u];
+        pc[u] = pn[u];
+        uc[u] = un[u];
+      }
+    }
+    kahan_merge(tot, a);  // the last block, then the empty ones: four merges in every form
+    for (++merged; merged < 4; ++merged) kahan_merge(tot, Acc32{});
+  }
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (run) {
+    f = acc_value(tot);
+    if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
+  }
+  verlet_tail(v, nn, k, P, st, run, f, pi4, ui4);
+  if (v.stats) {
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if ((threadIdx.x & 31) == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
+  }
+}
+
 // The bond loop of bond_node with L = 2 or 4 lanes per node (small handles: few nodes, long rows,
 // so few warps that each wait on a long chain). Global thread t serves node t / L; lane s of the
 // node takes whole blocks of its row (chain_len): block s with L = 4, blocks 2s and 2s + 1 with
@@ -684,6 +792,15 @@ __device__ __forceinline__ void bond_node_split(const DevView &v, uint64_t t) {
     for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(full, live, o);
     if (lane == 0 && live) atomicAdd(&v.cnt->live_bonds, (unsigned long long)live);
   }
+}
+
+template <int U, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_bond32a(const __grid_constant__ DevView v) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && v.xcount) {
+    v.xcount[1] = 0;
+    v.cnt->xall = 0;
+  }
+  bond_node_ahead<U>(v, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <int L, int U, int MINB>
@@ -1065,15 +1182,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_con
       v.xcount[1] = 0;
       v.cnt->xall = 0;
     }
-    if constexpr (L == 0) {  // warp tasks of 1, 2 or 4 lanes per node, longest rows first
-      for (uint64_t w = gwarp; w < a.ntasks; w += nwarps) {
-        const uint32_t task = a.tasks[w], node0 = task & ~7u, code = task & 7u;
-        if (code == 0) bond_node<4, 1, 1, 1, 0>(v, (uint64_t)node0 + lane);
-        else if (code == 1) bond_node_split<2, 4, 1, 0>(v, 2ull * node0 + lane);
-        else bond_node_split<4, 4, 1, 0>(v, 4ull * node0 + lane);
-      }
-    } else if constexpr (L == 1) {
-      for (uint64_t w = gwarp; w * 32 < v.N; w += nwarps) bond_node<4, 1, 1, 1, 0>(v, w * 32 + lane);
+    if constexpr (L == 1) {  // one lane per node, partner records gathered a group ahead
+      for (uint64_t w = gwarp; w * 32 < v.N; w += nwarps) bond_node_ahead<4, 0>(v, w * 32 + lane);
     } else {  // L lanes per node (bond_node_split)
       for (uint64_t w = gwarp; w * 32 < v.N * L; w += nwarps)
         bond_node_split<L, 4, 1, 0>(v, w * 32 + lane);
@@ -1099,7 +1209,6 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_con
 
 static const void *persist_kernel(int lanes) {
   switch (lanes) {
-    case 0: return (const void *)k_persist<0>;
     case 2: return (const void *)k_persist<2>;
     case 4: return (const void *)k_persist<4>;
     default: return (const void *)k_persist<1>;
@@ -1250,8 +1359,9 @@ void launch_anchor_next(const DevView &v, cudaStream_t s) {
 
 // Bond-kernel variants the autotuner chooses from: k_bond32 <positions per load group, min
 // blocks/SM, 256-bit record loads, column prefetch, fused non-bond work> with 128-thread blocks
-// (0-9, 18-20) and with 32/64-thread blocks (14-17), and the staged k_bond32s (10-13).
-const int kNumBondVariants = 25;
+// (0-9, 18-20) and with 32/64-thread blocks (14-17), the staged k_bond32s (10-13), k_bond32l with
+// 2 or 4 lanes per node (21-24) and k_bond32a, one lane per node gathering a group ahead (25-27).
+const int kNumBondVariants = 28;
 
 int num_bond_variants() { return kNumBondVariants; }
 
@@ -1295,6 +1405,10 @@ void launch_step_fp32c(const DevView &v, int variant, cudaStream_t s) {
     case 22: k_bond32l<2, 8, 4><<<(unsigned)((2 * v.N + 127) / 128), 128, 0, s>>>(v); break;
     case 23: k_bond32l<4, 4, 4><<<(unsigned)((4 * v.N + 127) / 128), 128, 0, s>>>(v); break;
     case 24: k_bond32l<4, 8, 4><<<(unsigned)((4 * v.N + 127) / 128), 128, 0, s>>>(v); break;
+    // one lane per node, partner records gathered a group ahead (small handles)
+    case 25: k_bond32a<4, 4><<<b, 128, 0, s>>>(v); break;
+    case 26: k_bond32a<4, 4><<<(unsigned)((v.N + 31) / 32), 32, 0, s>>>(v); break;
+    case 27: k_bond32a<2, 4><<<b, 128, 0, s>>>(v); break;
     default: k_bond32<4, 4, 1, 1, 0><<<b, 128, 0, s>>>(v); break;
   }
 }

@@ -68,16 +68,18 @@ def test_persistent_step_equals_step_graph(name, chunks, lanes):
     b.close()
 
 
-def test_mixed_lanes_on_a_mid_size_aggregate():
-    """53k nodes: too many slices for four lanes each, so the slices with the longest rows take
-    two lanes and the rest one (the task-list kernel); bit-identical to the step graph."""
+@pytest.mark.parametrize("lanes", [0, 4])
+def test_lanes_on_a_mid_size_aggregate(lanes):
+    """53k nodes, more than one resident thread each for four lanes per node: lanes 0 takes one
+    lane per node (the gather-ahead loop), lanes 4 has each warp loop over several 8-node slices;
+    both bit-identical to the step graph."""
     from peridem_gb300 import gen
     s, cfg = gen.aggregate(20, seed=7, steps=100)
     a = Sim(s, cfg, "fp32c")
     b = Sim(s, cfg, "fp32c")
     a.tune(graphs=1)
     b.tune(graphs=3)
-    b.set_persist_lanes(0)
+    b.set_persist_lanes(lanes)
     a.step(30)
     b.step(30)
     _compare(a, b, s.n_particles, "aggregate 53k")
