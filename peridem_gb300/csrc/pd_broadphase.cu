@@ -135,18 +135,18 @@ __global__ void k_bp_candidates(DevView v, const uint32_t *count, const uint32_t
   bp_candidates_node(v, n, count, start, sorted, mask, cand, cand_n, cap);
 }
 
-// One warp per node (bp_candidates_warp): small handles, whose one-thread-per-node search is a
+// Four nodes per warp (bp_candidates_quad): small handles, whose one-thread-per-node search is a
 // long chain of dependent loads on few warps.
 __global__ void __launch_bounds__(128) k_bp_candidates_w(DevView v, const uint32_t *count, const uint32_t *start,
                                                          const uint32_t *sorted, uint32_t mask, uint32_t *cand,
                                                          uint16_t *cand_n, uint32_t cap) {
-  __shared__ uint32_t sh[4][kMaxCandCap + 1];
+  __shared__ uint32_t sh[4][kCandQuadWords];
   if (!v.cnt->rebuild) return;
-  // a bounded grid whose warps take nodes in turn: in steps without a rebuild the launch costs
-  // a few waves less than one warp per node would
+  // a bounded grid whose warps take groups of four nodes in turn: in steps without a rebuild the
+  // launch costs a few waves less than one warp per group would
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t n = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < v.N; n += nwarps)
-    bp_candidates_warp(v, n, threadIdx.x & 31, count, start, sorted, mask, cand, cand_n, cap, sh[threadIdx.x >> 5]);
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 4 < v.N; w += nwarps)
+    bp_candidates_quad(v, w * 4, threadIdx.x & 31, count, start, sorted, mask, cand, cand_n, cap, sh[threadIdx.x >> 5]);
 }
 
 }  // namespace
@@ -164,7 +164,7 @@ void launch_broadphase(const DevView &v, BroadPhase &bp, cudaStream_t s) {
   if (nblk) {
     k_bp_scatter<<<(unsigned)nblk, 256, 0, s>>>(v, bp.start, bp.key, bp.slot, bp.sorted);
     if (v.N <= kWarpCandNodes)
-      k_bp_candidates_w<<<(unsigned)std::min<uint64_t>((v.N + 3) / 4, 152 * 8), 128, 0, s>>>(
+      k_bp_candidates_w<<<(unsigned)std::min<uint64_t>((v.N + 15) / 16, 152 * 8), 128, 0, s>>>(
           v, bp.count, bp.start, bp.sorted, mask, bp.cand, bp.cand_n, bp.cand_cap);
     else
       k_bp_candidates<<<(unsigned)((v.N + 127) / 128), 128, 0, s>>>(v, bp.count, bp.start, bp.sorted, mask,

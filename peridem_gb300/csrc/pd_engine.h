@@ -524,8 +524,8 @@ class Engine {
   bool graphs_ok_ = false;
 };
 
-// Handles up to this many nodes search contact candidates with one warp per node
-// (bp_candidates_warp), larger ones with one thread per node; the lists are the same.
+// Handles up to this many nodes search contact candidates with four nodes per warp
+// (bp_candidates_quad), larger ones with one thread per node; the lists are the same.
 constexpr uint64_t kWarpCandNodes = 1ull << 20;
 // Handles of at least this many nodes read their state back through pinned host memory.
 constexpr uint64_t kPinnedStageNodes = 1ull << 18;

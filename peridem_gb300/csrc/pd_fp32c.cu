@@ -1169,10 +1169,10 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_con
       if (!persist_scan(a, bar) || !bar.sync()) return;
       for (uint64_t n = gtid; n < v.N; n += gsize) bp_scatter_node(n, a.start, a.key, a.slot, a.sorted);
       if (!bar.sync()) return;
-      {  // one warp per node
-        __shared__ uint32_t csh[kPersistThreads / 32][kMaxCandCap + 1];
-        for (uint64_t n = gwarp; n < v.N; n += nwarps)
-          bp_candidates_warp(v, n, lane, a.count, a.start, a.sorted, a.mask, a.cand, a.cand_n, a.cap,
+      {  // four nodes per warp
+        __shared__ uint32_t csh[kPersistThreads / 32][kCandQuadWords];
+        for (uint64_t w = gwarp; w * 4 < v.N; w += nwarps)
+          bp_candidates_quad(v, w * 4, lane, a.count, a.start, a.sorted, a.mask, a.cand, a.cand_n, a.cap,
                              csh[threadIdx.x >> 5]);
       }
       if (!bar.sync()) return;
