@@ -258,7 +258,9 @@ int pd_profile_steps(pd_sim *sim, uint32_t nsteps, double *phase_ms);
 /* Autotuner: times every bond-kernel variant (loads issued per group, minimum blocks per SM,
  * lanes per node) for steps_per_variant steps from the same snapshot of the live state, restores
  * the state and keeps the fastest; then times the launch modes of pd_set_tuning the same way (the
- * persistent step with 1, 2 and 4 lanes per node, where it applies). Results do not depend on the variant or the mode: every form sums a node's bonds in
+ * persistent step with 1, 2 and 4 lanes per node, where it applies); then, where the contact
+ * candidate lists were rebuilt while the chosen mode stepped, the contact skin at 1.5 and 2 times
+ * its value (over at least 24 steps each). Results do not depend on the variant or the mode: every form sums a node's bonds in
  * the same four blocks of its row, merged in the same order. variant_ms (may be NULL) receives
  * pd_num_variants() timings in ms per step. */
 int pd_autotune(pd_sim *sim, uint32_t steps_per_variant, int *chosen, double *variant_ms);

@@ -1920,6 +1920,49 @@ int Engine::autotune(uint32_t steps_per_variant, int *chosen, double *variant_ms
     PD_TRY(set_persist_lanes(best_persist ? best_lanes : 0));
     graphs_ok_ = false;
   }
+  // contact skin: a wider skin rebuilds the candidate lists less often but makes them longer.
+  // Where the lists were rebuilt while the chosen mode stepped, 1.5 and 2 times the skin are timed
+  // as well, each from the same snapshot over enough steps to span several rebuilds (results do
+  // not depend on the skin)
+  {
+    cudaEvent_t e0, e1;
+    PD_TRY(check(cudaEventCreate(&e0), "event"));
+    PD_TRY(check(cudaEventCreate(&e1), "event"));
+    const uint32_t ks = std::max<uint32_t>(steps_per_variant, 24);
+    const double skin0 = bp_.skin_frac;
+    double best_skin = skin0;
+    float best_skin_ms = 0;
+    bool rebuilt = false;
+    int rc = PD_OK;
+    for (int i = 0; i < 3 && rc == PD_OK; ++i) {
+      if (i > 0 && !rebuilt) break;
+      const double skin = skin0 * (i == 0 ? 1.0 : i == 1 ? 1.5 : 2.0);
+      unsigned long long r0 = 0, r1 = 0;
+      rc = set_tuning(skin, 0, 0, -1, -1);
+      if (rc == PD_OK) rc = step(2);
+      if (rc == PD_OK) rc = check(cudaStreamSynchronize(stream_), "sync");
+      if (rc == PD_OK) rc = cpy(&r0, &d_cnt_->rebuilds, sizeof(r0), "read rebuilds");
+      if (rc == PD_OK) rc = check(cudaEventRecord(e0, stream_), "event");
+      if (rc == PD_OK) rc = step(ks);
+      if (rc == PD_OK) rc = check(cudaEventRecord(e1, stream_), "event");
+      if (rc == PD_OK) rc = check(cudaEventSynchronize(e1), "event");
+      if (rc == PD_OK) rc = cpy(&r1, &d_cnt_->rebuilds, sizeof(r1), "read rebuilds");
+      float ms = 0;
+      if (rc == PD_OK) cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == PD_OK) {
+        if (i == 0) rebuilt = r1 > r0;
+        if (i == 0 || ms < best_skin_ms) {
+          best_skin_ms = ms;
+          best_skin = skin;
+        }
+      }
+      if (rc == PD_OK) rc = restore();
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    PD_TRY(rc);
+    PD_TRY(set_tuning(best_skin, 0, 0, -1, -1));
+  }
   return PD_OK;
 }
 

@@ -137,8 +137,9 @@ class Sim:
         return out
 
     def autotune(self, steps_per_variant: int = 8) -> tuple[int, np.ndarray]:
-        """Times every bond-kernel variant on the live state (restored afterwards); keeps the
-        fastest. Returns (chosen, ms per step of each variant)."""
+        """Times every bond-kernel variant on the live state (restored afterwards) and keeps the
+        fastest, then the launch modes and, where the contact candidate lists were rebuilt while
+        stepping, wider contact skins. Returns (chosen variant, ms per step of each variant)."""
         nv = lib().pd_num_variants()
         ms = np.zeros(nv)
         ch = C.c_int()

@@ -161,6 +161,23 @@ def test_persistent_mode_falls_back_where_not_eligible(precision, stats):
     a.close()
 
 
+def test_autotune_with_rebuilds_keeps_results():
+    """Two small spheres colliding in a wall box rebuild their candidate lists every few steps, so
+    the autotuner also times wider contact skins; whatever it keeps, the results equal the untuned
+    step graph's."""
+    s, cfg = cases.impact_walls()
+    a = Sim(s, cfg, "fp32c")
+    b = Sim(s, cfg, "fp32c")
+    b.autotune(2)
+    a.tune(graphs=1)
+    a.step(25)
+    b.step(25)
+    _compare(a, b, s.n_particles, "autotuned with rebuilds")
+    assert b.stats()["rebuilds"] > 0
+    a.close()
+    b.close()
+
+
 def test_autotune_may_pick_the_persistent_step():
     s, cfg = cases.cubes_gravity()
     a = Sim(s, cfg, "fp32c")
