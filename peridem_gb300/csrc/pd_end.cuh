@@ -184,8 +184,12 @@ __device__ __forceinline__ void end_particle_warp(const DevView &v, uint32_t k, 
 
 // After every particle's end of step: the simulations advance (walls, step index, sticky
 // toggles, timeloop.h:785-797) and the broad phase's movement bookkeeping. Threads tid of
-// nthreads share the simulations.
-__device__ __forceinline__ void end_step_advance(const DevView &v, uint32_t tid, uint32_t nthreads) {
+// nthreads share the simulations; the last of them takes the counters, beside the first's
+// simulation. With decide, the counters also take the next step's rebuild decision and restart
+// its per-step counts, as bp_decide would at the start of that step (this step's bound having
+// just restarted at 0).
+__device__ __forceinline__ void end_step_advance(const DevView &v, uint32_t tid, uint32_t nthreads,
+                                                 bool decide = false, double half_skin = 0.0) {
   for (uint32_t s = tid; s < v.S; s += nthreads) {
     const DevSimParams &sp = v.sp[s];
     DevSimState &st = v.ss[s];
@@ -195,19 +199,25 @@ __device__ __forceinline__ void end_step_advance(const DevView &v, uint32_t tid,
       apply_sim_toggles(sp, st, st.t);
     }
   }
-  if (tid == 0) {
+  if (tid == nthreads - 1) {
     DevCounters &c = *v.cnt;
-    double stepmax = __longlong_as_double((long long)c.stepmax_bits);
+    const double stepmax = __longlong_as_double((long long)c.stepmax_bits);
+    double moved;
     if (c.rebuild) {
       // with the fused predictor, stepmax already bounds the next step's movement
-      c.moved = v.fused ? stepmax : 0.0;
+      moved = v.fused ? stepmax : 0.0;
       c.rebuilds += 1;
     } else {
-      c.moved += stepmax;
+      moved = c.moved + stepmax;
     }
+    c.moved = moved;
     c.last_stepmax = stepmax;
     c.stepmax_bits = 0;
-    c.rebuild = 0;
+    c.rebuild = decide && moved > half_skin ? 1u : 0u;  // bp_decide: moved + 0 against half the skin
+    if (decide) {
+      c.contacts = 0;
+      c.live_bonds = 0;
+    }
     c.end_blocks = 0;
   }
 }

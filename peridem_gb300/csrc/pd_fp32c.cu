@@ -1032,9 +1032,10 @@ struct GridBarrier {
     return !(*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT);
   }
 
-  // Thread 0: arrive; returns the number of blocks arrived so far, this one included.
+  // Thread 0, after a block barrier: arrive; returns the number of blocks arrived so far, this one
+  // included. The release half of the atomic publishes the block's writes (ordered before it by
+  // the block barrier), its acquire half lets the last arrival see every other block's.
   __device__ uint32_t arrive() {
-    __threadfence();
     uint32_t seen;
     asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(seen) : "l"(count) : "memory");
     return seen + 1;
@@ -1047,7 +1048,6 @@ struct GridBarrier {
     if (threadIdx.x == 0) {
       const uint32_t seen = arrive();
       ok = (seen >= target || wait_for(count, target)) ? 1u : 0u;
-      __threadfence();
     }
     __syncthreads();
     return ok != 0;
@@ -1060,22 +1060,17 @@ struct GridBarrier {
     target += gridDim.x;
     ++release;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      last = arrive() == target ? 1u : 0u;
-      __threadfence();
-    }
+    if (threadIdx.x == 0) last = arrive() == target ? 1u : 0u;
     __syncthreads();
     if (last) {
       fn();
       __syncthreads();
       if (threadIdx.x == 0) {
-        __threadfence();
         asm volatile("st.release.gpu.u32 [%0], %1;" ::"l"(count + 1), "r"(release) : "memory");
         ok = !(*(volatile uint32_t *)err & PD_DERR_BARRIER_TIMEOUT);
       }
     } else if (threadIdx.x == 0) {
       ok = wait_for(count + 1, release) ? 1u : 0u;
-      __threadfence();
     }
     __syncthreads();
     return ok != 0;
@@ -1188,20 +1183,26 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_persist(const __grid_con
       for (uint64_t w = gwarp; w * 32 < v.N * L; w += nwarps)
         bond_node_split<L, 4, 1, 0>(v, w * 32 + lane);
     }
-    if (!bar.sync()) return;
-    // end of step, one warp per particle; the last block to arrive at the barrier advances the
-    // simulations and takes the next step's rebuild decision (k_end_step_w, k_bp_decide)
-    for (uint64_t k = gwarp; k < v.P; k += nwarps) end_particle_warp(v, (uint32_t)k, lane);
+    // end of step, one warp per particle (k_end_step_w): after one more barrier over all blocks,
+    // or, for a handle of at most one particle per warp of a block, in the last block to arrive
+    // at the end barrier (one barrier less per step). That block then advances the simulations
+    // and takes the next step's rebuild decision (k_bp_decide).
+    const bool fold = v.P <= kPersistThreads / 32;
+    if (!fold) {
+      if (!bar.sync()) return;
+      for (uint64_t k = gwarp; k < v.P; k += nwarps) end_particle_warp(v, (uint32_t)k, lane);
+    }
     const bool more = step + 1 < a.nsteps;
     const DevView &vn = a.v[(a.cur0 + step + 1) & 1];
     if (!bar.sync_last([&] {
-          end_step_advance(v, threadIdx.x, blockDim.x);
-          if (more) {
+          if (fold) {
+            if ((threadIdx.x >> 5) < v.P) end_particle_warp(v, threadIdx.x >> 5, lane);
             __syncthreads();
-            if (threadIdx.x == 0) bp_decide(vn, a.half_skin);
+          }
+          end_step_advance(v, threadIdx.x, blockDim.x, more, a.half_skin);
+          if (more)  // the next step's wall reactions restart (other fields than the advance's)
             for (uint32_t i = threadIdx.x; i < vn.S; i += blockDim.x)
               for (int k = 0; k < 18; ++k) vn.ss[i].react[k] = 0.0;
-          }
         }))
       return;
   }
