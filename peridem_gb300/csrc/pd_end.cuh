@@ -117,18 +117,21 @@ __device__ __forceinline__ void end_step_particle(const DevView &v, uint32_t k, 
 __device__ __forceinline__ void end_particle_warp(const DevView &v, uint32_t k, uint32_t lane) {
   const unsigned full = 0xffffffffu;
   DevPart &P = v.parts[k];
-  const uint32_t sim = P.sim;
+  const uint32_t sim = v.S == 1 ? 0u : P.sim;  // one simulation: its state loads need not wait for P
   const DevSimState &st = v.ss[sim];
   const DevSimParams &sp = v.sp[sim];
   unsigned int *L = v.lrtb_local_next + 6 * (uint64_t)k;
   const uint64_t k3 = 3 * (uint64_t)k;
   const unsigned int key = lane < 6 ? L[lane] : 0u;
   double an = 0.0, ann = 0.0, dn = 0.0, apos = 0.0;
+  double blo = 0.0, bhi = 0.0;  // lanes < 3: coordinate lane of the particle's box, as kept below
   if (lane < 3) {
     an = v.anchor[k3 + lane];
     ann = v.anchor_next[k3 + lane];
     dn = v.disp_next[P.anchor + lane * v.Ncap];
     apos = P.anchor_pos[lane];
+    blo = v.lrtb[6 * (uint64_t)k + lane];
+    bhi = v.lrtb[6 * (uint64_t)k + 3 + lane];
   }
   const double move = __longlong_as_double((long long)v.cnt->stepmax_bits);  // this step's bound
   if (!st.active) return;
@@ -143,8 +146,10 @@ __device__ __forceinline__ void end_particle_warp(const DevView &v, uint32_t k, 
     const float lo = fval(klo), hi = fval(khi);
     const double base = apos + an;
     const double w = __dadd_rn(__dmul_rn(8.0 * (double)FLT_EPSILON, fmax(fabs((double)lo), fabs((double)hi))), 1e-30);
-    v.lrtb[6 * (uint64_t)k + lane] = base + (double)lo - w;
-    v.lrtb[6 * (uint64_t)k + 3 + lane] = base + (double)hi + w;
+    blo = base + (double)lo - w;
+    bhi = base + (double)hi + w;
+    v.lrtb[6 * (uint64_t)k + lane] = blo;
+    v.lrtb[6 * (uint64_t)k + 3 + lane] = bhi;
     ext = fmax(fabs((double)lo), fabs((double)hi)) + w;
   }
   for (int o = 1; o < 4; o <<= 1) ext = fmax(ext, __shfl_xor_sync(full, ext, o));
@@ -158,24 +163,30 @@ __device__ __forceinline__ void end_particle_warp(const DevView &v, uint32_t k, 
     v.anchor_next[k3 + lane] = dn;
   }
   // per-particle toggles for the next step (timeloop.h:481-498)
+  int32_t mov = movable, stop = P.stoppable;  // the flags after the toggles
   if (lane == 0) {
     const uint32_t kl = k - sp.p0;
-    if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn)
+    if (sp.set_movable_index != -1 && (uint32_t)sp.set_movable_index == kl && (uint32_t)sp.set_movable_ts == tn) {
       P.movable = 1;
+      mov = 1;
+    }
     if (sp.set_stoppable_index != -1 && (uint32_t)sp.set_stoppable_index == kl &&
-        (uint32_t)sp.set_stoppable_ts == tn)
+        (uint32_t)sp.set_stoppable_ts == tn) {
       P.stoppable = 1;
+      stop = 1;
+    }
   }
-  __syncwarp();
-  // work list of particles with FP64 non-bond work next step (end_step_particle)
+  mov = __shfl_sync(full, mov, 0);
+  stop = __shfl_sync(full, stop, 0);
+  // work list of particles with FP64 non-bond work next step (end_step_particle); the box and
+  // flags come from the lanes that computed them, not back from memory
+  const double lo_c = __shfl_sync(full, blo, c), hi_c = __shfl_sync(full, bhi, c);
   if (v.xparts) {
     const bool torque_next = st.torque || (sp.set_torque_ts != -1 && tn == (uint32_t)sp.set_torque_ts);
-    const int32_t mov = *(volatile int32_t *)&P.movable, stop = *(volatile int32_t *)&P.stoppable;
     bool need = (mov && P.has_ext) || torque_next;
     if (!need && mov && stop && sp.allow_wall) {
       const double lim = __dadd_rn(__dadd_rn(__dmul_rn(sp.Rc, 1.001), __dmul_rn(2.0, move)), 1e-12);
-      const volatile double *b = v.lrtb + 6 * (uint64_t)k;
-      const bool hit = lane < 6 && (b[c] - lim <= wn) && (b[3 + c] + lim >= wn);
+      const bool hit = lane < 6 && (lo_c - lim <= wn) && (hi_c + lim >= wn);
       need = __any_sync(full, hit);
     }
     if (need && lane == 0) v.xparts[atomicAdd(&v.xcount[1], 1u)] = k;

@@ -622,35 +622,37 @@ __device__ __forceinline__ void bond_node_ahead(const DevView &v, uint64_t n) {
   const uint32_t k = v.pid[nn];
   const DevPart &P = v.parts[k];
   const int32_t movable = P.movable;
-  const DevSimState &st = v.ss[P.sim];
+  const DevSimState &st = v.ss[v.S == 1 ? 0u : P.sim];  // one simulation: no wait for P
   const bool run = valid && st.active;
   float4 pi4, ui4;
   ld_rec<1, NC>(v.rec + nn, pi4, ui4);
+  // the row's first two groups of column entries and the first group's partner records are
+  // requested before the node's flags arrive (any node's row is a valid address)
+  const uint32_t lane = (uint32_t)(nn & 31);
+  const uint64_t sbase = v.slice_ptr[nn >> 5];
+  const uint32_t *colp = v.col + sbase + lane;
+  const int dg = v.deg[nn];
+  const Rec32 *__restrict__ rec = v.rec;
+  uint32_t qc[U], qn[U];
+  float4 pc[U], uc[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    qc[u] = u < dg ? ld_col<NC>(colp + 32 * u) : kColBroken;
+    qn[u] = U + u < dg ? ld_col<NC>(colp + 32 * (U + u)) : kColBroken;
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) ld_rec<1, NC>(rec + (qc[u] & kColIndex), pc[u], uc[u]);
   Acc32 tot = {};
   uint32_t live = 0;
   if (run && movable) {
-    const uint32_t lane = (uint32_t)(nn & 31);
-    const uint64_t sbase = v.slice_ptr[nn >> 5];
-    const uint32_t *colp = v.col + sbase + lane;
     uint32_t *colw = const_cast<uint32_t *>(colp);
     uint32_t *maskp = v.mask + (sbase >> 5);
-    const int dg = v.deg[nn];
     const bool brk = st.fracture && P.breakable && P.break_bonds;
     const float slo = P.snot_lo32, shi = P.snot_hi32;
-    const Rec32 *__restrict__ rec = v.rec;
     if (v.stats) live = row_live(colp, dg);
     const int cl = chain_len(dg), ng = (dg + U - 1) / U;
     int next = cl, merged = 0;
     Acc32 a = {};
-    uint32_t qc[U], qn[U];
-    float4 pc[U], uc[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      qc[u] = u < dg ? ld_col<NC>(colp + 32 * u) : kColBroken;
-      qn[u] = U + u < dg ? ld_col<NC>(colp + 32 * (U + u)) : kColBroken;
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) ld_rec<1, NC>(rec + (qc[u] & kColIndex), pc[u], uc[u]);
     for (int g = 0; g < ng; ++g) {
       const int j = g * U;
       float4 pn[U], un[U];
@@ -709,7 +711,7 @@ __device__ __forceinline__ void bond_node_split(const DevView &v, uint64_t t) {
   const uint32_t k = v.pid[nn];
   const DevPart &P = v.parts[k];
   const int32_t movable = P.movable;
-  const DevSimState &st = v.ss[P.sim];
+  const DevSimState &st = v.ss[v.S == 1 ? 0u : P.sim];  // one simulation: no wait for P
   const bool run = valid && st.active;
   const uint64_t C3 = v.Ncap;
   float4 pi4, ui4;

@@ -56,11 +56,12 @@ def test_fp64_bitexact(name):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
-@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("name", ["impact_walls", "cubes_gravity"])
 def test_launch_modes_give_the_same_results(name, mode, precision):
-    """Separate launches (0) and the step graph with the broad phase in a conditional node (2,
-    the default on large handles) against the plain step graph (1), rebuilds included."""
+    """Separate launches (0), the step graph with the broad phase in a conditional node (2, the
+    default on large handles) and the persistent step (3, the FP32 default on small handles; FP64
+    handles fall back to 2) against the plain step graph (1), rebuilds included."""
     s, cfg = cases.CASES[name]()
     a = Sim(s, cfg, precision)
     b = Sim(s, cfg, precision)
@@ -68,8 +69,10 @@ def test_launch_modes_give_the_same_results(name, mode, precision):
     b.tune(graphs=mode)
     a.step(25)
     b.step(25)
-    if mode == 2:
+    if mode == 2 or (mode == 3 and precision == "fp64"):
         assert b.graph_mode() in (1, 2)  # 1 where the conditional node is unsupported
+    if mode == 3 and precision == "fp32c":
+        assert b.graph_mode() == 3
     sa, sb = a.state(), b.state()
     for k in sa:
         np.testing.assert_array_equal(sa[k], sb[k])

@@ -161,6 +161,26 @@ def test_persistent_mode_falls_back_where_not_eligible(precision, stats):
     a.close()
 
 
+@pytest.mark.parametrize("workload", ["two_sphere", "cubes125"])
+def test_small_benchmark_configurations_equal_step_graph(workload):
+    """The two small benchmark configurations at full size (8,338 and 64,000 nodes): the default
+    launch (the persistent step) and the autotuned one equal the plain step graph bit for bit."""
+    from peridem_gb300 import gen
+    s, cfg = getattr(gen, workload)()
+    a = Sim(s, cfg, "fp32c")
+    b = Sim(s, cfg, "fp32c")
+    c = Sim(s, cfg, "fp32c")
+    a.tune(graphs=1)
+    c.autotune(2)
+    for x in (a, b, c):
+        x.step(40)
+    assert b.graph_mode() == 3
+    _compare(a, b, s.n_particles, workload + " default")
+    _compare(a, c, s.n_particles, workload + " autotuned")
+    for x in (a, b, c):
+        x.close()
+
+
 def test_autotune_with_rebuilds_keeps_results():
     """Two small spheres colliding in a wall box rebuild their candidate lists every few steps, so
     the autotuner also times wider contact skins; whatever it keeps, the results equal the untuned
