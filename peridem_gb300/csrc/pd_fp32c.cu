@@ -43,82 +43,150 @@ __device__ __forceinline__ bool extra_needed(const DevView &v, uint64_t n, uint3
   return false;
 }
 
-// FP64 non-bond force density of node n in the reference's order: self-contact
-// (timeloop.h:554-557), walls (contact.h:1060-1124), external force and torque
-// (timeloop.h:582-633), then contact with the other particles in ascending partner order
-// (timeloop.h:637-651). Kept out of line: the bond kernel calls it only for nodes that need it.
-__device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
-  const uint32_t k = v.pid[n];
-  const DevPart &P = v.parts[k];
-  const DevSimParams &sp = v.sp[P.sim];
-  DevSimState &st = v.ss[P.sim];
-  const bool nc = v.cand_n[n] != 0;  // contact candidates (a list, or the cell walk)
-  const bool mov = P.movable != 0;
-  bool wall_near = false;
-  if (mov && P.stoppable && sp.allow_wall) {
+// The node-level inputs of extra_force.
+struct ExtraCtx {
+  uint32_t k;
+  bool nc, mov, wall_near, ext, bdry_i;
+  D3 di, pi, vi;
+  double voli;
+};
+
+__device__ __forceinline__ ExtraCtx extra_ctx(const DevView &v, uint64_t n, const DevPart &P,
+                                              const DevSimParams &sp) {
+  ExtraCtx c;
+  c.k = v.pid[n];
+  c.nc = v.cand_n[n] != 0;  // contact candidates (a list, or the cell walk)
+  c.mov = P.movable != 0;
+  c.wall_near = false;
+  if (c.mov && P.stoppable && sp.allow_wall) {
     const float4 pl = v.rec[n].p, ul = v.rec[n].u;
     const float cx = pl.x + ul.x, cy = pl.y + ul.y, cz = pl.z + ul.z;
-    const float *wl = v.wall_local + 6 * (uint64_t)k;
+    const float *wl = v.wall_local + 6 * (uint64_t)c.k;
     const float lim = (float)sp.Rc * 1.001f;
-    wall_near = fabsf(cx - wl[0]) <= lim || fabsf(cx - wl[3]) <= lim || fabsf(cy - wl[1]) <= lim ||
-                fabsf(cy - wl[4]) <= lim || fabsf(cz - wl[2]) <= lim || fabsf(cz - wl[5]) <= lim;
+    c.wall_near = fabsf(cx - wl[0]) <= lim || fabsf(cx - wl[3]) <= lim || fabsf(cy - wl[1]) <= lim ||
+                  fabsf(cy - wl[4]) <= lim || fabsf(cz - wl[2]) <= lim || fabsf(cz - wl[5]) <= lim;
   }
-  const bool ext = mov && P.has_ext;
+  c.ext = c.mov && P.has_ext;
   const uint64_t C3 = v.Ncap;
-  const D3 di = ld3(v.disp, n, C3), pi = ld3(v.pos, n, C3), vi = ld3(v.vel_in, n, C3);
-  const double voli = v.vol[n];
-  const bool bdry_i = v.bdry[n] != 0;
-  D3 f = d3(0.0, 0.0, 0.0);
-  if (mov) {
-    if (nc && st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || bdry_i)) {
-      CandWalk walk(v, n);
-      uint32_t m;
-      while (walk.next(m)) {
-        if (m < P.g0) continue;
-        if (m >= P.g0 + P.n) break;
-        if (sp.nl_bdry_only && !v.bdry[m]) continue;
-        D3 xi = ld3(v.pos, m, C3) - pi;
-        D3 dir = (ld3(v.disp, m, C3) - di) + xi;
-        const double q = sq3(dir);
-        if (q >= sp.rc2_far) continue;  // outside Rc for certain: skip the square root
-        double dn = sqrt(q);
-        if (!(dn <= sp.Rc)) continue;
-        double xin = norm3(xi);
-        double len_ref = sp.Rc, sc = sp.sc;
-        if (row_has_live(v, n, m)) continue;
-        if (xin < sp.Rc) {
-          len_ref = xin;
-          sc = P.cnot;
-        }
-        if (!(dn < len_ref)) continue;
-        PairForce pf;
-        pair_force(dir, dn, len_ref, sc, v.vol[m], P.rho, vi, ld3(v.vel_in, m, C3), sp, st, pf);
-        if (P.stoppable) {
-          f = f + pf.fc;
-          if (pf.has_fd) f = f + pf.fd;
-          if (pf.has_ff) f = f + pf.ff;
-        }
-      }
+  c.di = ld3(v.disp, n, C3);
+  c.pi = ld3(v.pos, n, C3);
+  c.vi = ld3(v.vel_in, n, C3);
+  c.voli = v.vol[n];
+  c.bdry_i = v.bdry[n] != 0;
+  return c;
+}
+
+// One contact candidate's share of the node's force: the pair's forces and how they enter the
+// sum (kind 0: not at all; 1: added, in the self-contact loop and for a partner of a later
+// particle; 2: subtracted with the volume scaling, for a partner of an earlier particle).
+struct CandShare {
+  PairForce pf;
+  double volm;
+  int kind;
+};
+
+// Candidate m of node n in extra_force's self-contact loop (self) or contact loop (!self): the
+// loop's tests and its pair_force call (contact.h:746-942).
+__device__ __forceinline__ CandShare cand_share(const DevView &v, uint64_t n, const DevPart &P,
+                                                const DevSimParams &sp, const DevSimState &st, const ExtraCtx &c,
+                                                uint32_t m, bool self) {
+  CandShare o;
+  o.pf.fc = o.pf.fd = o.pf.ff = d3(0.0, 0.0, 0.0);
+  o.pf.has_fd = o.pf.has_ff = false;
+  o.volm = 0.0;
+  o.kind = 0;
+  const uint64_t C3 = v.Ncap;
+  const bool own = m >= P.g0 && m < P.g0 + P.n;
+  if (self) {  // self-contact with the particle's own nodes that are not bonded to n
+    if (!own) return o;
+    if (sp.nl_bdry_only && !v.bdry[m]) return o;
+    D3 xi = ld3(v.pos, m, C3) - c.pi;
+    D3 dir = (ld3(v.disp, m, C3) - c.di) + xi;
+    const double q = sq3(dir);
+    if (q >= sp.rc2_far) return o;  // outside Rc for certain: skip the square root
+    double dn = sqrt(q);
+    if (!(dn <= sp.Rc)) return o;
+    double xin = norm3(xi);
+    double len_ref = sp.Rc, sc = sp.sc;
+    if (row_has_live(v, n, m)) return o;
+    if (xin < sp.Rc) {
+      len_ref = xin;
+      sc = P.cnot;
     }
-    if (wall_near && !within_interior(v.lrtb + 6 * (uint64_t)k, st.wall, sp.Rc) && (!sp.nl_bdry_only || bdry_i)) {
-      D3 cur = pi + di;
+    if (!(dn < len_ref)) return o;
+    pair_force(dir, dn, len_ref, sc, v.vol[m], P.rho, c.vi, ld3(v.vel_in, m, C3), sp, st, o.pf);
+    if (P.stoppable) o.kind = 1;
+    return o;
+  }
+  if (own) return o;
+  const uint32_t km = v.pid[m];
+  const uint32_t a = km < c.k ? km : c.k, b = km < c.k ? c.k : km;
+  if (!(v.parts[a].movable || v.parts[b].movable)) return o;
+  if (!intersects_fext(v.lrtb + 6 * (uint64_t)a, v.lrtb + 6 * (uint64_t)b, sp.Rc)) return o;
+  if (sp.nl_bdry_only && !v.bdry[m]) return o;
+  const D3 pm = ld3(v.pos, m, C3), dm = ld3(v.disp, m, C3);
+  if (km > c.k) {
+    D3 dir = (dm - c.di) + (pm - c.pi);
+    const double q = sq3(dir);
+    if (q >= sp.rc2_far) return o;
+    double dn = sqrt(q);
+    if (!(dn < sp.Rc)) return o;
+    pair_force(dir, dn, sp.Rc, sp.sc, v.vol[m], P.rho, c.vi, ld3(v.vel_in, m, C3), sp, st, o.pf);
+    o.kind = 1;
+    if (v.stats) atomicAdd(&v.cnt->contacts, 1ull);
+  } else {
+    D3 dir = (c.di - dm) + (c.pi - pm);
+    const double q = sq3(dir);
+    if (q >= sp.rc2_far) return o;
+    double dn = sqrt(q);
+    if (!(dn < sp.Rc)) return o;
+    o.volm = v.vol[m];
+    pair_force(dir, dn, sp.Rc, sp.sc, c.voli, v.parts[km].rho, ld3(v.vel_in, m, C3), c.vi, sp, st, o.pf);
+    o.kind = 2;
+  }
+  return o;
+}
+
+// Adds a candidate's share to the running sum f, in the loops' order of operations.
+__device__ __forceinline__ void apply_share(D3 &f, const CandShare &s, double voli) {
+  if (s.kind == 1) {
+    f = f + s.pf.fc;
+    if (s.pf.has_fd) f = f + s.pf.fd;
+    if (s.pf.has_ff) f = f + s.pf.ff;
+  } else if (s.kind == 2) {
+    const double volm = s.volm;
+    f = f - (s.pf.fc / voli) * volm;
+    if (s.pf.has_fd) f = f - (s.pf.fd / sqrt(voli)) * sqrt(volm);
+    if (s.pf.has_ff) f = f - s.pf.ff;
+  }
+}
+
+// The part of extra_force between the two candidate loops: walls and external force of a
+// movable node, then torque.
+__device__ __forceinline__ void extra_middle(const DevView &v, uint64_t n, const DevPart &P, const DevSimParams &sp,
+                                             DevSimState &st, const ExtraCtx &c, D3 &f) {
+  const uint64_t C3 = v.Ncap;
+  if (c.mov) {
+    if (c.wall_near && !within_interior(v.lrtb + 6 * (uint64_t)c.k, st.wall, sp.Rc) &&
+        (!sp.nl_bdry_only || c.bdry_i)) {
+      D3 cur = c.pi + c.di;
       const bool rx = sp.compute_wall_reaction != 0;
-      wall_face(cur.x - st.wall[0], 0, vi, voli, P.rho, f, st.spd[0], 0, sp, st, rx);
-      wall_face(cur.x - st.wall[3], 0, vi, voli, P.rho, f, st.spd[3], 3, sp, st, rx);
-      wall_face(cur.y - st.wall[1], 1, vi, voli, P.rho, f, st.spd[1], 1, sp, st, rx);
-      wall_face(cur.y - st.wall[4], 1, vi, voli, P.rho, f, st.spd[4], 4, sp, st, rx);
-      wall_face(cur.z - st.wall[2], 2, vi, voli, P.rho, f, st.spd[2], 2, sp, st, rx);
-      wall_face(cur.z - st.wall[5], 2, vi, voli, P.rho, f, st.spd[5], 5, sp, st, rx);
+      wall_face(cur.x - st.wall[0], 0, c.vi, c.voli, P.rho, f, st.spd[0], 0, sp, st, rx);
+      wall_face(cur.x - st.wall[3], 0, c.vi, c.voli, P.rho, f, st.spd[3], 3, sp, st, rx);
+      wall_face(cur.y - st.wall[1], 1, c.vi, c.voli, P.rho, f, st.spd[1], 1, sp, st, rx);
+      wall_face(cur.y - st.wall[4], 1, c.vi, c.voli, P.rho, f, st.spd[4], 4, sp, st, rx);
+      wall_face(cur.z - st.wall[2], 2, c.vi, c.voli, P.rho, f, st.spd[2], 2, sp, st, rx);
+      wall_face(cur.z - st.wall[5], 2, c.vi, c.voli, P.rho, f, st.spd[5], 5, sp, st, rx);
     }
-    if (ext) {
+    if (c.ext) {
       D3 ex = ld3(v.ext, n, C3);
       if (sp.gradient_extforce) ex = st.extf_scale * ex;
       f = f + ex;
     }
   }
   if (st.torque) {
-    const double *c = v.centroid + 3 * (uint64_t)k;
-    D3 r = (pi + di) - d3(c[0], c[1], c[2]);
+    const double *cc = v.centroid + 3 * (uint64_t)c.k;
+    D3 r = (c.pi + c.di) - d3(cc[0], cc[1], cc[2]);
     double rn = norm3(r);
     double r_inv = (rn != 0.0 ? 1 / rn : 0);
     const int ta = (int)P.taxis;
@@ -135,44 +203,86 @@ __device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
     }
     f = f + (r_inv * P.tval) * perp;
   }
-  if (nc && P.stoppable && (!sp.nl_bdry_only || bdry_i)) {
+}
+
+// FP64 non-bond force density of node n in the reference's order: self-contact
+// (timeloop.h:554-557), walls (contact.h:1060-1124), external force and torque
+// (timeloop.h:582-633), then contact with the other particles in ascending partner order
+// (timeloop.h:637-651). Kept out of line: the bond kernel calls it only for nodes that need it.
+__device__ __noinline__ D3 extra_force(const DevView &v, uint64_t n) {
+  const DevPart &P = v.parts[v.pid[n]];
+  const DevSimParams &sp = v.sp[P.sim];
+  DevSimState &st = v.ss[P.sim];
+  const ExtraCtx c = extra_ctx(v, n, P, sp);
+  D3 f = d3(0.0, 0.0, 0.0);
+  if (c.mov && c.nc && st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || c.bdry_i)) {
     CandWalk walk(v, n);
     uint32_t m;
     while (walk.next(m)) {
-      if (m >= P.g0 && m < P.g0 + P.n) continue;
-      const uint32_t km = v.pid[m];
-      const uint32_t a = km < k ? km : k, b = km < k ? k : km;
-      if (!(v.parts[a].movable || v.parts[b].movable)) continue;
-      if (!intersects_fext(v.lrtb + 6 * (uint64_t)a, v.lrtb + 6 * (uint64_t)b, sp.Rc)) continue;
-      if (sp.nl_bdry_only && !v.bdry[m]) continue;
-      const D3 pm = ld3(v.pos, m, C3), dm = ld3(v.disp, m, C3);
-      if (km > k) {
-        D3 dir = (dm - di) + (pm - pi);
-        const double q = sq3(dir);
-        if (q >= sp.rc2_far) continue;
-        double dn = sqrt(q);
-        if (!(dn < sp.Rc)) continue;
-        PairForce pf;
-        pair_force(dir, dn, sp.Rc, sp.sc, v.vol[m], P.rho, vi, ld3(v.vel_in, m, C3), sp, st, pf);
-        f = f + pf.fc;
-        if (pf.has_fd) f = f + pf.fd;
-        if (pf.has_ff) f = f + pf.ff;
-        if (v.stats) atomicAdd(&v.cnt->contacts, 1ull);
-      } else {
-        D3 dir = (di - dm) + (pi - pm);
-        const double q = sq3(dir);
-        if (q >= sp.rc2_far) continue;
-        double dn = sqrt(q);
-        if (!(dn < sp.Rc)) continue;
-        const double volm = v.vol[m];
-        PairForce pf;
-        pair_force(dir, dn, sp.Rc, sp.sc, voli, v.parts[km].rho, ld3(v.vel_in, m, C3), vi, sp, st, pf);
-        f = f - (pf.fc / voli) * volm;
-        if (pf.has_fd) f = f - (pf.fd / sqrt(voli)) * sqrt(volm);
-        if (pf.has_ff) f = f - pf.ff;
-      }
+      if (m < P.g0) continue;
+      if (m >= P.g0 + P.n) break;
+      apply_share(f, cand_share(v, n, P, sp, st, c, m, true), c.voli);
     }
   }
+  extra_middle(v, n, P, sp, st, c, f);
+  if (c.nc && P.stoppable && (!sp.nl_bdry_only || c.bdry_i)) {
+    CandWalk walk(v, n);
+    uint32_t m;
+    while (walk.next(m)) apply_share(f, cand_share(v, n, P, sp, st, c, m, false), c.voli);
+  }
+  return f;
+}
+
+// Lane src's share, all lanes of mask gm taking part.
+__device__ __forceinline__ CandShare shfl_share(const CandShare &s, uint32_t src, unsigned gm) {
+  CandShare o;
+  o.pf.fc = d3(__shfl_sync(gm, s.pf.fc.x, src), __shfl_sync(gm, s.pf.fc.y, src), __shfl_sync(gm, s.pf.fc.z, src));
+  o.pf.fd = d3(__shfl_sync(gm, s.pf.fd.x, src), __shfl_sync(gm, s.pf.fd.y, src), __shfl_sync(gm, s.pf.fd.z, src));
+  o.pf.ff = d3(__shfl_sync(gm, s.pf.ff.x, src), __shfl_sync(gm, s.pf.ff.y, src), __shfl_sync(gm, s.pf.ff.z, src));
+  o.volm = __shfl_sync(gm, s.volm, src);
+  const int bits = __shfl_sync(gm, s.kind | (s.pf.has_fd ? 4 : 0) | (s.pf.has_ff ? 8 : 0), src);
+  o.kind = bits & 3;
+  o.pf.has_fd = (bits & 4) != 0;
+  o.pf.has_ff = (bits & 8) != 0;
+  return o;
+}
+
+// extra_force by the L lanes of node n (lanes first .. first + L - 1 of the warp, all calling it
+// with the same n; the result is valid on lane first) for a node whose candidates are a list:
+// the candidates are dealt over the lanes, each computing its candidates' shares with
+// cand_share, and lane first adds them in list order with apply_share, so the sum is
+// extra_force's bit for bit. A node in contact no longer evaluates its pairs one after another
+// on one lane while the node's other lanes wait (each pair is a chain of FP64 square roots and
+// divisions).
+template <int L>
+__device__ __noinline__ D3 extra_force_lanes(const DevView &v, uint64_t n, uint32_t sub, uint32_t first) {
+  const unsigned gm = ((1u << L) - 1u) << first;
+  const DevPart &P = v.parts[v.pid[n]];
+  const DevSimParams &sp = v.sp[P.sim];
+  DevSimState &st = v.ss[P.sim];
+  const ExtraCtx c = extra_ctx(v, n, P, sp);
+  const uint32_t *cl = v.cand + n * v.cand_cap;
+  const int ncand = (int)v.cand_n[n];
+  D3 f = d3(0.0, 0.0, 0.0);
+  auto loop = [&](bool self) {
+    for (int i0 = 0; i0 < ncand; i0 += L) {
+      const int i = i0 + (int)sub;
+      CandShare s;
+      s.pf.fc = s.pf.fd = s.pf.ff = d3(0.0, 0.0, 0.0);
+      s.pf.has_fd = s.pf.has_ff = false;
+      s.volm = 0.0;
+      s.kind = 0;
+      if (i < ncand) s = cand_share(v, n, P, sp, st, c, cl[i], self);
+      for (int j = 0; j < L && i0 + j < ncand; ++j) {
+        const CandShare t = shfl_share(s, first + (uint32_t)j, gm);
+        if (sub == 0) apply_share(f, t, c.voli);
+      }
+    }
+  };
+  if (c.mov && c.nc && st.fracture && P.breakable && st.self_contact && (!sp.nl_bdry_only || c.bdry_i))
+    loop(true);
+  if (sub == 0) extra_middle(v, n, P, sp, st, c, f);
+  if (c.nc && P.stoppable && (!sp.nl_bdry_only || c.bdry_i)) loop(false);
   return f;
 }
 
@@ -782,11 +892,20 @@ __device__ __forceinline__ void bond_node_split(const DevView &v, uint64_t t) {
   D3 f = d3(0.0, 0.0, 0.0);
   if (lead) {
     f = acc_value(tot);
-    if (FX) {
-      if (extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4)) f = f + extra_force(v, nn);
-    } else if (v.extra_flag[nn]) {
+    if (!FX && v.extra_flag[nn]) {
       f = f + ld3(v.f_extra, nn, C3);
       v.extra_flag[nn] = 0;
+    }
+  }
+  if (FX) {  // FP64 non-bond work: a node's lanes share its listed contact candidates
+    const bool need = __shfl_sync(full, lead && extra_needed(v, nn, k, P, v.sp[P.sim], st, pi4, ui4), first);
+    if (need) {
+      if (v.cand_n[nn] == kCandCells) {  // the cell walk: one lane
+        if (lead) f = f + extra_force(v, nn);
+      } else {
+        const D3 e = extra_force_lanes<L>(v, nn, sub, first);
+        if (lead) f = f + e;
+      }
     }
   }
   verlet_tail(v, nn, k, P, st, lead, f, pi4, ui4);
